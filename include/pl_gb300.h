@@ -1,0 +1,178 @@
+/*
+ * pl_gb300.h — C ABI of the GB300 (sm_103a) state-vector backend.
+ *
+ * This is the drop-in boundary for lightning.qubit's hot path: the entry
+ * points are what the reference's Python binding module
+ * (`lightning_qubit_ops`, built from
+ *  pennylane_lightning/core/bindings/Bindings.hpp and
+ *  pennylane_lightning/core/simulators/lightning_qubit/bindings/LQubitBindings.hpp)
+ * binds, flattened to plain pointers and sizes.  The reference paths cited
+ * below are relative to the reference project root.
+ *
+ * Conventions
+ *   - Every function returns PLGB_OK (0) or a non-zero status; the message of
+ *     the last failure on the calling thread is returned by plgb_last_error().
+ *     (Reference: PL_ABORT -> LightningException, core/utils/Error.hpp:23-65.)
+ *   - precision is 64 (complex64, float pairs) or 128 (complex128).
+ *   - Host state buffers are interleaved (re, im) arrays in the handle's
+ *     precision; matrices, coefficients and parameters are passed as
+ *     interleaved complex128 / double and converted to the handle's precision
+ *     (as the reference's binding converts numpy arrays to PrecisionT).
+ *   - Wire w is bit (n-1-w) of the amplitude index; within a k-wire matrix the
+ *     first listed wire is the most significant bit of the local index.
+ *   - Gate application is asynchronous on the state vector's CUDA stream;
+ *     every call that returns data to the host synchronizes first.
+ *   - There is no CPU fallback: when no CUDA device is present, creating a
+ *     state vector fails with PLGB_ERR_CUDA.
+ */
+#ifndef PL_GB300_H
+#define PL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PLGB_OK 0
+#define PLGB_ERR_INVALID 1    /* bad argument (wires, sizes, names) */
+#define PLGB_ERR_CUDA 2       /* CUDA runtime failure or no device */
+#define PLGB_ERR_UNSUPPORTED 3
+#define PLGB_ERR_INTERNAL 4
+
+typedef struct plgb_sv plgb_sv;   /* StateVectorLQubitManaged<T> counterpart */
+typedef struct plgb_obs plgb_obs; /* Observable<SV> counterpart */
+typedef struct plgb_ops plgb_ops; /* OpsData<SV> counterpart */
+
+/* ---- module level (Bindings.hpp:284-367, LQubitBindings.hpp:464-475) ---- */
+const char *plgb_last_error(void);
+/* JSON text: {"NAME": "lightning.gb300", ...}; backend_info() */
+int plgb_backend_info(char *buf, size_t len);
+/* JSON text with CUDA device / compile details; compile_info(), runtime_info() */
+int plgb_runtime_info(char *buf, size_t len);
+int plgb_device_count(int *out);
+
+/* ---- state vector (StateVectorLQubitManaged.hpp:52-188,
+ *      StateVectorLQubit.hpp:359-1036, Bindings.hpp:870-922,
+ *      LQubitBindings.hpp:178-243) ---- */
+/* StateVectorC64/C128.__init__(num_qubits): |0...0> */
+int plgb_sv_create(int num_qubits, int precision, plgb_sv **out);
+/* StateVectorLQubitRaw counterpart: wraps caller-owned DEVICE memory of
+ * 2^num_qubits amplitudes (not freed by plgb_sv_destroy) */
+int plgb_sv_create_raw(void *device_data, int num_qubits, int precision, plgb_sv **out);
+/* deep copy (StateVectorLQubitManaged copy constructor) */
+int plgb_sv_clone(const plgb_sv *src, plgb_sv **out);
+int plgb_sv_destroy(plgb_sv *sv);
+int plgb_sv_num_qubits(const plgb_sv *sv, int *out);
+int plgb_sv_precision(const plgb_sv *sv, int *out);
+/* __len__ / size */
+int plgb_sv_length(const plgb_sv *sv, uint64_t *out);
+int plgb_sv_device_ptr(plgb_sv *sv, void **out);
+int plgb_sv_synchronize(plgb_sv *sv);
+/* resetStateVector (StateVectorLQubit.hpp:959-963) */
+int plgb_sv_reset(plgb_sv *sv);
+/* setBasisState(state, wires) (StateVectorLQubit.hpp:939-957) */
+int plgb_sv_set_basis_state(plgb_sv *sv, const int64_t *bits, const int64_t *wires, int nw);
+/* setStateVector(state, wires) (StateVectorLQubit.hpp:971-1036); len = 2^nw */
+int plgb_sv_set_state_vector(plgb_sv *sv, const void *host_state, uint64_t len, const int64_t *wires, int nw);
+/* updateData(ndarray) (LQubitBindings.hpp:183-196) */
+int plgb_sv_update_data(plgb_sv *sv, const void *host_data, uint64_t len);
+/* getState(out_ndarray) (LQubitBindings.hpp:227-243) */
+int plgb_sv_get_state(const plgb_sv *sv, void *host_out, uint64_t len);
+/* per-gate methods: st.<Name>(wires, inverse, params) (Bindings.hpp:223-234,
+ * StateVectorLQubit.hpp:378-391) */
+int plgb_sv_apply_operation(plgb_sv *sv, const char *name, const int64_t *wires, int nw, int inverse,
+                            const double *params, int np);
+/* controlled per-gate methods: st.<Name>(cwires, cvals, wires, inverse, params)
+ * (Bindings.hpp:256-276, StateVectorLQubit.hpp:404-424) */
+int plgb_sv_apply_controlled_operation(plgb_sv *sv, const char *name, const int64_t *cwires, const uint8_t *cvals,
+                                       int ncw, const int64_t *wires, int nw, int inverse, const double *params,
+                                       int np);
+/* applyMatrix(matrix, wires, inverse) (Bindings.hpp:153-165,
+ * StateVectorLQubit.hpp:674-710); matrix: 4^nw interleaved complex128 */
+int plgb_sv_apply_matrix(plgb_sv *sv, const double *matrix, const int64_t *wires, int nw, int inverse);
+/* applyControlledMatrix (Bindings.hpp:177-200, StateVectorLQubit.hpp:571-622) */
+int plgb_sv_apply_controlled_matrix(plgb_sv *sv, const double *matrix, const int64_t *cwires, const uint8_t *cvals,
+                                    int ncw, const int64_t *wires, int nw, int inverse);
+/* applySparseMatrix / applyControlledSparseMatrix (LQubitBindings.hpp:150-175,
+ * StateVectorLQubit.hpp:724-870); local CSR operator on `wires` */
+int plgb_sv_apply_sparse_matrix(plgb_sv *sv, const int64_t *indptr, const int64_t *indices, const double *data,
+                                int64_t nnz, const int64_t *cwires, const uint8_t *cvals, int ncw,
+                                const int64_t *wires, int nw);
+/* applyPauliRot(wires, inverse, params, word) (LQubitBindings.hpp:198-207,
+ * GateImplementationsLM.hpp:577-629) */
+int plgb_sv_apply_pauli_rot(plgb_sv *sv, const int64_t *wires, int nw, int inverse, double angle, const char *word);
+/* applyGenerator, plain and controlled (StateVectorLQubit.hpp:527-560);
+ * writes the generator's scaling factor */
+int plgb_sv_apply_generator(plgb_sv *sv, const char *name, const int64_t *cwires, const uint8_t *cvals, int ncw,
+                            const int64_t *wires, int nw, int adj, double *scale_out);
+/* collapse(wire, branch) / normalize() (StateVectorLQubit.hpp:881-921) */
+int plgb_sv_collapse(plgb_sv *sv, int64_t wire, int branch);
+int plgb_sv_normalize(plgb_sv *sv);
+
+/* ---- measurements (MeasurementsLQubit.hpp:73-768, Bindings.hpp:651-688,
+ *      LQubitBindings.hpp:262-349) ---- */
+/* probs() (nw < 0) / probs(wires); out holds 2^nw (or 2^n) doubles */
+int plgb_meas_probs(plgb_sv *sv, const int64_t *wires, int nw, double *out);
+/* expval(name, wires) */
+int plgb_meas_expval_named(plgb_sv *sv, const char *name, const int64_t *wires, int nw, double *out);
+/* expval(matrix, wires) */
+int plgb_meas_expval_matrix(plgb_sv *sv, const double *matrix, const int64_t *wires, int nw, double *out);
+/* expval(row_map, col_idx, values) over the full register */
+int plgb_meas_expval_sparse(plgb_sv *sv, const int64_t *indptr, int64_t nptr, const int64_t *indices,
+                            const double *data, int64_t nnz, double *out);
+/* expval(obs) / var(obs) */
+int plgb_meas_expval_obs(plgb_sv *sv, const plgb_obs *obs, double *out);
+int plgb_meas_var_obs(plgb_sv *sv, const plgb_obs *obs, double *out);
+/* var(name, wires), var(matrix, wires), var(row_map, col_idx, values) */
+int plgb_meas_var_named(plgb_sv *sv, const char *name, const int64_t *wires, int nw, double *out);
+int plgb_meas_var_matrix(plgb_sv *sv, const double *matrix, const int64_t *wires, int nw, double *out);
+int plgb_meas_var_sparse(plgb_sv *sv, const int64_t *indptr, int64_t nptr, const int64_t *indices,
+                         const double *data, int64_t nnz, double *out);
+/* generate_samples(wires, shots) / generate_samples(num_wires, shots) (nw < 0)
+ * with set_random_seed(seed) (MeasurementsLQubit.hpp:646-679,
+ * MeasurementsBase.hpp:77-93); out holds shots * nw int64 bits, last wire
+ * fastest */
+int plgb_meas_generate_samples(plgb_sv *sv, const int64_t *wires, int nw, int64_t shots, uint64_t seed,
+                               int64_t *out);
+
+/* ---- observables (Bindings.hpp:467-591, LQubitBindings.hpp:358-407) ---- */
+/* NamedObsC*(name, wires) */
+int plgb_obs_named(const char *name, const int64_t *wires, int nw, plgb_obs **out);
+/* HermitianObsC*(matrix, wires); matrix: 4^nw interleaved complex128 */
+int plgb_obs_hermitian(const double *matrix, const int64_t *wires, int nw, plgb_obs **out);
+/* TensorProdObsC*(list) */
+int plgb_obs_tensor_prod(plgb_obs *const *obs, int n, plgb_obs **out);
+/* HamiltonianC*(coeffs, list) */
+int plgb_obs_hamiltonian(const double *coeffs, plgb_obs *const *obs, int n, plgb_obs **out);
+/* SparseHamiltonianC*(data, indices, indptr, wires) */
+int plgb_obs_sparse_hamiltonian(const double *data, const int64_t *indices, int64_t nnz, const int64_t *indptr,
+                                int64_t nptr, const int64_t *wires, int nw, plgb_obs **out);
+int plgb_obs_destroy(plgb_obs *obs);
+/* get_wires(): writes up to cap wires, *nw = total */
+int plgb_obs_wires(const plgb_obs *obs, int64_t *wires, int cap, int *nw);
+/* __repr__ */
+int plgb_obs_repr(const plgb_obs *obs, char *buf, size_t len);
+
+/* ---- algorithms (Bindings.hpp:704-851, JacobianData.hpp:39-393,
+ *      AdjointJacobianLQubit.hpp:347-491) ---- */
+/* OpsStructC*(names, params, wires, inverses, matrices, cwires, cvals) /
+ * create_ops_listC*: flattened with per-op counts; mat_sizes[k] = number of
+ * complex entries of op k's matrix (0 when none) */
+int plgb_ops_create(int nops, const char *const *names, const double *params, const int *nparams,
+                    const int64_t *wires, const int *nwires, const uint8_t *inverses, const double *mats,
+                    const int64_t *mat_sizes, const int64_t *cwires, const int *ncwires, const uint8_t *cvals,
+                    plgb_ops **out);
+int plgb_ops_destroy(plgb_ops *ops);
+int plgb_ops_num_par_ops(const plgb_ops *ops, int *out);
+/* AdjointJacobianC*.__call__(sv, observables, ops, trainable_params):
+ * jac_out holds nobs * ntp doubles, row-major [obs][param].  With apply_ops
+ * the operations are first applied to a copy of the state. */
+int plgb_adjoint_jacobian(plgb_sv *sv, plgb_obs *const *obs, int nobs, const plgb_ops *ops, const int64_t *trainable,
+                          int ntp, int apply_ops, double *jac_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PL_GB300_H */

@@ -1,0 +1,588 @@
+// extern "C" boundary (include/pl_gb300.h) over the C++ host layer.
+#include "pl_gb300.h"
+
+#include "host.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <sstream>
+#include <variant>
+
+using namespace plgb;
+
+struct plgb_sv {
+    int precision;
+    std::unique_ptr<StateVector<float>> f;
+    std::unique_ptr<StateVector<double>> d;
+};
+struct plgb_obs {
+    ObsPtr node;
+};
+struct plgb_ops {
+    OpsList list;
+};
+
+namespace {
+
+int fail(int code, const std::string &msg) {
+    set_last_error(msg);
+    return code;
+}
+
+template <class F> int guard(F &&f) {
+    try {
+        f();
+        return PLGB_OK;
+    } catch (const PLError &e) {
+        return fail(PLGB_ERR_INVALID, e.what());
+    } catch (const std::bad_alloc &) {
+        return fail(PLGB_ERR_CUDA, "out of memory");
+    } catch (const std::runtime_error &e) {
+        const std::string w = e.what();
+        return fail(w.find("cuda") != std::string::npos || w.find("CUDA") != std::string::npos ||
+                            w.find("launch") != std::string::npos || w.find("cudaMalloc") != std::string::npos
+                        ? PLGB_ERR_CUDA
+                        : PLGB_ERR_INTERNAL,
+                    w);
+    } catch (const std::exception &e) {
+        return fail(PLGB_ERR_INTERNAL, e.what());
+    }
+}
+
+void need(const void *p, const char *what) {
+    if (p == nullptr) {
+        throw PLError(std::string("null pointer: ") + what);
+    }
+}
+
+template <class F> int with_sv(plgb_sv *sv, F &&f) {
+    return guard([&] {
+        need(sv, "state vector");
+        if (sv->precision == 128) {
+            f(*sv->d);
+        } else {
+            f(*sv->f);
+        }
+    });
+}
+
+std::vector<int64_t> vec(const int64_t *p, int n) {
+    if (n > 0) {
+        need(p, "wires");
+    }
+    return n > 0 ? std::vector<int64_t>(p, p + n) : std::vector<int64_t>{};
+}
+std::vector<bool> bvec(const uint8_t *p, int n) {
+    std::vector<bool> v;
+    if (n > 0) {
+        need(p, "control values");
+    }
+    for (int i = 0; i < n; i++) {
+        v.push_back(p[i] != 0);
+    }
+    return v;
+}
+std::vector<cd> cmat(const double *p, size_t n) {
+    need(p, "matrix");
+    std::vector<cd> m(n);
+    for (size_t i = 0; i < n; i++) {
+        m[i] = {p[2 * i], p[2 * i + 1]};
+    }
+    return m;
+}
+std::vector<double> dvec(const double *p, int n) {
+    if (n > 0) {
+        need(p, "params");
+    }
+    return n > 0 ? std::vector<double>(p, p + n) : std::vector<double>{};
+}
+
+int copy_text(const std::string &s, char *buf, size_t len) {
+    if (!buf || len == 0) {
+        return fail(PLGB_ERR_INVALID, "null buffer");
+    }
+    const size_t k = std::min(len - 1, s.size());
+    std::memcpy(buf, s.data(), k);
+    buf[k] = '\0';
+    return s.size() + 1 > len ? fail(PLGB_ERR_INVALID, "buffer too small") : PLGB_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+const char *plgb_last_error(void) { return last_error(); }
+
+int plgb_device_count(int *out) {
+    return guard([&] {
+        need(out, "out");
+        int c = 0;
+        if (cudaGetDeviceCount(&c) != cudaSuccess) {
+            c = 0;
+        }
+        *out = c;
+    });
+}
+
+int plgb_backend_info(char *buf, size_t len) {
+    return copy_text("{\"NAME\": \"lightning.gb300\", \"ARCH\": \"sm_103a\", \"REFERENCE\": \"lightning.qubit\"}", buf,
+                     len);
+}
+
+int plgb_runtime_info(char *buf, size_t len) {
+    std::ostringstream os;
+    int dev = -1, rt = 0, drv = 0, count = 0;
+    cudaRuntimeGetVersion(&rt);
+    cudaDriverGetVersion(&drv);
+    if (cudaGetDeviceCount(&count) != cudaSuccess) {
+        count = 0;
+    }
+    os << "{\"cuda_runtime\": " << rt << ", \"cuda_driver\": " << drv << ", \"device_count\": " << count;
+    if (count > 0 && cudaGetDevice(&dev) == cudaSuccess) {
+        cudaDeviceProp p{};
+        if (cudaGetDeviceProperties(&p, dev) == cudaSuccess) {
+            os << ", \"device\": \"" << p.name << "\", \"sm\": " << p.major << p.minor
+               << ", \"multiprocessors\": " << p.multiProcessorCount << ", \"global_mem\": " << p.totalGlobalMem;
+        }
+    }
+    os << ", \"compiled_for\": \"sm_103a\", \"cuda_compiled\": " << CUDART_VERSION << "}";
+    return copy_text(os.str(), buf, len);
+}
+
+// ---- state vector ---------------------------------------------------------
+int plgb_sv_create(int num_qubits, int precision, plgb_sv **out) {
+    return guard([&] {
+        need(out, "out");
+        PLGB_REQUIRE(precision == 64 || precision == 128, "precision must be 64 or 128");
+        PLGB_REQUIRE(num_qubits >= 0 && num_qubits <= 36, "num_qubits must be in [0, 36]");
+        int count = 0;
+        if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+            throw std::runtime_error("CUDA: no GPU available (the GB300 backend has no CPU fallback)");
+        }
+        auto h = std::make_unique<plgb_sv>();
+        h->precision = precision;
+        if (precision == 128) {
+            h->d = std::make_unique<StateVector<double>>(num_qubits);
+        } else {
+            h->f = std::make_unique<StateVector<float>>(num_qubits);
+        }
+        *out = h.release();
+    });
+}
+
+int plgb_sv_create_raw(void *device_data, int num_qubits, int precision, plgb_sv **out) {
+    return guard([&] {
+        need(out, "out");
+        need(device_data, "device data");
+        PLGB_REQUIRE(precision == 64 || precision == 128, "precision must be 64 or 128");
+        auto h = std::make_unique<plgb_sv>();
+        h->precision = precision;
+        if (precision == 128) {
+            h->d = std::make_unique<StateVector<double>>(static_cast<cx<double> *>(device_data), num_qubits);
+        } else {
+            h->f = std::make_unique<StateVector<float>>(static_cast<cx<float> *>(device_data), num_qubits);
+        }
+        *out = h.release();
+    });
+}
+
+int plgb_sv_clone(const plgb_sv *src, plgb_sv **out) {
+    return guard([&] {
+        need(src, "source");
+        need(out, "out");
+        auto h = std::make_unique<plgb_sv>();
+        h->precision = src->precision;
+        if (src->precision == 128) {
+            h->d = std::make_unique<StateVector<double>>(src->d->num_qubits());
+            h->d->copy_from(*src->d);
+        } else {
+            h->f = std::make_unique<StateVector<float>>(src->f->num_qubits());
+            h->f->copy_from(*src->f);
+        }
+        *out = h.release();
+    });
+}
+
+int plgb_sv_destroy(plgb_sv *sv) {
+    return guard([&] { delete sv; });
+}
+int plgb_sv_num_qubits(const plgb_sv *sv, int *out) {
+    return with_sv(const_cast<plgb_sv *>(sv), [&](auto &s) {
+        need(out, "out");
+        *out = s.num_qubits();
+    });
+}
+int plgb_sv_precision(const plgb_sv *sv, int *out) {
+    return guard([&] {
+        need(sv, "sv");
+        need(out, "out");
+        *out = sv->precision;
+    });
+}
+int plgb_sv_length(const plgb_sv *sv, uint64_t *out) {
+    return with_sv(const_cast<plgb_sv *>(sv), [&](auto &s) {
+        need(out, "out");
+        *out = s.length();
+    });
+}
+int plgb_sv_device_ptr(plgb_sv *sv, void **out) {
+    return with_sv(sv, [&](auto &s) {
+        need(out, "out");
+        *out = s.data();
+    });
+}
+int plgb_sv_synchronize(plgb_sv *sv) {
+    return with_sv(sv, [&](auto &s) { s.synchronize(); });
+}
+int plgb_sv_reset(plgb_sv *sv) {
+    return with_sv(sv, [&](auto &s) { s.reset(); });
+}
+int plgb_sv_set_basis_state(plgb_sv *sv, const int64_t *bits, const int64_t *wires, int nw) {
+    return with_sv(sv, [&](auto &s) { s.set_basis_state(vec(bits, nw), vec(wires, nw)); });
+}
+int plgb_sv_set_state_vector(plgb_sv *sv, const void *host_state, uint64_t len, const int64_t *wires, int nw) {
+    return with_sv(sv, [&](auto &s) {
+        need(host_state, "state");
+        using T = std::remove_reference_t<decltype(*s.data())>;
+        using R = decltype(T{}.x);
+        s.reset();
+        s.set_state_vector(static_cast<const std::complex<R> *>(host_state), len, vec(wires, nw));
+    });
+}
+int plgb_sv_update_data(plgb_sv *sv, const void *host_data, uint64_t len) {
+    return with_sv(sv, [&](auto &s) {
+        need(host_data, "data");
+        using T = std::remove_reference_t<decltype(*s.data())>;
+        using R = decltype(T{}.x);
+        s.update_data(static_cast<const std::complex<R> *>(host_data), len);
+    });
+}
+int plgb_sv_get_state(const plgb_sv *sv, void *host_out, uint64_t len) {
+    return with_sv(const_cast<plgb_sv *>(sv), [&](auto &s) {
+        need(host_out, "out");
+        using T = std::remove_reference_t<decltype(*s.data())>;
+        using R = decltype(T{}.x);
+        s.get_state(static_cast<std::complex<R> *>(host_out), len);
+    });
+}
+int plgb_sv_apply_operation(plgb_sv *sv, const char *name, const int64_t *wires, int nw, int inverse,
+                            const double *params, int np) {
+    return with_sv(sv, [&](auto &s) {
+        need(name, "name");
+        s.apply_operation(name, vec(wires, nw), inverse != 0, dvec(params, np));
+    });
+}
+int plgb_sv_apply_controlled_operation(plgb_sv *sv, const char *name, const int64_t *cwires, const uint8_t *cvals,
+                                       int ncw, const int64_t *wires, int nw, int inverse, const double *params,
+                                       int np) {
+    return with_sv(sv, [&](auto &s) {
+        need(name, "name");
+        s.apply_controlled_operation(name, vec(cwires, ncw), bvec(cvals, ncw), vec(wires, nw), inverse != 0,
+                                     dvec(params, np));
+    });
+}
+int plgb_sv_apply_matrix(plgb_sv *sv, const double *matrix, const int64_t *wires, int nw, int inverse) {
+    return with_sv(sv, [&](auto &s) {
+        PLGB_REQUIRE(nw >= 1 && nw <= 12, "Number of wires must be larger than 0 (and at most 12)");
+        const auto m = cmat(matrix, size_t{1} << (2 * nw));
+        s.apply_matrix(m.data(), vec(wires, nw), inverse != 0);
+    });
+}
+int plgb_sv_apply_controlled_matrix(plgb_sv *sv, const double *matrix, const int64_t *cwires, const uint8_t *cvals,
+                                    int ncw, const int64_t *wires, int nw, int inverse) {
+    return with_sv(sv, [&](auto &s) {
+        PLGB_REQUIRE(nw >= 1 && nw <= 12, "Number of wires must be larger than 0 (and at most 12)");
+        const auto m = cmat(matrix, size_t{1} << (2 * nw));
+        s.apply_matrix(m.data(), vec(wires, nw), inverse != 0, vec(cwires, ncw), bvec(cvals, ncw));
+    });
+}
+int plgb_sv_apply_sparse_matrix(plgb_sv *sv, const int64_t *indptr, const int64_t *indices, const double *data,
+                                int64_t nnz, const int64_t *cwires, const uint8_t *cvals, int ncw,
+                                const int64_t *wires, int nw) {
+    return with_sv(sv, [&](auto &s) {
+        need(indptr, "indptr");
+        PLGB_REQUIRE(nw >= 1 && nw <= 12, "Number of wires must be larger than 0 (and at most 12)");
+        const auto d = cmat(nnz > 0 ? data : reinterpret_cast<const double *>(indptr), static_cast<size_t>(nnz));
+        s.apply_sparse_matrix(indptr, indices, d.data(), nnz, vec(wires, nw), vec(cwires, ncw), bvec(cvals, ncw));
+    });
+}
+int plgb_sv_apply_pauli_rot(plgb_sv *sv, const int64_t *wires, int nw, int inverse, double angle, const char *word) {
+    return with_sv(sv, [&](auto &s) {
+        need(word, "word");
+        s.apply_pauli_rot(vec(wires, nw), inverse != 0, angle, word);
+    });
+}
+int plgb_sv_apply_generator(plgb_sv *sv, const char *name, const int64_t *cwires, const uint8_t *cvals, int ncw,
+                            const int64_t *wires, int nw, int adj, double *scale_out) {
+    (void)adj;
+    return with_sv(sv, [&](auto &s) {
+        need(name, "name");
+        need(scale_out, "scale_out");
+        *scale_out = s.apply_generator(name, vec(cwires, ncw), bvec(cvals, ncw), vec(wires, nw));
+    });
+}
+int plgb_sv_collapse(plgb_sv *sv, int64_t wire, int branch) {
+    return with_sv(sv, [&](auto &s) { s.collapse(wire, branch != 0); });
+}
+int plgb_sv_normalize(plgb_sv *sv) {
+    return with_sv(sv, [&](auto &s) { s.normalize(); });
+}
+
+// ---- measurements ------------------------------------------------------------
+int plgb_meas_probs(plgb_sv *sv, const int64_t *wires, int nw, double *out) {
+    return with_sv(sv, [&](auto &s) {
+        need(out, "out");
+        using T = decltype(s.data()->x);
+        const auto p = Measure<T>::probs(s, nw < 0 ? std::vector<int64_t>{} : vec(wires, nw), nw < 0);
+        std::memcpy(out, p.data(), p.size() * sizeof(double));
+    });
+}
+int plgb_meas_expval_named(plgb_sv *sv, const char *name, const int64_t *wires, int nw, double *out) {
+    return with_sv(sv, [&](auto &s) {
+        need(out, "out");
+        need(name, "name");
+        using T = decltype(s.data()->x);
+        *out = Measure<T>::expval_named(s, name, vec(wires, nw));
+    });
+}
+int plgb_meas_expval_matrix(plgb_sv *sv, const double *matrix, const int64_t *wires, int nw, double *out) {
+    return with_sv(sv, [&](auto &s) {
+        need(out, "out");
+        PLGB_REQUIRE(nw >= 1 && nw <= 12, "Number of wires must be larger than 0 (and at most 12)");
+        using T = decltype(s.data()->x);
+        const auto m = cmat(matrix, size_t{1} << (2 * nw));
+        *out = Measure<T>::expval_matrix(s, m.data(), vec(wires, nw));
+    });
+}
+int plgb_meas_expval_sparse(plgb_sv *sv, const int64_t *indptr, int64_t nptr, const int64_t *indices,
+                            const double *data, int64_t nnz, double *out) {
+    return with_sv(sv, [&](auto &s) {
+        need(out, "out");
+        need(indptr, "indptr");
+        using T = decltype(s.data()->x);
+        const auto d = cmat(data, static_cast<size_t>(nnz));
+        *out = Measure<T>::expval_sparse(s, indptr, nptr, indices, d.data(), nnz);
+    });
+}
+int plgb_meas_var_sparse(plgb_sv *sv, const int64_t *indptr, int64_t nptr, const int64_t *indices,
+                         const double *data, int64_t nnz, double *out) {
+    return with_sv(sv, [&](auto &s) {
+        need(out, "out");
+        need(indptr, "indptr");
+        using T = decltype(s.data()->x);
+        const auto d = cmat(data, static_cast<size_t>(nnz));
+        *out = Measure<T>::var_sparse(s, indptr, nptr, indices, d.data(), nnz);
+    });
+}
+int plgb_meas_expval_obs(plgb_sv *sv, const plgb_obs *obs, double *out) {
+    return with_sv(sv, [&](auto &s) {
+        need(obs, "observable");
+        need(out, "out");
+        using T = decltype(s.data()->x);
+        *out = Measure<T>::expval_obs(s, *obs->node);
+    });
+}
+int plgb_meas_var_obs(plgb_sv *sv, const plgb_obs *obs, double *out) {
+    return with_sv(sv, [&](auto &s) {
+        need(obs, "observable");
+        need(out, "out");
+        using T = decltype(s.data()->x);
+        *out = Measure<T>::var_obs(s, *obs->node);
+    });
+}
+int plgb_meas_var_named(plgb_sv *sv, const char *name, const int64_t *wires, int nw, double *out) {
+    return with_sv(sv, [&](auto &s) {
+        need(out, "out");
+        need(name, "name");
+        using T = decltype(s.data()->x);
+        ObsNode o;
+        o.kind = ObsNode::Named;
+        o.name = name;
+        o.wires = vec(wires, nw);
+        *out = Measure<T>::var_obs(s, o);
+    });
+}
+int plgb_meas_var_matrix(plgb_sv *sv, const double *matrix, const int64_t *wires, int nw, double *out) {
+    return with_sv(sv, [&](auto &s) {
+        need(out, "out");
+        PLGB_REQUIRE(nw >= 1 && nw <= 12, "Number of wires must be larger than 0 (and at most 12)");
+        using T = decltype(s.data()->x);
+        ObsNode o;
+        o.kind = ObsNode::Herm;
+        o.mat = cmat(matrix, size_t{1} << (2 * nw));
+        o.wires = vec(wires, nw);
+        *out = Measure<T>::var_obs(s, o);
+    });
+}
+int plgb_meas_generate_samples(plgb_sv *sv, const int64_t *wires, int nw, int64_t shots, uint64_t seed,
+                               int64_t *out) {
+    return with_sv(sv, [&](auto &s) {
+        need(out, "out");
+        using T = decltype(s.data()->x);
+        std::vector<int64_t> w;
+        if (nw < 0) {
+            for (int i = 0; i < s.num_qubits(); i++) {
+                w.push_back(i);
+            }
+        } else {
+            w = vec(wires, nw);
+        }
+        const auto r = Measure<T>::samples(s, w, shots, seed);
+        std::memcpy(out, r.data(), r.size() * sizeof(int64_t));
+    });
+}
+
+// ---- observables --------------------------------------------------------------
+int plgb_obs_named(const char *name, const int64_t *wires, int nw, plgb_obs **out) {
+    return guard([&] {
+        need(name, "name");
+        need(out, "out");
+        const std::string n(name);
+        PLGB_REQUIRE(is_named_gate(n), "unknown observable name " + n);
+        auto o = std::make_shared<ObsNode>();
+        o->kind = ObsNode::Named;
+        o->name = n;
+        o->wires = vec(wires, nw);
+        *out = new plgb_obs{o};
+    });
+}
+int plgb_obs_hermitian(const double *matrix, const int64_t *wires, int nw, plgb_obs **out) {
+    return guard([&] {
+        need(out, "out");
+        PLGB_REQUIRE(nw >= 1 && nw <= 12, "Hermitian observables act on 1..12 wires");
+        auto o = std::make_shared<ObsNode>();
+        o->kind = ObsNode::Herm;
+        o->mat = cmat(matrix, size_t{1} << (2 * nw));
+        o->wires = vec(wires, nw);
+        *out = new plgb_obs{o};
+    });
+}
+int plgb_obs_tensor_prod(plgb_obs *const *obs, int n, plgb_obs **out) {
+    return guard([&] {
+        need(out, "out");
+        PLGB_REQUIRE(n >= 1, "a tensor product needs at least one observable");
+        auto o = std::make_shared<ObsNode>();
+        o->kind = ObsNode::Prod;
+        std::vector<int64_t> seen;
+        for (int i = 0; i < n; i++) {
+            need(obs[i], "observable");
+            for (auto w : obs[i]->node->all_wires()) {
+                PLGB_REQUIRE(std::find(seen.begin(), seen.end(), w) == seen.end(),
+                             "All wires in observables must be disjoint.");
+                seen.push_back(w);
+            }
+            o->children.push_back(obs[i]->node);
+        }
+        *out = new plgb_obs{o};
+    });
+}
+int plgb_obs_hamiltonian(const double *coeffs, plgb_obs *const *obs, int n, plgb_obs **out) {
+    return guard([&] {
+        need(out, "out");
+        auto o = std::make_shared<ObsNode>();
+        o->kind = ObsNode::Ham;
+        for (int i = 0; i < n; i++) {
+            need(obs[i], "observable");
+            o->children.push_back(obs[i]->node);
+            o->coeffs.push_back(coeffs[i]);
+        }
+        *out = new plgb_obs{o};
+    });
+}
+int plgb_obs_sparse_hamiltonian(const double *data, const int64_t *indices, int64_t nnz, const int64_t *indptr,
+                                int64_t nptr, const int64_t *wires, int nw, plgb_obs **out) {
+    return guard([&] {
+        need(out, "out");
+        need(indptr, "indptr");
+        auto o = std::make_shared<ObsNode>();
+        o->kind = ObsNode::Sparse;
+        o->sp_data = cmat(data, static_cast<size_t>(nnz));
+        o->sp_indices.assign(indices, indices + nnz);
+        o->sp_indptr.assign(indptr, indptr + nptr);
+        o->wires = vec(wires, nw);
+        *out = new plgb_obs{o};
+    });
+}
+int plgb_obs_destroy(plgb_obs *obs) {
+    return guard([&] { delete obs; });
+}
+int plgb_obs_wires(const plgb_obs *obs, int64_t *wires, int cap, int *nw) {
+    return guard([&] {
+        need(obs, "observable");
+        need(nw, "nw");
+        const auto w = obs->node->all_wires();
+        *nw = static_cast<int>(w.size());
+        for (int i = 0; i < cap && i < static_cast<int>(w.size()); i++) {
+            wires[i] = w[static_cast<size_t>(i)];
+        }
+    });
+}
+int plgb_obs_repr(const plgb_obs *obs, char *buf, size_t len) {
+    if (!obs) {
+        return fail(PLGB_ERR_INVALID, "null observable");
+    }
+    return copy_text(obs->node->repr(), buf, len);
+}
+
+// ---- algorithms -------------------------------------------------------------------
+int plgb_ops_create(int nops, const char *const *names, const double *params, const int *nparams,
+                    const int64_t *wires, const int *nwires, const uint8_t *inverses, const double *mats,
+                    const int64_t *mat_sizes, const int64_t *cwires, const int *ncwires, const uint8_t *cvals,
+                    plgb_ops **out) {
+    return guard([&] {
+        need(out, "out");
+        auto h = std::make_unique<plgb_ops>();
+        size_t ip = 0, iw = 0, im = 0, ic = 0;
+        for (int k = 0; k < nops; k++) {
+            OpRec op;
+            op.name = names[k];
+            for (int i = 0; i < nparams[k]; i++) {
+                op.params.push_back(params[ip++]);
+            }
+            for (int i = 0; i < nwires[k]; i++) {
+                op.wires.push_back(wires[iw++]);
+            }
+            op.inverse = inverses[k] != 0;
+            const auto ms = static_cast<size_t>(mat_sizes ? mat_sizes[k] : 0);
+            if (ms > 0) {
+                op.matrix = cmat(mats + 2 * im, ms);
+                im += ms;
+            }
+            const int nc = ncwires ? ncwires[k] : 0;
+            for (int i = 0; i < nc; i++) {
+                op.cwires.push_back(cwires[ic]);
+                op.cvals.push_back(cvals[ic] != 0);
+                ic++;
+            }
+            h->list.ops.push_back(std::move(op));
+        }
+        *out = h.release();
+    });
+}
+int plgb_ops_destroy(plgb_ops *ops) {
+    return guard([&] { delete ops; });
+}
+int plgb_ops_num_par_ops(const plgb_ops *ops, int *out) {
+    return guard([&] {
+        need(ops, "ops");
+        need(out, "out");
+        *out = static_cast<int>(ops->list.num_par_ops());
+    });
+}
+int plgb_adjoint_jacobian(plgb_sv *sv, plgb_obs *const *obs, int nobs, const plgb_ops *ops, const int64_t *trainable,
+                          int ntp, int apply_ops, double *jac_out) {
+    return with_sv(sv, [&](auto &s) {
+        need(ops, "ops");
+        need(jac_out, "jac_out");
+        using T = decltype(s.data()->x);
+        std::vector<ObsPtr> ob;
+        for (int i = 0; i < nobs; i++) {
+            need(obs[i], "observable");
+            ob.push_back(obs[i]->node);
+        }
+        const auto j = Adjoint<T>::jacobian(s, ob, ops->list, vec(trainable, ntp), apply_ops != 0);
+        std::memcpy(jac_out, j.data(), j.size() * sizeof(double));
+    });
+}
+
+} // extern "C"

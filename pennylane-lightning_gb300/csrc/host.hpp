@@ -1,0 +1,203 @@
+// C++ host layer: the GB300 counterparts of lightning.qubit's
+// StateVectorLQubitManaged / Measurements / Observables / AdjointJacobian.
+// Device memory is owned here (cudaMalloc), kernels are launched on the
+// state vector's stream, and results are copied back only by the calls that
+// return data to the host.
+#pragma once
+
+#include "kernels.hpp"
+
+#include <complex>
+#include <cstdint>
+#include <memory>
+#include <mutex>
+#include <random>
+#include <string>
+#include <vector>
+
+namespace plgb {
+
+struct PLError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+#define PLGB_REQUIRE(cond, msg)                                                                                   \
+    do {                                                                                                          \
+        if (!(cond)) {                                                                                            \
+            throw ::plgb::PLError(msg);                                                                           \
+        }                                                                                                         \
+    } while (0)
+
+using cd = std::complex<double>;
+
+// ---------------------------------------------------------------------------
+// Observables (precision-agnostic description; converted when applied).
+// ---------------------------------------------------------------------------
+struct ObsNode {
+    enum Kind { Named, Herm, Prod, Ham, Sparse } kind{Named};
+    std::string name;
+    std::vector<int64_t> wires;
+    std::vector<cd> mat;
+    std::vector<std::shared_ptr<ObsNode>> children;
+    std::vector<double> coeffs;
+    std::vector<cd> sp_data;
+    std::vector<int64_t> sp_indices, sp_indptr;
+    std::vector<int64_t> all_wires() const;
+    std::string repr() const;
+};
+using ObsPtr = std::shared_ptr<ObsNode>;
+
+// One operation of an OpsData list (core/algorithms/JacobianData.hpp:39-253)
+struct OpRec {
+    std::string name;
+    std::vector<double> params;
+    std::vector<int64_t> wires;
+    bool inverse{false};
+    std::vector<cd> matrix;
+    std::vector<int64_t> cwires;
+    std::vector<bool> cvals;
+};
+struct OpsList {
+    std::vector<OpRec> ops;
+    size_t num_par_ops() const;
+};
+
+bool is_named_gate(const std::string &name);
+
+// ---------------------------------------------------------------------------
+// Device scratch owned by a state vector.
+// ---------------------------------------------------------------------------
+struct DeviceScratch {
+    double *red{nullptr};       // reduction partials + outputs
+    double *host_out{nullptr};  // pinned
+    void *mat{nullptr};         // matrices / diagonals / offsets
+    size_t mat_bytes{0};
+    void ensure_mat(size_t bytes);
+    ~DeviceScratch();
+};
+
+template <class T> class StateVector {
+  public:
+    using CT = cx<T>;
+    explicit StateVector(int num_qubits, cudaStream_t stream = nullptr);
+    StateVector(CT *external, int num_qubits, cudaStream_t stream = nullptr); // non-owning
+    StateVector(const StateVector &other);                                     // deep copy, same stream
+    StateVector &operator=(const StateVector &) = delete;
+    ~StateVector();
+
+    int num_qubits() const { return n_; }
+    u64 length() const { return N_; }
+    CT *data() { return d_; }
+    const CT *data() const { return d_; }
+    cudaStream_t stream() const { return s_; }
+    void synchronize() const;
+
+    // state management (StateVectorLQubit.hpp:881-1036, Managed :169-183)
+    void reset();
+    void set_basis_state_index(u64 index);
+    void set_basis_state(const std::vector<int64_t> &bits, const std::vector<int64_t> &wires);
+    void set_state_vector(const std::complex<T> *host_state, u64 len, const std::vector<int64_t> &wires);
+    void update_data(const std::complex<T> *host, u64 len);
+    void get_state(std::complex<T> *host_out, u64 len) const;
+    void copy_from(const StateVector &other);
+    void collapse(int64_t wire, bool branch);
+    void normalize();
+
+    // gates (StateVectorLQubit.hpp:359-870)
+    void apply_operation(const std::string &name, const std::vector<int64_t> &wires, bool inverse,
+                         const std::vector<double> &params);
+    void apply_controlled_operation(const std::string &name, const std::vector<int64_t> &cwires,
+                                    const std::vector<bool> &cvals, const std::vector<int64_t> &wires,
+                                    bool inverse, const std::vector<double> &params);
+    void apply_matrix(const cd *mat, const std::vector<int64_t> &wires, bool inverse,
+                      const std::vector<int64_t> &cwires = {}, const std::vector<bool> &cvals = {});
+    void apply_sparse_matrix(const int64_t *indptr, const int64_t *indices, const cd *data, int64_t nnz,
+                             const std::vector<int64_t> &wires, const std::vector<int64_t> &cwires = {},
+                             const std::vector<bool> &cvals = {});
+    void apply_pauli_rot(const std::vector<int64_t> &wires, bool inverse, double angle, const std::string &word);
+    double apply_generator(const std::string &name, const std::vector<int64_t> &cwires,
+                           const std::vector<bool> &cvals, const std::vector<int64_t> &wires);
+    void apply_op(const OpRec &op, bool inverse);
+
+    // primitives used by the dispatcher, the observables and the adjoint
+    void prim_pair(const std::vector<int> &ins_bits, u64 o0, u64 o1, const std::vector<int64_t> &cwires,
+                   const std::vector<bool> &cvals, int mode, const Mat1<T> &m);
+    void prim_1q(int64_t wire, const std::vector<int64_t> &cwires, const std::vector<bool> &cvals, int mode,
+                 const Mat1<T> &m);
+    void prim_dense(const std::vector<int64_t> &wires, const std::vector<int64_t> &cwires,
+                    const std::vector<bool> &cvals, const std::vector<CT> &mat);
+    void prim_diag(const std::vector<int64_t> &wires, const std::vector<int64_t> &cwires,
+                   const std::vector<bool> &cvals, const std::vector<CT> &diag);
+    void prim_zero_outside(const std::vector<int64_t> &cwires, const std::vector<bool> &cvals);
+    void scale_add(const StateVector &x, cd factor); // this += factor * x
+
+    // reductions (return to host, synchronizing)
+    double norm2() const;
+    cd inner(const StateVector &ket) const; // <this|ket>
+    double *scratch_red() const { return scratch_.red; }
+    double *host_out() const { return scratch_.host_out; }
+    DeviceScratch &scratch() const { return scratch_; }
+    int bit_of(int64_t wire) const;
+
+  private:
+    void alloc_(bool zero);
+    void check_wires_(const std::vector<int64_t> &wires, const std::vector<int64_t> &cwires) const;
+    GroupGeom geom_(const std::vector<int> &target_bits, const std::vector<int64_t> &cwires,
+                    const std::vector<bool> &cvals) const;
+    void apply_named_(const std::string &name, std::vector<int64_t> cw, std::vector<bool> cv,
+                      std::vector<int64_t> wires, bool inverse, const std::vector<double> &params);
+    void global_phase_(const std::vector<int64_t> &cw, const std::vector<bool> &cv, bool inverse, T angle);
+
+    int n_{0};
+    u64 N_{0};
+    CT *d_{nullptr};
+    bool owns_{true};
+    cudaStream_t s_{nullptr};
+    bool owns_stream_{false};
+    mutable DeviceScratch scratch_;
+};
+
+// ---------------------------------------------------------------------------
+// Measurements (MeasurementsLQubit.hpp) and sampling.
+// ---------------------------------------------------------------------------
+template <class T> struct Measure {
+    static std::vector<double> probs(StateVector<T> &sv, const std::vector<int64_t> &wires, bool all_wires);
+    static double expval_named(StateVector<T> &sv, const std::string &name, const std::vector<int64_t> &wires);
+    static double expval_matrix(StateVector<T> &sv, const cd *mat, const std::vector<int64_t> &wires);
+    static double expval_sparse(StateVector<T> &sv, const int64_t *indptr, int64_t nptr, const int64_t *indices,
+                                const cd *data, int64_t nnz);
+    static double var_sparse(StateVector<T> &sv, const int64_t *indptr, int64_t nptr, const int64_t *indices,
+                             const cd *data, int64_t nnz);
+    static double expval_obs(StateVector<T> &sv, const ObsNode &obs);
+    static double var_obs(StateVector<T> &sv, const ObsNode &obs);
+    static std::vector<int64_t> samples(StateVector<T> &sv, const std::vector<int64_t> &wires, int64_t shots,
+                                        uint64_t seed);
+    static void apply_obs(StateVector<T> &sv, const ObsNode &obs);
+};
+
+// Pauli-sum compilation of an observable tree.
+struct PauliSum {
+    struct Term {
+        double c;
+        u64 x, yz;
+        int ny4;
+    };
+    std::vector<Term> terms;
+};
+bool compile_pauli(const ObsNode &obs, int n, PauliSum &out);
+std::vector<PauliGroup> group_pauli(const PauliSum &ps);
+
+// ---------------------------------------------------------------------------
+// Adjoint Jacobian (AdjointJacobianLQubit.hpp:225-491).
+// ---------------------------------------------------------------------------
+template <class T> struct Adjoint {
+    static std::vector<double> jacobian(StateVector<T> &sv, const std::vector<ObsPtr> &obs, const OpsList &ops,
+                                        const std::vector<int64_t> &trainable, bool apply_ops);
+};
+
+// ---------------------------------------------------------------------------
+// Thread-local error message for the C ABI.
+// ---------------------------------------------------------------------------
+void set_last_error(const std::string &msg);
+const char *last_error();
+
+} // namespace plgb

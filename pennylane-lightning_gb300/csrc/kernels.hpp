@@ -1,0 +1,116 @@
+// Internal launch interface between the C++ host layer and the CUDA kernels.
+// Everything here takes plain device pointers, sizes and small POD
+// descriptors; nothing is allocated by the launchers.
+#pragma once
+
+#include "plgb_common.cuh"
+
+namespace plgb {
+
+enum Mode1 : int {
+    M1_DENSE = 0,  // general complex 2x2
+    M1_REAL = 1,   // real 2x2 (RY, Hadamard)
+    M1_RXF = 2,    // [[c, i s], [i s, c]] (RX family)
+    M1_DIAG = 3,   // diag(d0, d1)
+    M1_PHASE1 = 4, // diag(1, d1): only the |1> half is touched
+    M1_SWAP = 5,   // X: amplitude swap, no arithmetic
+    M1_ANTI = 6,   // [[0, b], [c, 0]]
+    M1_NEG1 = 7,   // diag(1, -1): sign flip of the |1> half
+};
+
+template <class T> struct Mat1 {
+    cx<T> m[4];
+};
+template <class T> struct Mat2 {
+    cx<T> m[16];
+};
+struct LocalOffsets {
+    u64 off[32];
+};
+struct TBits {
+    int b[16];
+};
+
+template <class T>
+void launch_1q(cudaStream_t s, cx<T> *sv, const GroupGeom &g, u64 o0, u64 o1, int mode, const Mat1<T> &m);
+template <class T>
+void launch_2q(cudaStream_t s, cx<T> *sv, const GroupGeom &g, int bit_hi_local, int bit_lo_local, bool diag,
+               const Mat2<T> &m);
+template <class T>
+void launch_kq(cudaStream_t s, cx<T> *sv, const GroupGeom &g, int k, const LocalOffsets &lo, const cx<T> *dmat,
+               const u64 *dloc);
+template <class T>
+void launch_diag(cudaStream_t s, cx<T> *sv, u64 N, u64 cmask, u64 cval, int k, const TBits &tb, const cx<T> *dd);
+template <class T>
+void launch_parity(cudaStream_t s, cx<T> *sv, u64 N, u64 pmask, u64 cmask, u64 cval, cx<T> s0, cx<T> s1,
+                   bool zero_outside);
+template <class T> void launch_pauli_rot(cudaStream_t s, cx<T> *sv, int n, u64 mxy, u64 my, u64 mz, T c, cx<T> sn);
+template <class T> void launch_zero_outside(cudaStream_t s, cx<T> *sv, u64 N, u64 cmask, u64 cval);
+template <class T> void launch_scale(cudaStream_t s, cx<T> *sv, u64 N, cx<T> f, u64 cmask, u64 cval);
+template <class T> void launch_axpy(cudaStream_t s, cx<T> *y, const cx<T> *x, u64 N, cx<T> f);
+template <class T> void launch_scatter_sub(cudaStream_t s, cx<T> *sv, const cx<T> *sub, u64 D, const u64 *loc);
+template <class T>
+void launch_sparse_local(cudaStream_t s, cx<T> *sv, const GroupGeom &g, const LocalOffsets &lo, int k,
+                         const long long *indptr, const long long *indices, const cx<T> *vals);
+
+// ---------------------------------------------------------------------------
+// Reductions.  Every reduction writes per-block partial sums (double) into
+// `partials` (at least kReduceBlocks * nout doubles) and a final kernel sums
+// them in a fixed order into `out` (nout doubles, device memory), so results
+// are deterministic for a given size.
+// ---------------------------------------------------------------------------
+constexpr int kReduceBlocks = 152 * 4;
+constexpr int kReduceThreads = 256;
+
+// One Pauli word: P|k> = i^ny * (-1)^popcount(k & yz) |k ^ x>.
+struct PauliTerm {
+    double coeff;
+    u64 yz;
+    int ny4; // ny mod 4
+    int pad;
+};
+constexpr int kMaxTermsPerGroup = 64;
+struct PauliGroup {
+    u64 x;      // common flip mask
+    int hb;     // highest set bit of x (unused when x == 0)
+    int nterms; // <= kMaxTermsPerGroup
+    PauliTerm t[kMaxTermsPerGroup];
+};
+
+template <class T> void reduce_norm2(cudaStream_t s, const cx<T> *sv, u64 N, double *partials, double *out);
+template <class T>
+void reduce_inner(cudaStream_t s, const cx<T> *a, const cx<T> *b, u64 N, double *partials, double *out);
+// named one-wire expval: kind 0=X 1=Y 2=Z 3=H
+template <class T>
+void reduce_expval1(cudaStream_t s, const cx<T> *sv, u64 N, int tbit, int kind, double *partials, double *out);
+// Re <psi| sum_t c_t P_t |psi> over one flip-mask group
+template <class T>
+void reduce_pauli_group(cudaStream_t s, const cx<T> *sv, u64 N, const PauliGroup &g, double *partials, double *out);
+// Im / Re of <a| P |b> restricted to indices (j & pmask) == pval; out[0]=Re, out[1]=Im
+template <class T>
+void reduce_pauli_transition(cudaStream_t s, const cx<T> *a, const cx<T> *b, u64 N, u64 x, u64 yz, int ny4,
+                             u64 pmask, u64 pval, double *partials, double *out);
+// Re sum_groups v^H M v on k wires (Hermitian expval)
+template <class T>
+void reduce_expval_matrix(cudaStream_t s, const cx<T> *sv, const GroupGeom &g, int k, const LocalOffsets &lo,
+                          const cx<T> *dmat, double *partials, double *out);
+// Re <psi| A |psi> with A in CSR over the full register
+template <class T>
+void reduce_expval_csr(cudaStream_t s, const cx<T> *sv, u64 N, const long long *indptr, const long long *indices,
+                       const cx<T> *vals, double *partials, double *out);
+// out = A psi (CSR SpMV over the full register)
+template <class T>
+void launch_csr_apply(cudaStream_t s, const cx<T> *sv, cx<T> *out, u64 N, const long long *indptr,
+                      const long long *indices, const cx<T> *vals);
+
+// Hamiltonian apply, one flip-mask group: out (+)= sum_t c_t P_t psi
+template <class T>
+void launch_pauli_accumulate(cudaStream_t s, const cx<T> *psi, cx<T> *out, u64 N, const PauliGroup &g, bool first);
+
+// Probabilities: all wires (elementwise), or marginal over `k` wires given by
+// their bit positions (wires[0] = MSB of the output index).
+template <class T> void launch_probs_all(cudaStream_t s, const cx<T> *sv, u64 N, T *out);
+template <class T>
+void launch_probs_marginal(cudaStream_t s, const cx<T> *sv, u64 N, int k, const TBits &tb, double *out);
+
+} // namespace plgb

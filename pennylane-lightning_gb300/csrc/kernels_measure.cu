@@ -1,0 +1,443 @@
+// Measurement and linear-algebra kernels (sm_103a).  All reductions are
+// warp-shuffle + shared-memory tree reductions into per-block partials,
+// followed by a fixed-order final sum, so a result does not depend on
+// scheduling.  Accumulation is in double for both precisions.
+//
+// Reference semantics: pennylane_lightning/core/simulators/lightning_qubit/
+// measurements/MeasurementsLQubit.hpp (probs :90-163, expval :213-394),
+// ExpValFunc.hpp (:69-335), utils/LinearAlgebra.hpp innerProdC (:122-145),
+// observables/ObservablesLQubit.hpp HamiltonianApplyInPlace (:156-251).
+#include "kernels.hpp"
+
+namespace plgb {
+
+template <int NOUT> __device__ __forceinline__ void block_reduce_store(double (&v)[NOUT], double *partials) {
+    __shared__ double sh[NOUT][kReduceThreads / 32];
+#pragma unroll
+    for (int o = 0; o < NOUT; o++) {
+        double x = v[o];
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            x += __shfl_down_sync(0xffffffffu, x, d);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            sh[o][threadIdx.x >> 5] = x;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int o = 0; o < NOUT; o++) {
+            double x = threadIdx.x < (kReduceThreads / 32) ? sh[o][threadIdx.x] : 0.0;
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) {
+                x += __shfl_down_sync(0xffffffffu, x, d);
+            }
+            if (threadIdx.x == 0) {
+                partials[static_cast<size_t>(blockIdx.x) * NOUT + o] = x;
+            }
+        }
+    }
+}
+
+template <int NOUT> __global__ void k_finalize(const double *__restrict__ partials, int nblocks, double *out) {
+    // one warp per output, fixed order
+    const int o = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    if (o >= NOUT) {
+        return;
+    }
+    double x = 0.0;
+    for (int b = lane; b < nblocks; b += 32) {
+        x += partials[static_cast<size_t>(b) * NOUT + o];
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        x += __shfl_down_sync(0xffffffffu, x, d);
+    }
+    if (lane == 0) {
+        out[o] = x;
+    }
+}
+
+template <int NOUT> static void finalize(cudaStream_t s, const double *partials, int nblocks, double *out) {
+    k_finalize<NOUT><<<1, 32 * NOUT, 0, s>>>(partials, nblocks, out);
+    cuda_check(cudaGetLastError(), "k_finalize launch");
+}
+
+static int reduce_grid(u64 work) {
+    const u64 want = (work + kReduceThreads - 1) / kReduceThreads;
+    return static_cast<int>(want < static_cast<u64>(kReduceBlocks) ? (want < 1 ? 1 : want) : kReduceBlocks);
+}
+
+#define GRID_STRIDE(i, N)                                                                                         \
+    for (u64 i = static_cast<u64>(blockIdx.x) * blockDim.x + threadIdx.x; i < (N);                             \
+         i += static_cast<u64>(gridDim.x) * blockDim.x)
+
+// ---------------------------------------------------------------------------
+template <class T> __global__ void __launch_bounds__(kReduceThreads) k_norm2(const cx<T> *__restrict__ a, u64 N, double *partials) {
+    double v[1] = {0.0};
+    GRID_STRIDE(i, N) {
+        const cx<T> x = a[i];
+        v[0] += static_cast<double>(x.x) * x.x + static_cast<double>(x.y) * x.y;
+    }
+    block_reduce_store<1>(v, partials);
+}
+template <class T> void reduce_norm2(cudaStream_t s, const cx<T> *sv, u64 N, double *partials, double *out) {
+    const int g = reduce_grid(N);
+    k_norm2<T><<<g, kReduceThreads, 0, s>>>(sv, N, partials);
+    cuda_check(cudaGetLastError(), "k_norm2 launch");
+    finalize<1>(s, partials, g, out);
+}
+
+// <a|b> = sum conj(a_i) b_i
+template <class T>
+__global__ void __launch_bounds__(kReduceThreads) k_inner(const cx<T> *__restrict__ a, const cx<T> *__restrict__ b, u64 N, double *partials) {
+    double v[2] = {0.0, 0.0};
+    GRID_STRIDE(i, N) {
+        const cx<T> x = a[i];
+        const cx<T> y = b[i];
+        v[0] += static_cast<double>(x.x) * y.x + static_cast<double>(x.y) * y.y;
+        v[1] += static_cast<double>(x.x) * y.y - static_cast<double>(x.y) * y.x;
+    }
+    block_reduce_store<2>(v, partials);
+}
+template <class T>
+void reduce_inner(cudaStream_t s, const cx<T> *a, const cx<T> *b, u64 N, double *partials, double *out) {
+    const int g = reduce_grid(N);
+    k_inner<T><<<g, kReduceThreads, 0, s>>>(a, b, N, partials);
+    cuda_check(cudaGetLastError(), "k_inner launch");
+    finalize<2>(s, partials, g, out);
+}
+
+// Named one-wire observables (ExpValFunc.hpp:69-90 with the per-name cores of
+// MeasurementsLQubit.hpp:247-305).
+template <class T, int KIND>
+__global__ void __launch_bounds__(kReduceThreads) k_expval1(const cx<T> *__restrict__ a, u64 half, int tbit, double *partials) {
+    double v[1] = {0.0};
+    const u64 tm = u64{1} << tbit;
+    GRID_STRIDE(k, half) {
+        const u64 i0 = insert_zero(k, tbit);
+        const cx<T> p = a[i0];
+        const cx<T> q = a[i0 | tm];
+        const double px = p.x, py = p.y, qx = q.x, qy = q.y;
+        if constexpr (KIND == 0) {
+            v[0] += 2.0 * (px * qx + py * qy);
+        } else if constexpr (KIND == 1) {
+            v[0] += 2.0 * (px * qy - py * qx);
+        } else if constexpr (KIND == 2) {
+            v[0] += (px * px + py * py) - (qx * qx + qy * qy);
+        } else {
+            v[0] += 0.70710678118654752440 * ((px * px + py * py) - (qx * qx + qy * qy) + 2.0 * (px * qx + py * qy));
+        }
+    }
+    block_reduce_store<1>(v, partials);
+}
+template <class T>
+void reduce_expval1(cudaStream_t s, const cx<T> *sv, u64 N, int tbit, int kind, double *partials, double *out) {
+    const u64 half = N >> 1;
+    const int g = reduce_grid(half);
+    switch (kind) {
+    case 0: k_expval1<T, 0><<<g, kReduceThreads, 0, s>>>(sv, half, tbit, partials); break;
+    case 1: k_expval1<T, 1><<<g, kReduceThreads, 0, s>>>(sv, half, tbit, partials); break;
+    case 2: k_expval1<T, 2><<<g, kReduceThreads, 0, s>>>(sv, half, tbit, partials); break;
+    default: k_expval1<T, 3><<<g, kReduceThreads, 0, s>>>(sv, half, tbit, partials); break;
+    }
+    cuda_check(cudaGetLastError(), "k_expval1 launch");
+    finalize<1>(s, partials, g, out);
+}
+
+// ---------------------------------------------------------------------------
+// Pauli words.  With P|k> = i^ny (-1)^{|k & yz|} |k ^ x>, the expectation
+// over a pair (j, j' = j ^ x) is  sum_t c_t Re( i^ny [ s(j') A + s(j) conj(A) ] )
+// with A = conj(psi_j) psi_j' and s(k) = (-1)^{|k & yz|}.  One read of the
+// state serves every term of a flip-mask group.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double term_pair(const PauliTerm &t, u64 j, u64 jp, double ar, double ai) {
+    const double s = (__popcll(j & t.yz) & 1) ? -1.0 : 1.0;
+    const double sp = (__popcll(jp & t.yz) & 1) ? -1.0 : 1.0;
+    // i^ny * ((s'+s) ar + i (s'-s) ai), real part
+    switch (t.ny4) {
+    case 0: return (sp + s) * ar;
+    case 1: return -(sp - s) * ai;
+    case 2: return -(sp + s) * ar;
+    default: return (sp - s) * ai;
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kReduceThreads) k_pauli_group(const cx<T> *__restrict__ a, u64 N, const __grid_constant__ PauliGroup g,
+                                                               double *partials) {
+    double v[1] = {0.0};
+    if (g.x == 0) {
+        GRID_STRIDE(j, N) {
+            const cx<T> p = a[j];
+            const double w = static_cast<double>(p.x) * p.x + static_cast<double>(p.y) * p.y;
+            double f = 0.0;
+            for (int t = 0; t < g.nterms; t++) {
+                f += (__popcll(j & g.t[t].yz) & 1) ? -g.t[t].coeff : g.t[t].coeff;
+            }
+            v[0] += w * f;
+        }
+    } else {
+        const u64 half = N >> 1;
+        GRID_STRIDE(k, half) {
+            const u64 j = insert_zero(k, g.hb);
+            const u64 jp = j ^ g.x;
+            const cx<T> p = a[j];
+            const cx<T> q = a[jp];
+            // A = conj(p) q
+            const double ar = static_cast<double>(p.x) * q.x + static_cast<double>(p.y) * q.y;
+            const double ai = static_cast<double>(p.x) * q.y - static_cast<double>(p.y) * q.x;
+            double f = 0.0;
+            for (int t = 0; t < g.nterms; t++) {
+                f += g.t[t].coeff * term_pair(g.t[t], j, jp, ar, ai);
+            }
+            v[0] += f;
+        }
+    }
+    block_reduce_store<1>(v, partials);
+}
+template <class T>
+void reduce_pauli_group(cudaStream_t s, const cx<T> *sv, u64 N, const PauliGroup &g, double *partials, double *out) {
+    const int grid = reduce_grid(g.x == 0 ? N : N >> 1);
+    k_pauli_group<T><<<grid, kReduceThreads, 0, s>>>(sv, N, g, partials);
+    cuda_check(cudaGetLastError(), "k_pauli_group launch");
+    finalize<1>(s, partials, grid, out);
+}
+
+// <a| Pi P |b> where Pi projects on (j & pmask) == pval (row index j):
+// sum_j conj(a_j) i^ny (-1)^{|(j^x) & yz|} b_{j^x}.
+template <class T>
+__global__ void __launch_bounds__(kReduceThreads) k_pauli_transition(const cx<T> *__restrict__ a, const cx<T> *__restrict__ b, u64 N,
+                                                                    u64 x, u64 yz, int ny4, u64 pmask, u64 pval,
+                                                                    double *partials) {
+    double v[2] = {0.0, 0.0};
+    GRID_STRIDE(j, N) {
+        if ((j & pmask) != pval) {
+            continue;
+        }
+        const u64 k = j ^ x;
+        const cx<T> p = a[j];
+        const cx<T> q = b[k];
+        double re = static_cast<double>(p.x) * q.x + static_cast<double>(p.y) * q.y;
+        double im = static_cast<double>(p.x) * q.y - static_cast<double>(p.y) * q.x;
+        if (__popcll(k & yz) & 1) {
+            re = -re;
+            im = -im;
+        }
+        switch (ny4) {
+        case 0: v[0] += re; v[1] += im; break;
+        case 1: v[0] -= im; v[1] += re; break;
+        case 2: v[0] -= re; v[1] -= im; break;
+        default: v[0] += im; v[1] -= re; break;
+        }
+    }
+    block_reduce_store<2>(v, partials);
+}
+template <class T>
+void reduce_pauli_transition(cudaStream_t s, const cx<T> *a, const cx<T> *b, u64 N, u64 x, u64 yz, int ny4,
+                             u64 pmask, u64 pval, double *partials, double *out) {
+    const int g = reduce_grid(N);
+    k_pauli_transition<T><<<g, kReduceThreads, 0, s>>>(a, b, N, x, yz, ny4, pmask, pval, partials);
+    cuda_check(cudaGetLastError(), "k_pauli_transition launch");
+    finalize<2>(s, partials, g, out);
+}
+
+// Hamiltonian apply for one flip-mask group:
+// out_j (+)= psi_{j^x} * sum_t c_t i^ny (-1)^{|(j^x) & yz|}.
+template <class T>
+__global__ void __launch_bounds__(256) k_pauli_accumulate(const cx<T> *__restrict__ psi, cx<T> *__restrict__ out, u64 N,
+                                                         const __grid_constant__ PauliGroup g, int first) {
+    GRID_STRIDE(j, N) {
+        const u64 k = j ^ g.x;
+        double wr = 0.0, wi = 0.0;
+        for (int t = 0; t < g.nterms; t++) {
+            const double c = (__popcll(k & g.t[t].yz) & 1) ? -g.t[t].coeff : g.t[t].coeff;
+            switch (g.t[t].ny4) {
+            case 0: wr += c; break;
+            case 1: wi += c; break;
+            case 2: wr -= c; break;
+            default: wi -= c; break;
+            }
+        }
+        const cx<T> q = psi[k];
+        const cx<T> w{static_cast<T>(wr), static_cast<T>(wi)};
+        if (first) {
+            out[j] = w * q;
+        } else {
+            out[j] = cfma(w, q, out[j]);
+        }
+    }
+}
+template <class T>
+void launch_pauli_accumulate(cudaStream_t s, const cx<T> *psi, cx<T> *out, u64 N, const PauliGroup &g, bool first) {
+    k_pauli_accumulate<T><<<grid_for(N, 256, 8), 256, 0, s>>>(psi, out, N, g, first ? 1 : 0);
+    cuda_check(cudaGetLastError(), "k_pauli_accumulate launch");
+}
+
+// Hermitian matrix on k wires: sum over groups of Re(v^H M v).
+template <class T>
+__global__ void __launch_bounds__(kReduceThreads) k_expval_matrix(const cx<T> *__restrict__ a, GroupGeom g, int k, LocalOffsets lo,
+                                                                 const cx<T> *__restrict__ mat, double *partials) {
+    double v[1] = {0.0};
+    const int D = 1 << k;
+    GRID_STRIDE(q, g.ngroups) {
+        const u64 b = insert_zeros(q, g.ins, g.nins);
+        cx<double> x[32];
+        for (int j = 0; j < D; j++) {
+            const cx<T> t = a[b | lo.off[j]];
+            x[j] = cx<double>{static_cast<double>(t.x), static_cast<double>(t.y)};
+        }
+        for (int r = 0; r < D; r++) {
+            cx<double> acc{0, 0};
+            for (int j = 0; j < D; j++) {
+                const cx<T> m = mat[r * D + j];
+                acc = cfma(cx<double>{static_cast<double>(m.x), static_cast<double>(m.y)}, x[j], acc);
+            }
+            v[0] += x[r].x * acc.x + x[r].y * acc.y;
+        }
+    }
+    block_reduce_store<1>(v, partials);
+}
+template <class T>
+void reduce_expval_matrix(cudaStream_t s, const cx<T> *sv, const GroupGeom &g, int k, const LocalOffsets &lo,
+                          const cx<T> *dmat, double *partials, double *out) {
+    const int grid = reduce_grid(g.ngroups);
+    k_expval_matrix<T><<<grid, kReduceThreads, 0, s>>>(sv, g, k, lo, dmat, partials);
+    cuda_check(cudaGetLastError(), "k_expval_matrix launch");
+    finalize<1>(s, partials, grid, out);
+}
+
+// CSR: Re sum_r conj(psi_r) sum_p A_rp psi_col(p)
+template <class T>
+__global__ void __launch_bounds__(kReduceThreads) k_expval_csr(const cx<T> *__restrict__ a, u64 N, const long long *__restrict__ ip,
+                                                              const long long *__restrict__ ix,
+                                                              const cx<T> *__restrict__ val, double *partials) {
+    double v[1] = {0.0};
+    GRID_STRIDE(r, N) {
+        double ar = 0.0, ai = 0.0;
+        for (long long p = ip[r]; p < ip[r + 1]; p++) {
+            const cx<T> m = val[p];
+            const cx<T> x = a[ix[p]];
+            ar += static_cast<double>(m.x) * x.x - static_cast<double>(m.y) * x.y;
+            ai += static_cast<double>(m.x) * x.y + static_cast<double>(m.y) * x.x;
+        }
+        const cx<T> y = a[r];
+        v[0] += static_cast<double>(y.x) * ar + static_cast<double>(y.y) * ai;
+    }
+    block_reduce_store<1>(v, partials);
+}
+template <class T>
+void reduce_expval_csr(cudaStream_t s, const cx<T> *sv, u64 N, const long long *indptr, const long long *indices,
+                       const cx<T> *vals, double *partials, double *out) {
+    const int g = reduce_grid(N);
+    k_expval_csr<T><<<g, kReduceThreads, 0, s>>>(sv, N, indptr, indices, vals, partials);
+    cuda_check(cudaGetLastError(), "k_expval_csr launch");
+    finalize<1>(s, partials, g, out);
+}
+
+template <class T>
+__global__ void k_csr_apply(const cx<T> *__restrict__ a, cx<T> *__restrict__ out, u64 N, const long long *__restrict__ ip,
+                            const long long *__restrict__ ix, const cx<T> *__restrict__ val) {
+    GRID_STRIDE(r, N) {
+        cx<T> acc{0, 0};
+        for (long long p = ip[r]; p < ip[r + 1]; p++) {
+            acc = cfma(val[p], a[ix[p]], acc);
+        }
+        out[r] = acc;
+    }
+}
+template <class T>
+void launch_csr_apply(cudaStream_t s, const cx<T> *sv, cx<T> *out, u64 N, const long long *indptr,
+                      const long long *indices, const cx<T> *vals) {
+    k_csr_apply<T><<<grid_for(N, 256, 8), 256, 0, s>>>(sv, out, N, indptr, indices, vals);
+    cuda_check(cudaGetLastError(), "k_csr_apply launch");
+}
+
+// ---------------------------------------------------------------------------
+// Probabilities.
+// ---------------------------------------------------------------------------
+// |psi_i|^2 rounded exactly as std::norm does without contraction (two
+// products, one sum), so the distribution a seeded sampler consumes is
+// bit-identical to the reference's.
+__device__ __forceinline__ double norm_rn(cx<double> x) { return __dadd_rn(__dmul_rn(x.x, x.x), __dmul_rn(x.y, x.y)); }
+__device__ __forceinline__ float norm_rn(cx<float> x) { return __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y)); }
+
+template <class T> __global__ void k_probs_all(const cx<T> *__restrict__ a, u64 N, T *__restrict__ out) {
+    GRID_STRIDE(i, N) { out[i] = norm_rn(a[i]); }
+}
+template <class T> void launch_probs_all(cudaStream_t s, const cx<T> *sv, u64 N, T *out) {
+    k_probs_all<T><<<grid_for(N, 256, 8), 256, 0, s>>>(sv, N, out);
+    cuda_check(cudaGetLastError(), "k_probs_all launch");
+}
+
+// Marginal over k wires: shared-memory histogram for k <= 12, global
+// atomics beyond.  Output index bit (k-1-m) is wire m of the request.
+template <class T>
+__global__ void __launch_bounds__(256) k_probs_marginal(const cx<T> *__restrict__ a, u64 N, int k, TBits tb, double *out) {
+    extern __shared__ double hist[];
+    const int D = 1 << k;
+    const bool use_smem = k <= 12;
+    if (use_smem) {
+        for (int i = threadIdx.x; i < D; i += blockDim.x) {
+            hist[i] = 0.0;
+        }
+        __syncthreads();
+    }
+    GRID_STRIDE(i, N) {
+        const cx<T> x = a[i];
+        const double p = static_cast<double>(x.x) * x.x + static_cast<double>(x.y) * x.y;
+        unsigned j = 0;
+        for (int m = 0; m < k; m++) {
+            j = (j << 1) | static_cast<unsigned>((i >> tb.b[m]) & 1U);
+        }
+        if (use_smem) {
+            atomicAdd(&hist[j], p);
+        } else {
+            atomicAdd(&out[j], p);
+        }
+    }
+    if (use_smem) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < D; i += blockDim.x) {
+            if (hist[i] != 0.0) {
+                atomicAdd(&out[i], hist[i]);
+            }
+        }
+    }
+}
+template <class T>
+void launch_probs_marginal(cudaStream_t s, const cx<T> *sv, u64 N, int k, const TBits &tb, double *out) {
+    cuda_check(cudaMemsetAsync(out, 0, sizeof(double) << k, s), "probs memset");
+    const size_t smem = k <= 12 ? (sizeof(double) << k) : 0;
+    if (smem > 48 * 1024) {
+        cuda_check(cudaFuncSetAttribute(k_probs_marginal<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        static_cast<int>(smem)),
+                   "probs smem attribute");
+    }
+    k_probs_marginal<T><<<grid_for(N, 256, 2), 256, smem, s>>>(sv, N, k, tb, out);
+    cuda_check(cudaGetLastError(), "k_probs_marginal launch");
+}
+
+#define PLGB_INST_MEAS(T)                                                                                         \
+    template void reduce_norm2<T>(cudaStream_t, const cx<T> *, u64, double *, double *);                        \
+    template void reduce_inner<T>(cudaStream_t, const cx<T> *, const cx<T> *, u64, double *, double *);         \
+    template void reduce_expval1<T>(cudaStream_t, const cx<T> *, u64, int, int, double *, double *);            \
+    template void reduce_pauli_group<T>(cudaStream_t, const cx<T> *, u64, const PauliGroup &, double *, double *); \
+    template void reduce_pauli_transition<T>(cudaStream_t, const cx<T> *, const cx<T> *, u64, u64, u64, int, u64, \
+                                             u64, double *, double *);                                            \
+    template void reduce_expval_matrix<T>(cudaStream_t, const cx<T> *, const GroupGeom &, int, const LocalOffsets &, \
+                                          const cx<T> *, double *, double *);                                     \
+    template void reduce_expval_csr<T>(cudaStream_t, const cx<T> *, u64, const long long *, const long long *,   \
+                                       const cx<T> *, double *, double *);                                        \
+    template void launch_csr_apply<T>(cudaStream_t, const cx<T> *, cx<T> *, u64, const long long *,              \
+                                      const long long *, const cx<T> *);                                          \
+    template void launch_pauli_accumulate<T>(cudaStream_t, const cx<T> *, cx<T> *, u64, const PauliGroup &, bool); \
+    template void launch_probs_all<T>(cudaStream_t, const cx<T> *, u64, T *);                                    \
+    template void launch_probs_marginal<T>(cudaStream_t, const cx<T> *, u64, int, const TBits &, double *);
+
+PLGB_INST_MEAS(float)
+PLGB_INST_MEAS(double)
+
+} // namespace plgb

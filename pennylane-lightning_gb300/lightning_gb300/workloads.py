@@ -1,0 +1,196 @@
+"""Seeded synthetic circuits for the benchmark configurations.
+
+No public benchmark suite is involved: every circuit, angle, matrix and
+observable below is generated from ``numpy.random.default_rng(seed)`` with
+seed = 1000 + configuration index, so a run is reproducible everywhere.
+
+* config 0 — hardware-efficient ansatz: per layer RX, RY, RZ on every qubit,
+  then a CNOT ring i -> i+1 mod n; observable sum_i Z_i.
+* config 1 — 30-qubit random circuit: per cycle a Haar SU(2) on every qubit,
+  then CZ on n/2 disjoint random pairs (each wire >= 24 is paired with a wire
+  < 24, so every cycle exercises the small-stride bits); a 64-term Pauli
+  Hamiltonian of weight 1..4 with N(0,1) coefficients.
+* config 2 — batch of independent config-0 circuits with n ~ U{10..22} and
+  depth ~ U{4..16}; each returns <sum Z_i> and 3 weight-2 Pauli strings.
+* config 3 — strongly entangling ansatz: per layer Rot on each qubit (as
+  RZ, RY, RZ for the adjoint) then CNOT(i, i + r mod n), r = (layer mod
+  (n-1)) + 1; a 200-term Pauli Hamiltonian of weight <= 4.
+* config 4 — open-loop Poisson request stream with n in 8..26,
+  P(n) ~ 2^(-n/4), config-0 bodies of depth 2..12, 1..32-term Hamiltonians,
+  30 % adjoint requests.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+TWO_PI = 2.0 * np.pi
+
+
+@dataclass
+class Op:
+    name: str
+    wires: list[int]
+    params: list[float] = field(default_factory=list)
+    matrix: np.ndarray | None = None
+    inverse: bool = False
+
+    def as_dict(self) -> dict:
+        d = {"name": self.name, "wires": list(self.wires), "params": list(self.params), "inverse": self.inverse}
+        if self.matrix is not None:
+            d["matrix"] = self.matrix
+        return d
+
+
+@dataclass
+class PauliSum:
+    coeffs: list[float]
+    words: list[str]
+    wires: list[list[int]]
+
+    def terms(self):
+        return list(zip(self.coeffs, self.words, self.wires))
+
+
+def haar_su2(rng) -> np.ndarray:
+    """Haar-random SU(2): QR of a complex Ginibre 2x2 with the phase fix,
+    then the determinant phase removed."""
+    z = (rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2))) / np.sqrt(2.0)
+    q, r = np.linalg.qr(z)
+    d = np.diag(r)
+    q = q * (d / np.abs(d))
+    return q / np.sqrt(np.linalg.det(q))
+
+
+def random_pauli_sum(rng, n: int, nterms: int, wmin: int = 1, wmax: int = 4) -> PauliSum:
+    coeffs, words, wires = [], [], []
+    for _ in range(nterms):
+        w = int(rng.integers(wmin, wmax + 1))
+        wires.append([int(x) for x in rng.choice(n, size=w, replace=False)])
+        words.append("".join(rng.choice(list("XYZ"), size=w)))
+        coeffs.append(float(rng.normal()))
+    return PauliSum(coeffs, words, wires)
+
+
+def sum_z(n: int) -> PauliSum:
+    return PauliSum([1.0] * n, ["Z"] * n, [[q] for q in range(n)])
+
+
+# --------------------------------------------------------------------- config 0
+def config0(n: int = 20, layers: int = 10, seed: int = 1000) -> list[Op]:
+    rng = np.random.default_rng(seed)
+    angles = rng.uniform(0.0, TWO_PI, size=(layers, n, 3))
+    ops: list[Op] = []
+    for layer in range(layers):
+        for q in range(n):
+            ops.append(Op("RX", [q], [float(angles[layer, q, 0])]))
+            ops.append(Op("RY", [q], [float(angles[layer, q, 1])]))
+            ops.append(Op("RZ", [q], [float(angles[layer, q, 2])]))
+        for q in range(n):
+            ops.append(Op("CNOT", [q, (q + 1) % n]))
+    return ops
+
+
+# --------------------------------------------------------------------- config 1
+def cz_pairs(rng, n: int, high_from: int) -> list[tuple[int, int]]:
+    high = [q for q in range(n) if q >= high_from]
+    low = [int(q) for q in rng.permutation([q for q in range(n) if q < high_from])]
+    pairs = []
+    for h in rng.permutation(high):
+        pairs.append((low.pop(), int(h)))
+    while len(low) >= 2:
+        pairs.append((low.pop(), low.pop()))
+    return pairs
+
+
+def config1(n: int = 30, cycles: int = 20, seed: int = 1001, nterms: int = 64) -> tuple[list[Op], PauliSum]:
+    rng = np.random.default_rng(seed)
+    ops: list[Op] = []
+    high_from = max(0, n - 6) if n >= 12 else n // 2
+    for _ in range(cycles):
+        for q in range(n):
+            ops.append(Op("QubitUnitary", [q], matrix=haar_su2(rng)))
+        for a, b in cz_pairs(rng, n, high_from):
+            ops.append(Op("CZ", [a, b]))
+    return ops, random_pauli_sum(rng, n, nterms)
+
+
+def unfused_bytes(ops: list[Op], n: int, itemsize: int) -> float:
+    """Algorithmic HBM bytes of applying `ops` one by one: 2 f N S per gate,
+    f = fraction of amplitudes a gate changes (1 for dense / rotation gates,
+    1/2 for CNOT/SWAP-like permutations, 1/4 for CZ-like phases)."""
+    N = float(1 << n)
+    frac = {"CZ": 0.25, "ControlledPhaseShift": 0.25, "CNOT": 0.5, "SWAP": 0.5, "PauliX": 1.0, "Toffoli": 0.25}
+    return sum(2.0 * frac.get(op.name, 1.0) * N * itemsize for op in ops)
+
+
+# --------------------------------------------------------------------- config 2
+@dataclass
+class BatchCircuit:
+    n: int
+    ops: list[Op]
+    observables: list[PauliSum]
+
+
+def config2(num: int = 4096, seed: int = 1002) -> list[BatchCircuit]:
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(num):
+        n = int(rng.integers(10, 23))
+        depth = int(rng.integers(4, 17))
+        body = config0(n, depth, seed=int(rng.integers(0, 2**31 - 1)))
+        obs = [sum_z(n)] + [random_pauli_sum(rng, n, 1, 2, 2) for _ in range(3)]
+        out.append(BatchCircuit(n, body, obs))
+    return out
+
+
+# --------------------------------------------------------------------- config 3
+def config3(n: int = 28, layers: int = 12, seed: int = 1003, nterms: int = 200) -> tuple[list[Op], PauliSum]:
+    rng = np.random.default_rng(seed)
+    ops: list[Op] = []
+    for layer in range(layers):
+        r = (layer % (n - 1)) + 1
+        ang = rng.uniform(0.0, TWO_PI, size=(n, 3))
+        for q in range(n):
+            phi, theta, omega = (float(x) for x in ang[q])
+            # Rot(phi, theta, omega) = RZ(omega) RY(theta) RZ(phi), as the
+            # adjoint transforms decompose it
+            ops.append(Op("RZ", [q], [phi]))
+            ops.append(Op("RY", [q], [theta]))
+            ops.append(Op("RZ", [q], [omega]))
+        for q in range(n):
+            ops.append(Op("CNOT", [q, (q + r) % n]))
+    return ops, random_pauli_sum(rng, n, nterms, 1, 4)
+
+
+# --------------------------------------------------------------------- config 4
+@dataclass
+class Request:
+    rid: int
+    arrival: float
+    n: int
+    ops: list[Op]
+    ham: PauliSum
+    adjoint: bool
+
+
+def config4(rate: float = 2000.0, duration: float = 60.0, seed: int = 1004) -> list[Request]:
+    rng = np.random.default_rng(seed)
+    ns = np.arange(8, 27)
+    pn = 2.0 ** (-ns / 4.0)
+    pn /= pn.sum()
+    t = 0.0
+    reqs = []
+    rid = 0
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t >= duration:
+            break
+        n = int(rng.choice(ns, p=pn))
+        depth = int(rng.integers(2, 13))
+        body = config0(n, depth, seed=int(rng.integers(0, 2**31 - 1)))
+        ham = random_pauli_sum(rng, n, int(rng.integers(1, 33)))
+        reqs.append(Request(rid, t, n, body, ham, bool(rng.random() < 0.3)))
+        rid += 1
+    return reqs

@@ -1,0 +1,135 @@
+"""GPU measurements vs the CPU oracle: probs (index ordering), expval / var of
+named, Hermitian, Pauli-sum, mixed and sparse observables, seeded samples.
+
+Mirrors pennylane_lightning/core/simulators/lightning_qubit/measurements/tests/
+Test_MeasurementsLQubit.cpp (:205-430 expval by name/matrix, :534-968 probs
+index ordering with permuted targets) and core/measurements/tests/
+Test_MeasurementsBase.cpp (:1319-1323 seeded samples).
+"""
+import numpy as np
+import pytest
+
+from helpers import DTYPES, assert_close, meas_class, obs_ns, rand_hermitian, rand_state, seed_of, sv_class
+
+pytestmark = pytest.mark.gpu
+
+WIRE_LISTS = [None, [0], [6], [2, 5], [5, 2], [1, 4, 6], [6, 0, 3, 2], [0, 1, 2, 3, 4], [4, 2, 0, 6, 5, 1],
+              [0, 1, 2, 3, 4, 5, 6], [6, 5, 4, 3, 2, 1, 0]]
+
+
+def _setup(ops, oracle, n, dt, seed):
+    rng = np.random.default_rng(seed)
+    st = rand_state(rng, n, dt)
+    sv = sv_class(ops, dt)(n)
+    sv.updateData(st)
+    o = oracle.sv(n, dt)
+    o.set_state(st)
+    return rng, sv, meas_class(ops, dt)(sv), o
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+def test_probs_ordering(ops_module, oracle, dt):
+    _, sv, m, o = _setup(ops_module, oracle, 7, dt, seed_of("probs", dt.__name__))
+    for wires in WIRE_LISTS:
+        p = m.probs() if wires is None else m.probs(wires)
+        assert_close(p, o.probs(wires), dt, what=f"probs {wires}")
+    # the all-wires distribution is computed element-wise: bit-exact
+    assert np.array_equal(m.probs().astype(np.float64), o.probs())
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+def test_expval_var_named(ops_module, oracle, dt):
+    _, sv, m, o = _setup(ops_module, oracle, 6, dt, seed_of("named", dt.__name__))
+    for name in ("PauliX", "PauliY", "PauliZ", "Hadamard", "Identity"):
+        for w in range(6):
+            assert_close(m.expval(name, [w]), o.expval_named(name, [w]), dt, scale=10, what=f"E {name}{w}")
+            assert_close(m.var(name, [w]), o.var_named(name, [w]), dt, scale=10, what=f"V {name}{w}")
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5, 6])
+def test_expval_var_matrix(ops_module, oracle, k, dt):
+    rng, sv, m, o = _setup(ops_module, oracle, 8, dt, seed_of("hmat", k, dt.__name__))
+    H = rand_hermitian(rng, k)
+    w = [int(x) for x in rng.choice(8, size=k, replace=False)]
+    assert_close(m.expval(H, w), o.expval_matrix(H, w), dt, scale=100, what="E herm")
+    assert_close(m.var(H, w), o.var_matrix(H, w), dt, scale=1000, what="V herm")
+
+
+def _pauli_terms(rng, n, nterms, maxw=4):
+    terms = []
+    for _ in range(nterms):
+        wt = int(rng.integers(1, maxw + 1))
+        terms.append((float(rng.normal()), "".join(rng.choice(list("XYZ"), size=wt)),
+                      [int(x) for x in rng.choice(n, size=wt, replace=False)]))
+    return terms
+
+
+def _ham_obs(ops, dt, terms):
+    Named, Herm, Prod, Ham, _ = obs_ns(ops, dt)
+    names = {"X": "PauliX", "Y": "PauliY", "Z": "PauliZ"}
+    return Ham([c for c, _, _ in terms],
+               [Prod([Named(names[ch], [w]) for ch, w in zip(word, wires)]) for _, word, wires in terms])
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+def test_expval_pauli_hamiltonian(ops_module, oracle, dt):
+    from oracle.pyoracle import pauli_sum_spec
+
+    rng, sv, m, o = _setup(ops_module, oracle, 10, dt, seed_of("ham", dt.__name__))
+    terms = _pauli_terms(rng, 10, 64)
+    # repeated flip masks: same X/Y positions, different Z tails
+    terms += [(0.5, "XZ", [1, 4]), (-0.25, "XZ", [1, 7]), (0.75, "YY", [2, 3]), (0.1, "XX", [2, 3])]
+    H = _ham_obs(ops_module, dt, terms)
+    spec = pauli_sum_spec(terms)
+    assert_close(m.expval(H), o.expval_obs(spec), dt, scale=100, what="E ham")
+    assert_close(m.var(H), o.var_obs(spec), dt, scale=1000, what="V ham")
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+def test_expval_mixed_observables(ops_module, oracle, dt):
+    from oracle.pyoracle import ObsData
+
+    rng, sv, m, o = _setup(ops_module, oracle, 7, dt, seed_of("mixed", dt.__name__))
+    Named, Herm, Prod, Ham, _ = obs_ns(ops_module, dt)
+    H2 = rand_hermitian(rng, 2)
+    od = ObsData()
+    off = od.add_matrix(H2)
+    obs = Ham([0.5, -1.25, 0.3],
+              [Prod([Named("PauliX", [0]), Herm(H2, [3, 5])]), Named("PauliY", [2]),
+               Prod([Named("Hadamard", [1]), Named("PauliZ", [6])])])
+    spec = (f"ham 3 0.5 prod 2 named PauliX 0 herm 2 3 5 {off} -1.25 named PauliY 2 "
+            f"0.3 prod 2 named Hadamard 1 named PauliZ 6")
+    assert_close(m.expval(obs), o.expval_obs(spec, od), dt, scale=100, what="E mixed")
+    assert_close(m.var(obs), o.var_obs(spec, od), dt, scale=1000, what="V mixed")
+    single = Prod([Named("PauliZ", [0]), Named("PauliZ", [1]), Named("PauliZ", [2])])
+    assert_close(m.expval(single), o.expval_obs("prod 3 named PauliZ 0 named PauliZ 1 named PauliZ 2"), dt,
+                 scale=10, what="E ZZZ")
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+def test_expval_sparse(ops_module, oracle, dt):
+    import scipy.sparse as sp
+
+    rng, sv, m, o = _setup(ops_module, oracle, 7, dt, seed_of("sp", dt.__name__))
+    A = sp.random(128, 128, density=0.05, random_state=3) + 1j * sp.random(128, 128, density=0.05, random_state=4)
+    A = (A + A.conj().T).tocsr()
+    A.sort_indices()
+    assert_close(m.expval(A.indptr, A.indices, A.data), o.expval_sparse(A.indptr, A.indices, A.data), dt,
+                 scale=100, what="E sparse")
+    *_, Sparse = obs_ns(ops_module, dt)
+    obs = Sparse(A.data, A.indices, A.indptr, list(range(7)))
+    assert_close(m.expval(obs), o.expval_sparse(A.indptr, A.indices, A.data), dt, scale=100, what="E sparseH")
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+def test_samples_exact(ops_module, oracle, dt):
+    # Integer outputs under a fixed seed must be identical to the oracle's.
+    _, sv, m, o = _setup(ops_module, oracle, 8, dt, seed_of("samples", dt.__name__))
+    m.set_random_seed(37)
+    s = m.generate_samples(8, 5000)
+    assert s.shape == (5000, 8)
+    assert np.array_equal(s.astype(np.int64), o.samples(5000, 37))
+    for wires in ([3], [7, 0, 2]):
+        s = m.generate_samples(wires, 3000)
+        assert np.array_equal(s.astype(np.int64), o.samples(3000, 37, wires))

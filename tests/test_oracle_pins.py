@@ -1,0 +1,229 @@
+"""CPU tests that pin the oracle (the LM restatement in oracle/lm_oracle.hpp).
+
+1. Against the golden fixtures generated from the reference's own C++
+   (tests/golden/make_golden.py) — runs everywhere.
+2. Against the reference shim directly, on fresh random inputs — runs where
+   oracle/_ref/libplref.so could be built from the reference checkout.
+3. Against the reference's own known-answer values
+   (core/algorithms/tests/Test_AdjointJacobian.cpp:336-431).
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from gate_table import CONTROLLED_GATES, CONTROLLED_GENERATORS, GATES, GENERATORS, gate_params, gate_wires
+from helpers import assert_close, rand_state, rand_unitary, seed_of
+
+GOLDEN = Path(__file__).resolve().parent / "golden" / "golden_lq.npz"
+DT = {"c128": np.complex128, "c64": np.complex64}
+
+
+@pytest.fixture(scope="module")
+def golden():
+    g = np.load(GOLDEN)
+    return g, json.loads(str(g["meta"]))
+
+
+def _ref():
+    from oracle.pyoracle import Oracle, available
+
+    if not available("ref"):
+        pytest.skip("reference shim not built here (no reference checkout)")
+    return Oracle("ref")
+
+
+@pytest.mark.parametrize("tag", ["c128", "c64"])
+def test_golden_gates(oracle, golden, tag):
+    g, meta = golden
+    dt = DT[tag]
+    st = g[f"state_in_{tag}"]
+    n = 5
+    checked = 0
+    for key, m in meta.items():
+        if not key.startswith((f"gate_{tag}_", f"cgate_{tag}_", f"gen_{tag}_", f"cgen_{tag}_", f"mat_{tag}_")):
+            continue
+        o = oracle.sv(n, dt)
+        o.set_state(st)
+        kind = key.split("_")[0]
+        if kind == "gate":
+            o.apply(key.split("_")[2], m["wires"], m["inverse"], m["params"])
+        elif kind == "cgate":
+            o.apply(key.split("_")[2], m["wires"], False, m["params"], m["cwires"], m["cvals"])
+        elif kind == "gen":
+            assert o.apply_generator(key.split("_")[2], m["wires"]) == m["scale"]
+        elif kind == "cgen":
+            assert o.apply_generator(key.split("_")[2], m["wires"], False, m["cwires"], m["cvals"]) == m["scale"]
+        else:
+            o.apply_matrix(g[key + "_U"], m["wires"], m["inverse"])
+        assert_close(o.state(), g[key], dt, scale=4, what=key)
+        checked += 1
+    assert checked > 130
+
+
+@pytest.mark.parametrize("tag", ["c128", "c64"])
+def test_golden_measurements(oracle, golden, tag):
+    g, meta = golden
+    dt = DT[tag]
+    o = oracle.sv(5, dt)
+    o.set_state(g[f"state_in_{tag}"])
+    for i in range(8):
+        assert_close(o.probs(meta[f"probs_{tag}_{i}"]["wires"]), g[f"probs_{tag}_{i}"], dt, what=f"probs {i}")
+    for name in ("PauliX", "PauliY", "PauliZ", "Hadamard"):
+        assert_close([o.expval_named(name, [w]) for w in range(5)], g[f"expval_{tag}_{name}"], dt, scale=10)
+    from oracle.pyoracle import pauli_sum_spec
+
+    spec = pauli_sum_spec([tuple(t) for t in meta[f"ham_{tag}"]["terms"]])
+    assert_close([o.expval_obs(spec), o.var_obs(spec)], g[f"ham_{tag}"], dt, scale=100, what="ham")
+    # seeded samples: exact integers
+    assert np.array_equal(o.samples(2000, 37), g[f"samples_{tag}"])
+    assert np.array_equal(o.samples(2000, 37, [3, 0]), g[f"samples_w_{tag}"])
+
+
+def test_golden_config0_small(oracle, golden):
+    from lightning_gb300.workloads import config0, sum_z
+    from oracle.pyoracle import pauli_sum_spec
+
+    g, _ = golden
+    circuit = config0(8, 3, seed=1000)
+    o = oracle.sv(8, np.complex128)
+    for op in circuit:
+        o.apply(op.name, op.wires, False, op.params)
+    st = o.state()
+    assert_close(st[g["config0_small_idx"]], g["config0_small_amps"], np.complex128, what="state")
+    spec = pauli_sum_spec(sum_z(8).terms())
+    assert abs(o.expval_obs(spec) - g["config0_small_expval"][0]) < 1e-12
+    tp = list(range(sum(1 for op in circuit if op.params)))
+    jac = oracle.sv(8, np.complex128).adjoint([op.as_dict() for op in circuit], [spec], tp, apply_ops=True)[0]
+    assert np.max(np.abs(jac - g["config0_small_jac"])) < 1e-12
+
+
+def test_golden_config1_config3_small(oracle, golden):
+    from lightning_gb300.workloads import config1, config3
+    from oracle.pyoracle import pauli_sum_spec
+
+    g, _ = golden
+    circuit, ham = config1(12, 4, seed=1001)
+    o = oracle.sv(12, np.complex128)
+    for op in circuit:
+        if op.matrix is not None:
+            o.apply_matrix(op.matrix, op.wires, False)
+        else:
+            o.apply(op.name, op.wires, False, op.params)
+    assert_close(o.state(), g["config1_small_state"], np.complex128, scale=10, what="config1 state")
+    assert abs(o.expval_obs(pauli_sum_spec(ham.terms())) - g["config1_small_expval"][0]) < 1e-11
+    circuit, ham = config3(8, 3, seed=1003, nterms=20)
+    tp = list(range(sum(1 for op in circuit if op.params)))
+    jac = oracle.sv(8, np.complex128).adjoint([op.as_dict() for op in circuit], [pauli_sum_spec(ham.terms())], tp,
+                                              apply_ops=True)[0]
+    assert np.max(np.abs(jac - g["config3_small_jac"])) < 1e-11
+
+
+def test_known_answers_adjoint(oracle):
+    # Test_AdjointJacobian.cpp:336-373 and :375-431
+    p = [-np.pi / 7, np.pi / 5, 2 * np.pi / 3]
+    ops = [dict(name="RX", params=[p[i]], wires=[i]) for i in range(3)]
+    j = oracle.sv(3).adjoint(ops, ["prod 3 named PauliZ 0 named PauliZ 1 named PauliZ 2"], [0, 1, 2], apply_ops=True)
+    np.testing.assert_allclose(j[0], [-0.1755096592645253, 0.26478810666384334, -0.6312451595102775], atol=1e-7)
+    cnot = np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0]], dtype=np.complex128)
+    ops = [dict(name="RZ", params=[p[0]], wires=[0]), dict(name="RY", params=[p[1]], wires=[0]),
+           dict(name="RZ", params=[p[2]], wires=[0]), dict(name="QubitUnitary", wires=[0, 1], matrix=cnot),
+           dict(name="CNOT", wires=[1, 2]), dict(name="RZ", params=[p[0]], wires=[1]),
+           dict(name="RY", params=[p[1]], wires=[1]), dict(name="RZ", params=[p[2]], wires=[1])]
+    j = oracle.sv(3).adjoint(ops, ["prod 3 named PauliX 0 named PauliX 1 named PauliX 2"], list(range(6)),
+                             apply_ops=True)
+    np.testing.assert_allclose(j[0], [0.0, -0.674214427, 0.275139672, 0.275139672, -0.0129093062, 0.323846156],
+                               atol=1e-7)
+
+
+# ---------------------------------------------------------------- direct pins vs the reference shim
+@pytest.mark.parametrize("dt", [np.complex128, np.complex64])
+def test_restatement_vs_reference_gates(oracle, dt):
+    ref = _ref()
+    rng = np.random.default_rng(seed_of("pin-gates", dt.__name__))
+    n = 6
+    for name in GATES:
+        for inv in (False, True):
+            st = rand_state(rng, n, dt)
+            w = gate_wires(name, rng, n)
+            p = gate_params(name, rng)
+            a, b = oracle.sv(n, dt), ref.sv(n, dt)
+            a.set_state(st)
+            b.set_state(st)
+            a.apply(name, w, inv, p)
+            b.apply(name, w, inv, p)
+            assert_close(a.state(), b.state(), dt, what=name)
+    for name in CONTROLLED_GATES:
+        nwk = GATES[name][0] or 2
+        ws = [int(x) for x in rng.choice(n, size=nwk + 2, replace=False)]
+        cv = [bool(x) for x in rng.integers(0, 2, size=2)]
+        p = gate_params(name, rng)
+        st = rand_state(rng, n, dt)
+        a, b = oracle.sv(n, dt), ref.sv(n, dt)
+        a.set_state(st)
+        b.set_state(st)
+        a.apply(name, ws[:nwk], True, p, ws[nwk:], cv)
+        b.apply(name, ws[:nwk], True, p, ws[nwk:], cv)
+        assert_close(a.state(), b.state(), dt, what="C" + name)
+    for name in GENERATORS:
+        w = gate_wires(name, rng, n)
+        st = rand_state(rng, n, dt)
+        a, b = oracle.sv(n, dt), ref.sv(n, dt)
+        a.set_state(st)
+        b.set_state(st)
+        assert a.apply_generator(name, w) == b.apply_generator(name, w)
+        assert_close(a.state(), b.state(), dt, what="gen " + name)
+    for name in CONTROLLED_GENERATORS:
+        nwk = GATES[name][0] or 2
+        ws = [int(x) for x in rng.choice(n, size=nwk + 1, replace=False)]
+        st = rand_state(rng, n, dt)
+        a, b = oracle.sv(n, dt), ref.sv(n, dt)
+        a.set_state(st)
+        b.set_state(st)
+        assert a.apply_generator(name, ws[:nwk], False, ws[nwk:], [True]) == \
+            b.apply_generator(name, ws[:nwk], False, ws[nwk:], [True])
+        assert_close(a.state(), b.state(), dt, what="cgen " + name)
+
+
+@pytest.mark.parametrize("dt", [np.complex128, np.complex64])
+def test_restatement_vs_reference_measurements(oracle, dt):
+    from oracle.pyoracle import ObsData, pauli_sum_spec
+
+    ref = _ref()
+    rng = np.random.default_rng(seed_of("pin-meas", dt.__name__))
+    n = 7
+    st = rand_state(rng, n, dt)
+    a, b = oracle.sv(n, dt), ref.sv(n, dt)
+    a.set_state(st)
+    b.set_state(st)
+    for wires in (None, [3], [6, 1], [2, 5, 0], list(range(n))[::-1]):
+        assert_close(a.probs(wires), b.probs(wires), dt)
+    for k in (1, 2, 3, 4):
+        U = rand_unitary(rng, k)
+        H = U + U.conj().T
+        w = [int(x) for x in rng.choice(n, size=k, replace=False)]
+        assert_close(a.expval_matrix(H, w), b.expval_matrix(H, w), dt, scale=100)
+    terms = [(float(rng.normal()), "".join(rng.choice(list("XYZ"), size=m)),
+              [int(x) for x in rng.choice(n, size=m, replace=False)]) for m in (1, 2, 3, 4)]
+    spec = pauli_sum_spec(terms)
+    assert_close(a.expval_obs(spec), b.expval_obs(spec), dt, scale=100)
+    od = ObsData()
+    off = od.add_matrix(rand_unitary(rng, 1) + rand_unitary(rng, 1).conj().T)
+    spec2 = f"ham 2 0.5 prod 2 named PauliX 0 herm 1 3 {off} -1.25 named Hadamard 2"
+    assert_close(a.var_obs(spec2, od), b.var_obs(spec2, od), dt, scale=100)
+    assert np.array_equal(a.samples(3000, 11), b.samples(3000, 11))
+
+
+def test_restatement_vs_reference_adjoint(oracle):
+    from lightning_gb300.workloads import config3
+    from oracle.pyoracle import pauli_sum_spec
+
+    ref = _ref()
+    circuit, ham = config3(6, 2, seed=5, nterms=15)
+    tp = list(range(0, sum(1 for op in circuit if op.params), 2))
+    ops = [op.as_dict() for op in circuit]
+    specs = [pauli_sum_spec(ham.terms()), "named PauliX 1"]
+    ja = oracle.sv(6).adjoint(ops, specs, tp, apply_ops=True)
+    jb = ref.sv(6).adjoint(ops, specs, tp, apply_ops=True)
+    assert np.max(np.abs(ja - jb)) < 1e-11

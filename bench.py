@@ -1,0 +1,367 @@
+#!/usr/bin/env python3
+"""Benchmark: gate-application bandwidth of the 30-qubit complex128 random
+circuit (20 cycles of a Haar SU(2) on every qubit followed by CZ on 15
+disjoint pairs), the single-large-circuit configuration the GB300 target is
+quoted on.
+
+A *step* applies the whole circuit (600 SU(2) + 300 CZ gates) to a state that
+is resident in HBM.  ``value`` is the unfused algorithmic traffic of the
+step (sum over gates of 2 f N S, f = fraction of amplitudes a gate changes)
+divided by the step time, in GB/s; ``e2e`` is the same metric through the
+public binding with the state copied in from pinned host memory and back out
+every step.  The 16 GiB state is far larger than L2, so no flush is needed.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU
+(the path does not shard; replicas only) and rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path[:0] = [str(REPO), str(REPO / "pennylane-lightning_gb300")]
+
+METRIC = "30q c128 gate GB/s (unfused-equivalent algorithmic bytes / s)"
+UNIT = "GB/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--qubits", type=int, default=30)
+    ap.add_argument("--cycles", type=int, default=20)
+    ap.add_argument("--no-c64", action="store_true", help="skip the complex64 variant")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return ap.parse_args()
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.idx)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------- workload
+def workload(n, cycles):
+    from lightning_gb300.workloads import config1, unfused_bytes
+
+    circuit, ham = config1(n, cycles, seed=1001)
+    return circuit, ham, unfused_bytes
+
+
+def apply_circuit(sv, circuit, mats, on_dense=None):
+    for i, op in enumerate(circuit):
+        if op.matrix is not None:
+            if on_dense is not None:
+                on_dense(0)
+            sv.applyMatrix(mats[i], op.wires, False)
+            if on_dense is not None:
+                on_dense(1)
+        else:
+            getattr(sv, op.name)(op.wires, False, op.params)
+
+
+def traffic_from_profiles(kernel_tag: str):
+    """Per-launch DRAM bytes (read + write) recorded in profiles/<tag>.md."""
+    p = REPO / "profiles" / f"{kernel_tag}.md"
+    if not p.exists():
+        return None
+    for ln in p.read_text().splitlines():
+        if ln.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(ln.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def gpu_arm(args) -> dict | None:
+    import torch
+
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from lightning_gb300 import lightning_gb300_ops as ops
+
+    peaks = json.loads((REPO / "MEASURED_PEAKS.json").read_text()) if (REPO / "MEASURED_PEAKS.json").exists() else {}
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+
+    n, cycles = args.qubits, args.cycles
+    circuit, ham, unfused_bytes = workload(n, cycles)
+    mats = [np.ascontiguousarray(op.matrix, dtype=np.complex128) if op.matrix is not None else None for op in circuit]
+    alg_bytes = unfused_bytes(circuit, n, 16)
+    n_dense = sum(1 for op in circuit if op.matrix is not None)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    sv = ops.StateVectorC128(n)
+    stream = torch.cuda.ExternalStream(sv.cuda_stream())
+    for _ in range(args.warmup):
+        apply_circuit(sv, circuit, mats)
+    sv.synchronize()
+
+    # per-launch events for the dominant kernel (dense one-qubit update)
+    ev = [[torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)]
+          for _ in range(n_dense * args.steps)]
+    cursor = [0]
+
+    def on_dense(which):
+        ev[cursor[0]][which].record(stream)
+        if which == 1:
+            cursor[0] += 1
+
+    step_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches0 = ops.kernel_launches()
+    barrier()
+    sv.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            step_ev[k][0].record(stream)
+            apply_circuit(sv, circuit, mats, on_dense)
+            step_ev[k][1].record(stream)
+        sv.synchronize()
+        barrier()
+        wall = time.perf_counter() - t0
+    launches = ops.kernel_launches() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in step_ev]
+    total_s = sum(step_ms) / 1e3
+    if ws > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    dense_ms = [a.elapsed_time(b) for a, b in ev[: cursor[0]]]
+    dense_avg_s = statistics.mean(dense_ms) / 1e3
+    dense_bytes = 2.0 * (1 << n) * 16
+    achieved = dense_bytes / dense_avg_s / 1e9
+    traffic = traffic_from_profiles("k_1q_dense_c128")
+    if traffic is not None:
+        traffic = traffic * ((1 << n) / float(1 << 28))  # profile captured at 28 qubits, scaled per launch
+
+    # expectation value of the 64-term Hamiltonian (one read per flip-mask group)
+    H = ops.observables.HamiltonianC128(
+        ham.coeffs, [ops.observables.TensorProdObsC128(
+            [ops.observables.NamedObsC128({"X": "PauliX", "Y": "PauliY", "Z": "PauliZ"}[c], [w])
+             for c, w in zip(word, wires)]) for word, wires in zip(ham.words, ham.wires)])
+    m = ops.MeasurementsC128(sv)
+    m.expval(H)
+    t = time.perf_counter()
+    ev_val = m.expval(H)
+    expval_ms = (time.perf_counter() - t) * 1e3
+
+    # e2e through the binding: pinned host state in, circuit, state out
+    host_in = torch.empty(1 << n, dtype=torch.complex128, pin_memory=True)
+    host_out = torch.empty(1 << n, dtype=torch.complex128, pin_memory=True)
+    host_in.zero_()
+    host_in[0] = 1.0
+    hin, hout = host_in.numpy(), host_out.numpy()
+    e2e_steps = max(1, min(args.steps, 2))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sv.updateData(hin)
+        apply_circuit(sv, circuit, mats)
+        sv.getState(hout)
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    h2d = (1 << n) * 16 + sum(m_.nbytes for m_ in mats if m_ is not None)
+    d2h = (1 << n) * 16
+    del sv
+
+    res = {
+        "metric": METRIC, "value": ws * alg_bytes * args.steps / total_s / 1e9, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64 arithmetic)",
+        "data": "synthetic (seeded Haar SU(2) + CZ circuit, seed 1001)",
+        "config": {"workload": f"config1: {n} qubits complex128, {cycles} cycles x ({n} Haar SU(2) + {n // 2} CZ)",
+                   "qubits": n, "gates_per_step": len(circuit), "algorithmic_bytes_per_step": alg_bytes,
+                   "l2": "inputs larger than L2 (16 GiB state)", "parallelism": f"replicas x{ws}",
+                   "path": "unfused per-gate kernels"},
+        "e2e": {"value": alg_bytes / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+        "roofline": {"kernel": "k_1q<double, DENSE> (dense SU(2) update)", "bound": "hbm", "achieved": achieved,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                     "peak_source": f"{peak_src} hbm_gbs",
+                     "traffic": traffic, "algorithmic_bytes_per_launch": dense_bytes,
+                     "avg_launch_ms": dense_avg_s * 1e3},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "expval_64_terms": {"value": ev_val, "ms": expval_ms},
+        "wall_s_timed": wall,
+    }
+    if not args.no_c64:
+        sv64 = ops.StateVectorC64(n)
+        apply_circuit(sv64, circuit, mats)
+        sv64.synchronize()
+        s64 = torch.cuda.ExternalStream(sv64.cuda_stream())
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s64)
+        apply_circuit(sv64, circuit, mats)
+        b.record(s64)
+        sv64.synchronize()
+        ms = a.elapsed_time(b)
+        res["c64"] = {"value": unfused_bytes(circuit, n, 8) / (ms / 1e3) / 1e9, "unit": UNIT, "ms_per_step": ms}
+        del sv64
+    return res
+
+
+# --------------------------------------------------------------------------- CPU legs
+def cpu_setup():
+    ncores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(ncores))
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+    os.environ.setdefault("OMP_PLACES", "cores")
+    from oracle.build_oracle import build_restatement
+    from oracle.pyoracle import Oracle
+
+    build_restatement()
+    return Oracle("orc")
+
+
+def cpu_sample(orc, n_cpu: int, reps: int = 1):
+    """Config-1's first cycle at `n_cpu` qubits, timed on the host cores."""
+    from lightning_gb300.workloads import config1, unfused_bytes
+
+    circuit, _ = config1(n_cpu, 1, seed=1001)
+    sv = orc.sv(n_cpu, np.complex128)
+    for op in circuit[:2]:
+        sv.apply_matrix(op.matrix, op.wires) if op.matrix is not None else sv.apply(op.name, op.wires)
+    times = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        for op in circuit:
+            if op.matrix is not None:
+                sv.apply_matrix(op.matrix, op.wires)
+            else:
+                sv.apply(op.name, op.wires)
+        times.append(time.perf_counter() - t)
+    b = unfused_bytes(circuit, n_cpu, 16)
+    return b, statistics.median(times), len(circuit), orc.num_threads()
+
+
+def reference_arm(args) -> None:
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    orc = cpu_setup()
+    n_cpu = min(args.qubits, 28)
+    for _ in range(args.warmup):
+        cpu_sample(orc, n_cpu)
+    vals = []
+    t_total = 0.0
+    for _ in range(args.steps):
+        b, t, ng, threads = cpu_sample(orc, n_cpu)
+        vals.append(b / t / 1e9)
+        t_total += t
+    v = statistics.median(vals)
+    sample = (f"first cycle of the config-1 circuit ({ng} gates) at {n_cpu} qubits complex128 per step; "
+              f"LM-kernel restatement with OpenMP (port of lightning.qubit's algorithm; no AVX on this host)")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_total * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64 arithmetic)", "data": "synthetic",
+        "config": {"workload": f"config1 cycle sample at {n_cpu} qubits (CPU)", "qubits": n_cpu},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    ws, rank, _ = dist_info()
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        orc = cpu_setup()
+        n_cpu = min(args.qubits, 28)
+        b, t, ng, threads = cpu_sample(orc, n_cpu)
+        cpu = {"value": b / t / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"first cycle of the config-1 circuit ({ng} gates) at {n_cpu} qubits complex128, "
+                         f"{t:.1f} s; LM-kernel restatement with OpenMP on the host cores"}
+    res = gpu_arm(args)
+    if rank == 0 and res is not None:
+        res["cpu_baseline"] = cpu
+        print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

@@ -52,6 +52,8 @@ int plgb_backend_info(char *buf, size_t len);
 /* JSON text with CUDA device / compile details; compile_info(), runtime_info() */
 int plgb_runtime_info(char *buf, size_t len);
 int plgb_device_count(int *out);
+/* number of kernels this library has launched in the process (monotonic) */
+int plgb_kernel_launches(uint64_t *out);
 
 /* ---- state vector (StateVectorLQubitManaged.hpp:52-188,
  *      StateVectorLQubit.hpp:359-1036, Bindings.hpp:870-922,
@@ -70,6 +72,9 @@ int plgb_sv_precision(const plgb_sv *sv, int *out);
 int plgb_sv_length(const plgb_sv *sv, uint64_t *out);
 int plgb_sv_device_ptr(plgb_sv *sv, void **out);
 int plgb_sv_synchronize(plgb_sv *sv);
+/* the CUDA stream (cudaStream_t) the state vector's kernels run on, so a
+ * caller can time them with CUDA events or order its own work after them */
+int plgb_sv_stream(plgb_sv *sv, void **out);
 /* resetStateVector (StateVectorLQubit.hpp:959-963) */
 int plgb_sv_reset(plgb_sv *sv);
 /* setBasisState(state, wires) (StateVectorLQubit.hpp:939-957) */

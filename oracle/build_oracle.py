@@ -26,7 +26,9 @@ HERE = Path(__file__).resolve().parent
 REF_ROOT = Path(os.environ.get("PL_REFERENCE_ROOT", "/root/reference"))
 REF_OUT = HERE / "_ref"
 
-CXXFLAGS = ["-std=c++20", "-O3", "-DNDEBUG", "-fPIC", "-fopenmp"]
+# -ffp-contract=off: no FMA contraction, so the restatement rounds like the
+# reference's x86 build (which has no FMA unit enabled) on every host.
+CXXFLAGS = ["-std=c++20", "-O3", "-DNDEBUG", "-fPIC", "-fopenmp", "-ffp-contract=off"]
 
 
 def _run(cmd: list[str]) -> None:

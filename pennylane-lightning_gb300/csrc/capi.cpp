@@ -124,6 +124,13 @@ int plgb_device_count(int *out) {
     });
 }
 
+int plgb_kernel_launches(uint64_t *out) {
+    return guard([&] {
+        need(out, "out");
+        *out = launch_count();
+    });
+}
+
 int plgb_backend_info(char *buf, size_t len) {
     return copy_text("{\"NAME\": \"lightning.gb300\", \"ARCH\": \"sm_103a\", \"REFERENCE\": \"lightning.qubit\"}", buf,
                      len);
@@ -233,6 +240,12 @@ int plgb_sv_device_ptr(plgb_sv *sv, void **out) {
 }
 int plgb_sv_synchronize(plgb_sv *sv) {
     return with_sv(sv, [&](auto &s) { s.synchronize(); });
+}
+int plgb_sv_stream(plgb_sv *sv, void **out) {
+    return with_sv(sv, [&](auto &s) {
+        need(out, "out");
+        *out = static_cast<void *>(s.stream());
+    });
 }
 int plgb_sv_reset(plgb_sv *sv) {
     return with_sv(sv, [&](auto &s) { s.reset(); });

@@ -72,8 +72,13 @@ struct DeviceScratch {
     void *mat{nullptr};         // matrices / diagonals / offsets
     size_t mat_bytes{0};
     void ensure_mat(size_t bytes);
+    // Carve consecutive sub-buffers of the given byte sizes out of `mat`,
+    // each starting on a 256-byte boundary (16-byte vector loads of
+    // complex128 need at least 16).
+    std::vector<char *> carve(std::initializer_list<size_t> sizes);
     ~DeviceScratch();
 };
+inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 
 template <class T> class StateVector {
   public:

@@ -218,13 +218,12 @@ template <class T> void Measure<T>::apply_obs(StateVector<T> &sv, const ObsNode 
                      "SparseH wire count does not match state-vector size");
         StateVector<T> src(sv);
         const int64_t nnz = static_cast<int64_t>(o.sp_data.size());
-        const size_t bytes = (o.sp_indptr.size() + static_cast<size_t>(nnz)) * sizeof(long long) +
-                             static_cast<size_t>(nnz) * sizeof(cx<T>);
-        sv.scratch().ensure_mat(bytes + 64);
-        char *base = static_cast<char *>(sv.scratch().mat);
-        long long *dip = reinterpret_cast<long long *>(base);
-        long long *dix = dip + o.sp_indptr.size();
-        cx<T> *dval = reinterpret_cast<cx<T> *>(base + (o.sp_indptr.size() + static_cast<size_t>(nnz)) * sizeof(long long));
+        const auto bufs = sv.scratch().carve({o.sp_indptr.size() * sizeof(long long),
+                                              static_cast<size_t>(nnz) * sizeof(long long),
+                                              static_cast<size_t>(nnz) * sizeof(cx<T>)});
+        long long *dip = reinterpret_cast<long long *>(bufs[0]);
+        long long *dix = reinterpret_cast<long long *>(bufs[1]);
+        cx<T> *dval = reinterpret_cast<cx<T> *>(bufs[2]);
         std::vector<cx<T>> vals(static_cast<size_t>(nnz));
         for (size_t i = 0; i < vals.size(); i++) {
             vals[i] = cx<T>{static_cast<T>(o.sp_data[i].real()), static_cast<T>(o.sp_data[i].imag())};
@@ -381,13 +380,12 @@ double Measure<T>::expval_sparse(StateVector<T> &sv, const int64_t *indptr, int6
                                  const cd *data, int64_t nnz) {
     // MeasurementsLQubit.hpp:322-338
     PLGB_REQUIRE(static_cast<u64>(nptr - 1) == sv.length(), "Statevector and Hamiltonian have incompatible sizes.");
-    const size_t bytes = (static_cast<size_t>(nptr) + static_cast<size_t>(nnz)) * sizeof(long long) +
-                         static_cast<size_t>(nnz) * sizeof(cx<T>);
-    sv.scratch().ensure_mat(bytes + 64);
-    char *base = static_cast<char *>(sv.scratch().mat);
-    long long *dip = reinterpret_cast<long long *>(base);
-    long long *dix = dip + nptr;
-    cx<T> *dval = reinterpret_cast<cx<T> *>(base + (static_cast<size_t>(nptr) + static_cast<size_t>(nnz)) * sizeof(long long));
+    const auto bufs = sv.scratch().carve({static_cast<size_t>(nptr) * sizeof(long long),
+                                          static_cast<size_t>(nnz) * sizeof(long long),
+                                          static_cast<size_t>(nnz) * sizeof(cx<T>)});
+    long long *dip = reinterpret_cast<long long *>(bufs[0]);
+    long long *dix = reinterpret_cast<long long *>(bufs[1]);
+    cx<T> *dval = reinterpret_cast<cx<T> *>(bufs[2]);
     std::vector<cx<T>> vals(static_cast<size_t>(nnz));
     for (size_t i = 0; i < vals.size(); i++) {
         vals[i] = cx<T>{static_cast<T>(data[i].real()), static_cast<T>(data[i].imag())};

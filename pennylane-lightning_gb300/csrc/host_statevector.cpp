@@ -7,6 +7,7 @@
 #include "host.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <unordered_map>
@@ -26,6 +27,10 @@ int LaunchGeom::sm_count() {
     return sms;
 }
 
+static std::atomic<unsigned long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+unsigned long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
 static thread_local std::string g_last_error;
 void set_last_error(const std::string &msg) { g_last_error = msg; }
 const char *last_error() { return g_last_error.c_str(); }
@@ -41,6 +46,21 @@ void DeviceScratch::ensure_mat(size_t bytes) {
     cuda_check(cudaMalloc(&mat, bytes), "cudaMalloc(scratch)");
     mat_bytes = bytes;
 }
+std::vector<char *> DeviceScratch::carve(std::initializer_list<size_t> sizes) {
+    size_t total = 0;
+    for (auto sz : sizes) {
+        total += align_up(sz);
+    }
+    ensure_mat(total + 256);
+    std::vector<char *> out;
+    char *p = static_cast<char *>(mat);
+    for (auto sz : sizes) {
+        out.push_back(p);
+        p += align_up(sz);
+    }
+    return out;
+}
+
 DeviceScratch::~DeviceScratch() {
     if (red) {
         cudaFree(red);
@@ -216,9 +236,9 @@ void StateVector<T>::set_state_vector(const std::complex<T> *host_state, u64 len
             return;
         }
     }
-    scratch_.ensure_mat(len * (sizeof(CT) + sizeof(u64)));
-    CT *dsub = static_cast<CT *>(scratch_.mat);
-    u64 *dloc = reinterpret_cast<u64 *>(static_cast<char *>(scratch_.mat) + len * sizeof(CT));
+    const auto bufs = scratch_.carve({len * sizeof(CT), len * sizeof(u64)});
+    CT *dsub = reinterpret_cast<CT *>(bufs[0]);
+    u64 *dloc = reinterpret_cast<u64 *>(bufs[1]);
     std::vector<u64> loc(len);
     const size_t k = wires.size();
     for (u64 j = 0; j < len; j++) {
@@ -363,9 +383,9 @@ void StateVector<T>::prim_dense(const std::vector<int64_t> &wires, const std::ve
         }
     }
     const size_t mbytes = D * D * sizeof(CT);
-    scratch_.ensure_mat(mbytes + D * sizeof(u64));
-    CT *dm = static_cast<CT *>(scratch_.mat);
-    u64 *dloc = reinterpret_cast<u64 *>(static_cast<char *>(scratch_.mat) + mbytes);
+    const auto bufs = scratch_.carve({mbytes, D * sizeof(u64)});
+    CT *dm = reinterpret_cast<CT *>(bufs[0]);
+    u64 *dloc = reinterpret_cast<u64 *>(bufs[1]);
     cuda_check(cudaMemcpyAsync(dm, mat.data(), mbytes, cudaMemcpyHostToDevice, s_), "H2D matrix");
     cuda_check(cudaMemcpyAsync(dloc, loc.data(), D * sizeof(u64), cudaMemcpyHostToDevice, s_), "H2D offsets");
     launch_kq<T>(s_, d_, g, static_cast<int>(k), lo, dm, dloc);

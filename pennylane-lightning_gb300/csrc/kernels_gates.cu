@@ -99,6 +99,7 @@ void launch_1q(cudaStream_t s, cx<T> *sv, const GroupGeom &g, u64 o0, u64 o1, in
     default: throw std::runtime_error("launch_1q: bad mode");
     }
     cuda_check(cudaGetLastError(), "k_1q launch");
+    note_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -145,6 +146,7 @@ void launch_2q(cudaStream_t s, cx<T> *sv, const GroupGeom &g, int bit_hi_local, 
         k_2q<T, false><<<grid, B, 0, s>>>(sv, g, off1, off0, m);
     }
     cuda_check(cudaGetLastError(), "k_2q launch");
+    note_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -224,6 +226,7 @@ void launch_kq(cudaStream_t s, cx<T> *sv, const GroupGeom &g, int k, const Local
     }
     }
     cuda_check(cudaGetLastError(), "k_kq launch");
+    note_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -249,6 +252,7 @@ template <class T>
 void launch_diag(cudaStream_t s, cx<T> *sv, u64 N, u64 cmask, u64 cval, int k, const TBits &tb, const cx<T> *dd) {
     k_diag<T><<<grid_for(N, 256, 8), 256, 0, s>>>(sv, N, cmask, cval, k, tb, dd);
     cuda_check(cudaGetLastError(), "k_diag launch");
+    note_launch();
 }
 
 // Parity phase: a[i] *= s[popcount(i & pmask) & 1] where (i & cmask) == cval
@@ -275,6 +279,7 @@ void launch_parity(cudaStream_t s, cx<T> *sv, u64 N, u64 pmask, u64 cmask, u64 c
                    bool zero_outside) {
     k_parity<T><<<grid_for(N, 256, 8), 256, 0, s>>>(sv, N, pmask, cmask, cval, s0, s1, zero_outside ? 1 : 0);
     cuda_check(cudaGetLastError(), "k_parity launch");
+    note_launch();
 }
 
 // PauliRot (LM:577-629): pairs (i, i ^ mask_xy), i < partner.
@@ -304,6 +309,7 @@ void launch_pauli_rot(cudaStream_t s, cx<T> *sv, int n, u64 mxy, u64 my, u64 mz,
     const int hb = 63 - __builtin_clzll(mxy);
     k_pauli_rot<T><<<grid_for(half, 256, 8), 256, 0, s>>>(sv, half, hb, mxy, my, mz, __builtin_popcountll(my), c, sn);
     cuda_check(cudaGetLastError(), "k_pauli_rot launch");
+    note_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -321,6 +327,7 @@ __global__ void k_zero_outside(cx<T> *__restrict__ a, u64 N, u64 cmask, u64 cval
 template <class T> void launch_zero_outside(cudaStream_t s, cx<T> *sv, u64 N, u64 cmask, u64 cval) {
     k_zero_outside<T><<<grid_for(N, 256, 8), 256, 0, s>>>(sv, N, cmask, cval);
     cuda_check(cudaGetLastError(), "k_zero_outside launch");
+    note_launch();
 }
 
 template <class T> __global__ void k_scale(cx<T> *__restrict__ a, u64 N, cx<T> f, u64 cmask, u64 cval) {
@@ -334,6 +341,7 @@ template <class T> __global__ void k_scale(cx<T> *__restrict__ a, u64 N, cx<T> f
 template <class T> void launch_scale(cudaStream_t s, cx<T> *sv, u64 N, cx<T> f, u64 cmask, u64 cval) {
     k_scale<T><<<grid_for(N, 256, 8), 256, 0, s>>>(sv, N, f, cmask, cval);
     cuda_check(cudaGetLastError(), "k_scale launch");
+    note_launch();
 }
 
 // y += f * x
@@ -346,6 +354,7 @@ template <class T> __global__ void k_axpy(cx<T> *__restrict__ y, const cx<T> *__
 template <class T> void launch_axpy(cudaStream_t s, cx<T> *y, const cx<T> *x, u64 N, cx<T> f) {
     k_axpy<T><<<grid_for(N, 256, 8), 256, 0, s>>>(y, x, N, f);
     cuda_check(cudaGetLastError(), "k_axpy launch");
+    note_launch();
 }
 
 // Scatter a 2^k sub-state onto the subspace where every other wire is 0
@@ -360,6 +369,7 @@ __global__ void k_scatter_sub(cx<T> *__restrict__ a, const cx<T> *__restrict__ s
 template <class T> void launch_scatter_sub(cudaStream_t s, cx<T> *sv, const cx<T> *sub, u64 D, const u64 *loc) {
     k_scatter_sub<T><<<grid_for(D, 256, 8), 256, 0, s>>>(sv, sub, D, loc);
     cuda_check(cudaGetLastError(), "k_scatter_sub launch");
+    note_launch();
 }
 
 // Sparse local operator on k wires (CSR, applyNCMultiQubitSparseOp LM:505-560),
@@ -391,6 +401,7 @@ void launch_sparse_local(cudaStream_t s, cx<T> *sv, const GroupGeom &g, const Lo
                          const long long *indptr, const long long *indices, const cx<T> *vals) {
     k_sparse_local<T><<<grid_for(g.ngroups, 128, 8), 128, 0, s>>>(sv, g, lo, k, indptr, indices, vals);
     cuda_check(cudaGetLastError(), "k_sparse_local launch");
+    note_launch();
 }
 
 #define PLGB_INST_GATES(T)                                                                                        \

@@ -63,6 +63,7 @@ template <int NOUT> __global__ void k_finalize(const double *__restrict__ partia
 template <int NOUT> static void finalize(cudaStream_t s, const double *partials, int nblocks, double *out) {
     k_finalize<NOUT><<<1, 32 * NOUT, 0, s>>>(partials, nblocks, out);
     cuda_check(cudaGetLastError(), "k_finalize launch");
+    note_launch();
 }
 
 static int reduce_grid(u64 work) {
@@ -87,6 +88,7 @@ template <class T> void reduce_norm2(cudaStream_t s, const cx<T> *sv, u64 N, dou
     const int g = reduce_grid(N);
     k_norm2<T><<<g, kReduceThreads, 0, s>>>(sv, N, partials);
     cuda_check(cudaGetLastError(), "k_norm2 launch");
+    note_launch();
     finalize<1>(s, partials, g, out);
 }
 
@@ -107,6 +109,7 @@ void reduce_inner(cudaStream_t s, const cx<T> *a, const cx<T> *b, u64 N, double 
     const int g = reduce_grid(N);
     k_inner<T><<<g, kReduceThreads, 0, s>>>(a, b, N, partials);
     cuda_check(cudaGetLastError(), "k_inner launch");
+    note_launch();
     finalize<2>(s, partials, g, out);
 }
 
@@ -144,6 +147,7 @@ void reduce_expval1(cudaStream_t s, const cx<T> *sv, u64 N, int tbit, int kind, 
     default: k_expval1<T, 3><<<g, kReduceThreads, 0, s>>>(sv, half, tbit, partials); break;
     }
     cuda_check(cudaGetLastError(), "k_expval1 launch");
+    note_launch();
     finalize<1>(s, partials, g, out);
 }
 
@@ -203,6 +207,7 @@ void reduce_pauli_group(cudaStream_t s, const cx<T> *sv, u64 N, const PauliGroup
     const int grid = reduce_grid(g.x == 0 ? N : N >> 1);
     k_pauli_group<T><<<grid, kReduceThreads, 0, s>>>(sv, N, g, partials);
     cuda_check(cudaGetLastError(), "k_pauli_group launch");
+    note_launch();
     finalize<1>(s, partials, grid, out);
 }
 
@@ -241,6 +246,7 @@ void reduce_pauli_transition(cudaStream_t s, const cx<T> *a, const cx<T> *b, u64
     const int g = reduce_grid(N);
     k_pauli_transition<T><<<g, kReduceThreads, 0, s>>>(a, b, N, x, yz, ny4, pmask, pval, partials);
     cuda_check(cudaGetLastError(), "k_pauli_transition launch");
+    note_launch();
     finalize<2>(s, partials, g, out);
 }
 
@@ -274,6 +280,7 @@ template <class T>
 void launch_pauli_accumulate(cudaStream_t s, const cx<T> *psi, cx<T> *out, u64 N, const PauliGroup &g, bool first) {
     k_pauli_accumulate<T><<<grid_for(N, 256, 8), 256, 0, s>>>(psi, out, N, g, first ? 1 : 0);
     cuda_check(cudaGetLastError(), "k_pauli_accumulate launch");
+    note_launch();
 }
 
 // Hermitian matrix on k wires: sum over groups of Re(v^H M v).
@@ -306,6 +313,7 @@ void reduce_expval_matrix(cudaStream_t s, const cx<T> *sv, const GroupGeom &g, i
     const int grid = reduce_grid(g.ngroups);
     k_expval_matrix<T><<<grid, kReduceThreads, 0, s>>>(sv, g, k, lo, dmat, partials);
     cuda_check(cudaGetLastError(), "k_expval_matrix launch");
+    note_launch();
     finalize<1>(s, partials, grid, out);
 }
 
@@ -334,6 +342,7 @@ void reduce_expval_csr(cudaStream_t s, const cx<T> *sv, u64 N, const long long *
     const int g = reduce_grid(N);
     k_expval_csr<T><<<g, kReduceThreads, 0, s>>>(sv, N, indptr, indices, vals, partials);
     cuda_check(cudaGetLastError(), "k_expval_csr launch");
+    note_launch();
     finalize<1>(s, partials, g, out);
 }
 
@@ -353,6 +362,7 @@ void launch_csr_apply(cudaStream_t s, const cx<T> *sv, cx<T> *out, u64 N, const 
                       const long long *indices, const cx<T> *vals) {
     k_csr_apply<T><<<grid_for(N, 256, 8), 256, 0, s>>>(sv, out, N, indptr, indices, vals);
     cuda_check(cudaGetLastError(), "k_csr_apply launch");
+    note_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -370,6 +380,7 @@ template <class T> __global__ void k_probs_all(const cx<T> *__restrict__ a, u64 
 template <class T> void launch_probs_all(cudaStream_t s, const cx<T> *sv, u64 N, T *out) {
     k_probs_all<T><<<grid_for(N, 256, 8), 256, 0, s>>>(sv, N, out);
     cuda_check(cudaGetLastError(), "k_probs_all launch");
+    note_launch();
 }
 
 // Marginal over k wires: shared-memory histogram for k <= 12, global
@@ -418,6 +429,7 @@ void launch_probs_marginal(cudaStream_t s, const cx<T> *sv, u64 N, int k, const 
     }
     k_probs_marginal<T><<<grid_for(N, 256, 2), 256, smem, s>>>(sv, N, k, tb, out);
     cuda_check(cudaGetLastError(), "k_probs_marginal launch");
+    note_launch();
 }
 
 #define PLGB_INST_MEAS(T)                                                                                         \

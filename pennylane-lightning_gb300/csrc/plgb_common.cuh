@@ -67,6 +67,11 @@ struct GroupGeom {
     int ins[PLGB_MAX_INS];
 };
 
+// Monotonic count of kernel launches issued by this library (all launchers
+// call note_launch() after a successful launch).
+void note_launch();
+unsigned long long launch_count();
+
 inline void cuda_check(cudaError_t e, const char *what) {
     if (e != cudaSuccess) {
         throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));

@@ -24,6 +24,7 @@ SIGNATURES = {
     "plgb_backend_info": (C.c_int, [C.c_char_p, C.c_size_t]),
     "plgb_runtime_info": (C.c_int, [C.c_char_p, C.c_size_t]),
     "plgb_device_count": (C.c_int, [IP]),
+    "plgb_kernel_launches": (C.c_int, [C.POINTER(C.c_uint64)]),
     "plgb_sv_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(VP)]),
     "plgb_sv_create_raw": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(VP)]),
     "plgb_sv_clone": (C.c_int, [VP, C.POINTER(VP)]),
@@ -33,6 +34,7 @@ SIGNATURES = {
     "plgb_sv_length": (C.c_int, [VP, C.POINTER(C.c_uint64)]),
     "plgb_sv_device_ptr": (C.c_int, [VP, C.POINTER(VP)]),
     "plgb_sv_synchronize": (C.c_int, [VP]),
+    "plgb_sv_stream": (C.c_int, [VP, C.POINTER(VP)]),
     "plgb_sv_reset": (C.c_int, [VP]),
     "plgb_sv_set_basis_state": (C.c_int, [VP, I64P, I64P, C.c_int]),
     "plgb_sv_set_state_vector": (C.c_int, [VP, VP, C.c_uint64, I64P, C.c_int]),

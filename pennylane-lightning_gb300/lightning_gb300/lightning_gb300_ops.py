@@ -91,6 +91,13 @@ def compile_info() -> dict:
             "AVX2": False, "AVX512F": False, "GPU.arch": info.get("compiled_for")}
 
 
+def kernel_launches() -> int:
+    """Kernels launched by the backend library so far in this process."""
+    v = C.c_uint64()
+    call("plgb_kernel_launches", C.byref(v))
+    return int(v.value)
+
+
 def allocate_aligned_array(size: int, dtype, zero_init: bool = False) -> np.ndarray:
     """Bindings.hpp:422-456: numpy array of `size` entries (64-byte aligned)."""
     dtype = np.dtype(dtype)
@@ -155,6 +162,12 @@ class _StateVectorBase:
 
     def synchronize(self) -> None:
         call("plgb_sv_synchronize", self._h)
+
+    def cuda_stream(self) -> int:
+        """Address of the cudaStream_t this state vector's kernels run on."""
+        p = VP()
+        call("plgb_sv_stream", self._h, C.byref(p))
+        return int(p.value or 0)
 
     def resetStateVector(self) -> None:
         call("plgb_sv_reset", self._h)

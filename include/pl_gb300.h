@@ -171,6 +171,13 @@ int plgb_ops_create(int nops, const char *const *names, const double *params, co
                     plgb_ops **out);
 int plgb_ops_destroy(plgb_ops *ops);
 int plgb_ops_num_par_ops(const plgb_ops *ops, int *out);
+/* StateVectorBase::applyOperations (core/simulators/base/StateVectorBase.hpp:
+ * 127-175): apply every operation of `ops` (each with its own inverse flag).
+ * tile_bits = 0 launches one kernel per gate; tile_bits = t > 0 fuses the
+ * list into shared-memory tile passes of up to 2^t amplitudes (the compiled
+ * passes are cached on `ops` per register size, precision and t).
+ * *passes_out (optional) receives the number of kernel passes per call. */
+int plgb_sv_apply_operations(plgb_sv *sv, plgb_ops *ops, int tile_bits, int *passes_out);
 /* AdjointJacobianC*.__call__(sv, observables, ops, trainable_params):
  * jac_out holds nobs * ntp doubles, row-major [obs][param].  With apply_ops
  * the operations are first applied to a copy of the state. */

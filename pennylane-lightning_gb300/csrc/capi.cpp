@@ -5,6 +5,9 @@
 
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <sstream>
 #include <variant>
 
@@ -20,6 +23,10 @@ struct plgb_obs {
 };
 struct plgb_ops {
     OpsList list;
+    // compiled fused programs, keyed by (num_qubits, precision, tile bits)
+    std::map<std::tuple<int, int, int>, std::shared_ptr<FusedProgram<float>>> prog_f;
+    std::map<std::tuple<int, int, int>, std::shared_ptr<FusedProgram<double>>> prog_d;
+    std::mutex mu;
 };
 
 namespace {
@@ -582,6 +589,50 @@ int plgb_ops_num_par_ops(const plgb_ops *ops, int *out) {
         *out = static_cast<int>(ops->list.num_par_ops());
     });
 }
+int plgb_sv_apply_operations(plgb_sv *sv, plgb_ops *ops, int tile_bits, int *passes_out) {
+    return with_sv(sv, [&](auto &s) {
+        need(ops, "ops");
+        using T = decltype(s.data()->x);
+        if (tile_bits <= 0) {
+            for (const auto &op : ops->list.ops) {
+                s.apply_op(op, op.inverse);
+            }
+            if (passes_out) {
+                *passes_out = static_cast<int>(ops->list.ops.size());
+            }
+            return;
+        }
+        PLGB_REQUIRE(tile_bits <= 14, "tile_bits must be in 1..14");
+        std::shared_ptr<FusedProgram<T>> prog;
+        {
+            std::lock_guard<std::mutex> lk(ops->mu);
+            const auto key = std::make_tuple(s.num_qubits(), static_cast<int>(sizeof(T)), tile_bits);
+            auto &cache = [&]() -> auto & {
+                if constexpr (std::is_same_v<T, double>) {
+                    return ops->prog_d;
+                } else {
+                    return ops->prog_f;
+                }
+            }();
+            auto it = cache.find(key);
+            if (it == cache.end()) {
+                std::vector<Prim<T>> prims;
+                for (const auto &op : ops->list.ops) {
+                    auto p = s.lower_op(op, op.inverse);
+                    prims.insert(prims.end(), std::make_move_iterator(p.begin()), std::make_move_iterator(p.end()));
+                }
+                it = cache.emplace(key, compile_fused<T>(s.num_qubits(), prims, tile_bits)).first;
+            }
+            prog = it->second;
+        }
+        run_fused<T>(s, *prog);
+        if (passes_out) {
+            const auto st = fused_stats<T>(*prog);
+            *passes_out = static_cast<int>(st.passes + st.unfused);
+        }
+    });
+}
+
 int plgb_adjoint_jacobian(plgb_sv *sv, plgb_obs *const *obs, int nobs, const plgb_ops *ops, const int64_t *trainable,
                           int ntp, int apply_ops, double *jac_out) {
     return with_sv(sv, [&](auto &s) {

@@ -1,0 +1,63 @@
+// Descriptors of the fused tile passes (kernels_fused.cu, host_fusion.cpp).
+#pragma once
+
+#include "kernels.hpp"
+
+namespace plgb {
+
+constexpr int kTileThreads = 256;
+constexpr int kMaxTileBits = 14;
+constexpr int kMaxMixedForms = 16;
+
+enum TileKind : int {
+    TK_PAIR = 0,    // two-amplitude update (Mode1), local targets, local/global controls
+    TK_SROT = 1,    // scaled real rotation [[a,-b],[b,a]], one of a, b == 1; scale folded into the pass
+    TK_DENSE2 = 2,  // dense 4x4 on two local bits
+    TK_DIAGTAB = 3, // merged diagonal: local table x global scalar x local/global sign flips
+    TK_PARITY = 4,  // parity phase on the full index (MultiRZ and its generator)
+};
+
+struct TilePassDesc {
+    int t;          // local bits in a tile
+    int L;          // the lowest L bits are always local
+    int H;          // number of further local bits
+    int hb[kMaxTileBits];
+    u64 ntiles;     // 2^(n - t)
+    int op_begin, nops;
+    double pass_scale; // product of the scalars factored out of rotations
+};
+
+template <class T> struct TileOp {
+    int kind{0};
+    int mode{0};
+    u32 lo0{0}, lo1{0};          // local offsets of the mixed amplitudes (DENSE2: first, second wire)
+    int nlins{0};                // sorted local bits cleared when enumerating pairs (targets + local controls)
+    int lins[12]{};
+    u32 lcval{0};                // local control values
+    u64 gcmask{0}, gcval{0};     // global control mask / values (tile-uniform)
+    // DIAGTAB
+    int has_table{0};
+    int table_off{0};
+    int gform_begin{0}, ngforms{0};
+    int mform_begin{0}, nmforms{0};
+    // PARITY (full index)
+    u64 pmask{0}, cmask{0}, cval{0};
+    int zero_outside{0};
+    cx<T> m[16]{};
+};
+
+// A diagonal factor on at most 4 bits: tab[k] with k = bits (first = MSB).
+// For a mixed (global x local) form, bits[0] is the global bit and
+// local_bit is the tile-local position of the other bit.
+template <class T> struct DiagForm {
+    int nb{0};
+    int bits[4]{};
+    int local_bit{0};
+    cx<T> tab[16]{};
+};
+
+template <class T>
+void launch_tile_pass(cudaStream_t s, cx<T> *sv, const TilePassDesc &d, const TileOp<T> *ops, const DiagForm<T> *forms,
+                      const cx<T> *tables);
+
+} // namespace plgb

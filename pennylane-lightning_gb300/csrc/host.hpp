@@ -80,6 +80,25 @@ struct DeviceScratch {
 };
 inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 
+// A gate lowered to one streaming-kernel primitive.  The unfused path
+// launches one kernel per primitive; the fusion engine (host_fusion.cpp)
+// schedules primitives into shared-memory tile passes.
+template <class T> struct Prim {
+    enum Kind : int { Pair, Dense2, DenseK, DiagK, Parity, Scale, PauliRot, ZeroOut };
+    Kind kind{Pair};
+    int mode{0};              // Pair: Mode1
+    std::vector<int> tbits;   // target bit positions (first = MSB of the local index)
+    u64 o0{0}, o1{0};         // Pair: offsets of the two mixed amplitudes
+    std::vector<int> cbits;   // control bit positions
+    u64 cmask{0}, cval{0};    // control mask / values over the full index
+    std::vector<cx<T>> m;     // coefficients (Pair 4, Dense2 16, DenseK 4^k, DiagK 2^k, Parity 2, Scale 1)
+    u64 pmask{0}, my{0}, mz{0}; // Parity mask; PauliRot x|y mask, y mask, z mask
+    T c{0};                   // PauliRot cosine
+    bool zero_outside{false};
+    u64 touched() const;      // every bit the primitive reads or writes
+    bool diagonal() const;    // multiplies each amplitude by a factor (no mixing)
+};
+
 template <class T> class StateVector {
   public:
     using CT = cx<T>;
@@ -135,6 +154,13 @@ template <class T> class StateVector {
     void prim_zero_outside(const std::vector<int64_t> &cwires, const std::vector<bool> &cvals);
     void scale_add(const StateVector &x, cd factor); // this += factor * x
 
+    // lowering: the primitives an operation expands to, without running them
+    std::vector<Prim<T>> lower_op(const OpRec &op, bool inverse);
+    void run_prim(const Prim<T> &p);
+    // fused application of a primitive list in shared-memory tile passes
+    // (host_fusion.cpp); tile_bits = log2 of the amplitudes a CTA stages
+    void apply_prims_fused(const std::vector<Prim<T>> &prims, int tile_bits);
+
     // reductions (return to host, synchronizing)
     double norm2() const;
     cd inner(const StateVector &ket) const; // <this|ket>
@@ -152,6 +178,8 @@ template <class T> class StateVector {
                       std::vector<int64_t> wires, bool inverse, const std::vector<double> &params);
     void global_phase_(const std::vector<int64_t> &cw, const std::vector<bool> &cv, bool inverse, T angle);
 
+    void emit_(Prim<T> &&p);
+    std::vector<Prim<T>> *sink_{nullptr};
     int n_{0};
     u64 N_{0};
     CT *d_{nullptr};
@@ -160,6 +188,19 @@ template <class T> class StateVector {
     bool owns_stream_{false};
     mutable DeviceScratch scratch_;
 };
+
+// ---------------------------------------------------------------------------
+// Fusion (host_fusion.cpp): a primitive list compiled into tile passes, with
+// its op tables resident in device memory; reusable across calls.
+// ---------------------------------------------------------------------------
+template <class T> struct FusedProgram;
+template <class T>
+std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>> &prims, int tile_bits);
+template <class T> void run_fused(StateVector<T> &sv, const FusedProgram<T> &prog);
+struct FusedStats {
+    size_t passes, unfused, prims;
+};
+template <class T> FusedStats fused_stats(const FusedProgram<T> &prog);
 
 // ---------------------------------------------------------------------------
 // Measurements (MeasurementsLQubit.hpp) and sampling.

@@ -1,0 +1,586 @@
+// Gate fusion: lowered primitives -> shared-memory tile passes.
+//
+// 1. Rewrite (exact algebra, rounding-level differences only):
+//    * a dense one-wire unitary U is written D1 R D2 with D diagonal and R a
+//      real rotation, and the rotation as s [[a,-b],[b,a]] with one of a, b
+//      equal to 1 (|other| <= 1): two fused multiply-adds per amplitude
+//      instead of eight, which is what the FP64 pipe of a GB300 (1.25
+//      TFLOP/s) makes decisive for complex128.  The scalar s of every
+//      rotation in a pass is applied once, at the tile store.
+//    * RY-shaped real rotations take the same scaled form.
+// 2. Schedule: in program order, a primitive joins the current pass when
+//    every earlier primitive it does not commute with is already placed and
+//    its mixing targets fit the pass's local bit set (diagonal primitives
+//    commute with each other and need no local bits).  Per-bit "blocked"
+//    flags make this linear in the number of primitives per pass.
+// 3. Translate: consecutive diagonals of a pass merge into one op: factors on
+//    local bits multiply into a table over the local index, factors on
+//    global bits into one scalar per tile, and two-bit factors across the
+//    boundary into integer sign flips (CZ) or a per-tile local factor.
+//
+// Primitives a tile cannot run (dense blocks on 3+ wires, Pauli rotations,
+// projections, wide diagonals across the tile boundary) run unfused
+// between passes.
+#include "fused.hpp"
+#include "host.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+
+namespace plgb {
+
+namespace {
+
+constexpr int kModeSrotA = 100; // [[1,-b],[b,1]]
+constexpr int kModeSrotB = 101; // [[a,-1],[1,a]]
+
+bool pair_is_diag(int mode) { return mode == M1_DIAG || mode == M1_PHASE1 || mode == M1_NEG1; }
+
+template <class T> std::vector<Prim<T>> rewrite(const std::vector<Prim<T>> &in) {
+    std::vector<Prim<T>> out;
+    out.reserve(in.size() * 2);
+    for (const auto &p : in) {
+        const bool single = p.kind == Prim<T>::Pair && p.tbits.size() == 1 && p.cbits.empty() && p.o0 == 0 &&
+                            p.o1 == (u64{1} << p.tbits[0]);
+        if (single && p.mode == M1_REAL && p.m[0].x == p.m[3].x && p.m[1].x == -p.m[2].x) {
+            // real rotation [[c, -s], [s, c]]
+            const double c = p.m[0].x, s = p.m[2].x;
+            Prim<T> r = p;
+            if (std::fabs(c) >= std::fabs(s)) {
+                r.mode = kModeSrotA;
+                r.m = {cx<T>{1, static_cast<T>(s / c)}};
+                r.c = static_cast<T>(c);
+            } else {
+                r.mode = kModeSrotB;
+                r.m = {cx<T>{static_cast<T>(c / s), 1}};
+                r.c = static_cast<T>(s);
+            }
+            out.push_back(std::move(r));
+            continue;
+        }
+        if (single && p.mode == M1_DENSE) {
+            // U = diag(e^{i a0}, e^{i a1}) [[c, -s], [s, c]] diag(e^{i b0}, e^{i b1}), b0 = 0
+            const std::complex<double> u00(p.m[0].x, p.m[0].y), u01(p.m[1].x, p.m[1].y), u10(p.m[2].x, p.m[2].y),
+                u11(p.m[3].x, p.m[3].y);
+            const double cm = std::abs(u00), sm = std::abs(u10);
+            const double a0 = std::arg(u00), a1 = std::arg(u10);
+            const double b1 = cm >= sm ? std::arg(u11) - a1 : std::arg(-u01) - a0;
+            const double th = std::atan2(sm, cm);
+            const double c = std::cos(th), s = std::sin(th);
+            auto ph = [](double a) { return cx<T>{static_cast<T>(std::cos(a)), static_cast<T>(std::sin(a))}; };
+            Prim<T> d2 = p;
+            d2.mode = M1_PHASE1;
+            d2.m = {cx<T>{1, 0}, cx<T>{0, 0}, cx<T>{0, 0}, ph(b1)};
+            Prim<T> r = p;
+            if (c >= s) {
+                r.mode = kModeSrotA;
+                r.m = {cx<T>{1, static_cast<T>(s / c)}};
+                r.c = static_cast<T>(c);
+            } else {
+                r.mode = kModeSrotB;
+                r.m = {cx<T>{static_cast<T>(c / s), 1}};
+                r.c = static_cast<T>(s);
+            }
+            Prim<T> d1 = p;
+            d1.mode = M1_DIAG;
+            d1.m = {ph(a0), cx<T>{0, 0}, cx<T>{0, 0}, ph(a1)};
+            out.push_back(std::move(d2));
+            out.push_back(std::move(r));
+            out.push_back(std::move(d1));
+            continue;
+        }
+        out.push_back(p);
+    }
+    return out;
+}
+
+// Canonical diagonal: factor tab[k], k over `bits` (first = MSB).
+template <class T> struct Diag {
+    std::vector<int> bits;
+    std::vector<std::complex<double>> tab;
+};
+
+template <class T> bool to_diag(const Prim<T> &p, Diag<T> &d) {
+    auto ctrl_table = [&](const std::vector<int> &tb, auto factor) {
+        d.bits = tb;
+        d.bits.insert(d.bits.end(), p.cbits.begin(), p.cbits.end());
+        const size_t k = d.bits.size();
+        d.tab.assign(size_t{1} << k, {1.0, 0.0});
+        for (size_t idx = 0; idx < d.tab.size(); idx++) {
+            bool match = true;
+            for (size_t c = 0; c < p.cbits.size(); c++) {
+                const size_t pos = tb.size() + c;
+                const u64 bitval = (idx >> (k - 1 - pos)) & 1U;
+                const u64 want = (p.cval >> p.cbits[c]) & 1U;
+                match = match && bitval == want;
+            }
+            if (match) {
+                d.tab[idx] = factor(idx >> p.cbits.size());
+            }
+        }
+    };
+    auto C = [](cx<T> v) { return std::complex<double>(v.x, v.y); };
+    if (p.kind == Prim<T>::Pair && pair_is_diag(p.mode) && p.tbits.size() == 1 && p.o0 == 0 &&
+        p.o1 == (u64{1} << p.tbits[0])) {
+        std::complex<double> d0{1, 0}, d1{-1, 0};
+        if (p.mode == M1_DIAG) {
+            d0 = C(p.m[0]);
+            d1 = C(p.m[3]);
+        } else if (p.mode == M1_PHASE1) {
+            d1 = C(p.m[3]);
+        }
+        ctrl_table(p.tbits, [&](size_t t) { return t ? d1 : d0; });
+        return true;
+    }
+    if (p.kind == Prim<T>::DiagK) {
+        ctrl_table(p.tbits, [&](size_t t) { return C(p.m[t]); });
+        return true;
+    }
+    if (p.kind == Prim<T>::Scale) {
+        ctrl_table({}, [&](size_t) { return C(p.m[0]); });
+        return true;
+    }
+    return false;
+}
+
+struct PassPlan {
+    bool fused{false};
+    std::vector<size_t> prims; // indices into the rewritten list
+    u64 local{0};
+};
+
+} // namespace
+
+template <class T> struct FusedProgram {
+    struct Seg {
+        bool tile{false};
+        TilePassDesc desc{};
+        Prim<T> prim; // unfused segment
+    };
+    std::vector<Seg> segs;
+    void *dev{nullptr};
+    TileOp<T> *d_ops{nullptr};
+    DiagForm<T> *d_forms{nullptr};
+    cx<T> *d_tables{nullptr};
+    int n{0};
+    size_t passes{0}, unfused{0}, prims{0};
+    ~FusedProgram() {
+        if (dev) {
+            cudaFree(dev);
+        }
+    }
+};
+
+template <class T>
+std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>> &in, int tile_bits) {
+    auto prog = std::make_shared<FusedProgram<T>>();
+    prog->n = n;
+    const int tmax = std::max(1, std::min({tile_bits, n, kMaxTileBits}));
+    const int Lbase = sizeof(T) == 8 ? 4 : 5;
+    const int L = std::min(Lbase, tmax);
+    const u64 lowmask = (u64{1} << L) - 1;
+    const std::vector<Prim<T>> P = rewrite(in);
+    prog->prims = P.size();
+
+    // per-primitive properties
+    const size_t m = P.size();
+    std::vector<u64> need(m), touch(m);
+    std::vector<char> diag(m), fusible(m);
+    for (size_t i = 0; i < m; i++) {
+        const auto &p = P[i];
+        touch[i] = p.touched();
+        Diag<T> dd;
+        const bool isd = to_diag(p, dd) || p.kind == Prim<T>::Parity;
+        diag[i] = isd;
+        u64 nb = 0;
+        if (!isd) {
+            for (int b : p.tbits) {
+                nb |= u64{1} << b;
+            }
+        }
+        need[i] = nb;
+        bool ok = false;
+        if (p.kind == Prim<T>::Pair || p.kind == Prim<T>::Dense2) {
+            ok = __builtin_popcountll(nb | lowmask) <= tmax && p.tbits.size() <= 12;
+        } else if (p.kind == Prim<T>::Parity) {
+            ok = true;
+        } else if (isd) {
+            ok = dd.bits.size() <= 16;
+        }
+        fusible[i] = ok;
+    }
+
+    // ---- schedule
+    std::vector<PassPlan> plan;
+    std::vector<char> done(m, 0);
+    size_t seg_start = 0;
+    while (seg_start < m) {
+        size_t seg_end = seg_start;
+        while (seg_end < m && fusible[seg_end]) {
+            seg_end++;
+        }
+        // fused passes over [seg_start, seg_end)
+        size_t remaining = seg_end - seg_start;
+        while (remaining > 0) {
+            PassPlan pp;
+            pp.fused = true;
+            pp.local = lowmask;
+            u64 blocked_nd = 0, blocked_d = 0;
+            // global bits of placed cross-boundary diagonals must stay global
+            // (their fused form was chosen for that split)
+            u64 frozen = 0;
+            for (size_t i = seg_start; i < seg_end; i++) {
+                if (done[i]) {
+                    continue;
+                }
+                bool ok = !(touch[i] & blocked_nd) && (diag[i] || !(touch[i] & blocked_d));
+                if (ok) {
+                    const u64 nl = pp.local | need[i];
+                    if (__builtin_popcountll(nl) <= tmax && !(need[i] & ~pp.local & frozen)) {
+                        pp.local = nl;
+                    } else {
+                        ok = false;
+                    }
+                }
+                if (ok && diag[i]) {
+                    // a diagonal across the tile boundary must have a fused form
+                    Diag<T> dd;
+                    if (to_diag(P[i], dd)) {
+                        int nglob = 0, nloc = 0;
+                        u64 gbits = 0;
+                        for (int b : dd.bits) {
+                            if ((pp.local >> b) & 1U) {
+                                nloc++;
+                            } else {
+                                nglob++;
+                                gbits |= u64{1} << b;
+                            }
+                        }
+                        ok = nglob == 0 || (nloc == 0 && nglob <= 4) || (nglob == 1 && nloc == 1);
+                        if (ok) {
+                            frozen |= gbits;
+                        }
+                    }
+                }
+                if (ok) {
+                    pp.prims.push_back(i);
+                    done[i] = 1;
+                    remaining--;
+                } else if (diag[i]) {
+                    blocked_d |= touch[i];
+                } else {
+                    blocked_nd |= touch[i];
+                }
+            }
+            if (pp.prims.empty()) {
+                // cannot place the first open primitive in a tile: run it unfused
+                for (size_t i = seg_start; i < seg_end; i++) {
+                    if (!done[i]) {
+                        PassPlan up;
+                        up.prims = {i};
+                        plan.push_back(up);
+                        done[i] = 1;
+                        remaining--;
+                        break;
+                    }
+                }
+                continue;
+            }
+            plan.push_back(std::move(pp));
+        }
+        if (seg_end < m) {
+            PassPlan up;
+            up.prims = {seg_end};
+            plan.push_back(up);
+            done[seg_end] = 1;
+            seg_end++;
+        }
+        seg_start = seg_end;
+    }
+
+    // ---- translate
+    std::vector<TileOp<T>> ops;
+    std::vector<DiagForm<T>> forms;
+    std::vector<cx<T>> tables;
+    for (auto &pp : plan) {
+        typename FusedProgram<T>::Seg seg;
+        if (!pp.fused) {
+            seg.tile = false;
+            seg.prim = P[pp.prims[0]];
+            if (seg.prim.kind == Prim<T>::Pair && (seg.prim.mode == kModeSrotA || seg.prim.mode == kModeSrotB)) {
+                // a scaled rotation outside a tile: back to s [[a,-b],[b,a]]
+                const T sc = seg.prim.c;
+                const T a = seg.prim.mode == kModeSrotA ? T(1) : seg.prim.m[0].x;
+                const T b = seg.prim.mode == kModeSrotA ? seg.prim.m[0].y : T(1);
+                seg.prim.mode = M1_REAL;
+                seg.prim.m = {cx<T>{sc * a, 0}, cx<T>{-sc * b, 0}, cx<T>{sc * b, 0}, cx<T>{sc * a, 0}};
+            }
+            prog->segs.push_back(std::move(seg));
+            prog->unfused++;
+            continue;
+        }
+        seg.tile = true;
+        TilePassDesc &d = seg.desc;
+        d.L = L;
+        std::vector<int> hb;
+        for (int b = L; b < n; b++) {
+            if ((pp.local >> b) & 1U) {
+                hb.push_back(b);
+            }
+        }
+        d.H = static_cast<int>(hb.size());
+        d.t = L + d.H;
+        for (int i = 0; i < d.H; i++) {
+            d.hb[i] = hb[static_cast<size_t>(i)];
+        }
+        d.ntiles = u64{1} << (n - d.t);
+        d.op_begin = static_cast<int>(ops.size());
+        d.pass_scale = 1.0;
+        auto lpos = [&](int b) -> int {
+            if (b < L) {
+                return b;
+            }
+            for (int i = 0; i < d.H; i++) {
+                if (d.hb[i] == b) {
+                    return L + i;
+                }
+            }
+            return -1;
+        };
+        auto is_local = [&](int b) { return ((pp.local >> b) & 1U) != 0; };
+        auto local_mask = [&](u64 gm) {
+            u32 lm = 0;
+            for (int b = 0; b < n; b++) {
+                if ((gm >> b) & 1U) {
+                    const int lp = lpos(b);
+                    if (lp >= 0) {
+                        lm |= 1u << lp;
+                    }
+                }
+            }
+            return lm;
+        };
+        // pending merged diagonal
+        std::vector<Diag<T>> pend;
+        auto flush = [&]() {
+            if (pend.empty()) {
+                return;
+            }
+            TileOp<T> op;
+            op.kind = TK_DIAGTAB;
+            std::vector<std::complex<double>> tab;
+            bool has_table = false;
+            std::vector<DiagForm<T>> gforms, mforms;
+            for (auto &dg : pend) {
+                int nloc = 0, nglob = 0;
+                for (int b : dg.bits) {
+                    is_local(b) ? nloc++ : nglob++;
+                }
+                if (nglob == 0) {
+                    if (!has_table) {
+                        tab.assign(size_t{1} << d.t, {1.0, 0.0});
+                        has_table = true;
+                    }
+                    const size_t k = dg.bits.size();
+                    std::vector<int> lp(k);
+                    for (size_t i = 0; i < k; i++) {
+                        lp[i] = lpos(dg.bits[i]);
+                    }
+                    for (size_t j = 0; j < tab.size(); j++) {
+                        size_t idx = 0;
+                        for (size_t i = 0; i < k; i++) {
+                            idx = (idx << 1) | ((j >> lp[i]) & 1U);
+                        }
+                        tab[j] *= dg.tab[idx];
+                    }
+                } else if (nloc == 0) {
+                    DiagForm<T> f;
+                    f.nb = static_cast<int>(dg.bits.size());
+                    for (int i = 0; i < f.nb; i++) {
+                        f.bits[i] = dg.bits[static_cast<size_t>(i)];
+                    }
+                    for (size_t i = 0; i < dg.tab.size(); i++) {
+                        f.tab[i] = cx<T>{static_cast<T>(dg.tab[i].real()), static_cast<T>(dg.tab[i].imag())};
+                    }
+                    gforms.push_back(f);
+                } else {
+                    // one global, one local bit: reorder as [global][local]
+                    DiagForm<T> f;
+                    f.nb = 2;
+                    const bool g_first = !is_local(dg.bits[0]);
+                    f.bits[0] = g_first ? dg.bits[0] : dg.bits[1];
+                    f.local_bit = lpos(g_first ? dg.bits[1] : dg.bits[0]);
+                    for (int gbv = 0; gbv < 2; gbv++) {
+                        for (int lbv = 0; lbv < 2; lbv++) {
+                            const int idx = g_first ? (gbv << 1 | lbv) : (lbv << 1 | gbv);
+                            const auto v = dg.tab[static_cast<size_t>(idx)];
+                            f.tab[gbv * 2 + lbv] = cx<T>{static_cast<T>(v.real()), static_cast<T>(v.imag())};
+                        }
+                    }
+                    mforms.push_back(f);
+                }
+            }
+            // split the form lists into ops of bounded size
+            size_t gi = 0, mi = 0;
+            bool first = true;
+            while (first || gi < gforms.size() || mi < mforms.size()) {
+                TileOp<T> o = op;
+                o.has_table = first && has_table ? 1 : 0;
+                if (o.has_table) {
+                    o.table_off = static_cast<int>(tables.size());
+                    for (auto &v : tab) {
+                        tables.push_back(cx<T>{static_cast<T>(v.real()), static_cast<T>(v.imag())});
+                    }
+                }
+                o.gform_begin = static_cast<int>(forms.size());
+                const size_t gtake = std::min<size_t>(gforms.size() - gi, 64);
+                for (size_t i = 0; i < gtake; i++) {
+                    forms.push_back(gforms[gi++]);
+                }
+                o.ngforms = static_cast<int>(gtake);
+                o.mform_begin = static_cast<int>(forms.size());
+                const size_t mtake = std::min<size_t>(mforms.size() - mi, kMaxMixedForms);
+                for (size_t i = 0; i < mtake; i++) {
+                    forms.push_back(mforms[mi++]);
+                }
+                o.nmforms = static_cast<int>(mtake);
+                if (o.has_table || o.ngforms || o.nmforms) {
+                    ops.push_back(o);
+                }
+                first = false;
+            }
+            pend.clear();
+        };
+
+        for (size_t pi : pp.prims) {
+            const auto &p = P[pi];
+            Diag<T> dg;
+            if (to_diag(p, dg)) {
+                pend.push_back(std::move(dg));
+                continue;
+            }
+            if (p.kind == Prim<T>::Parity) {
+                TileOp<T> o;
+                o.kind = TK_PARITY;
+                o.pmask = p.pmask;
+                o.cmask = p.cmask;
+                o.cval = p.cval;
+                o.zero_outside = p.zero_outside ? 1 : 0;
+                o.m[0] = p.m[0];
+                o.m[1] = p.m[1];
+                ops.push_back(o);
+                continue;
+            }
+            flush();
+            TileOp<T> o;
+            // controls: local ones enumerate, global ones gate the whole tile
+            std::vector<int> lins;
+            for (int b : p.tbits) {
+                lins.push_back(lpos(b));
+            }
+            for (int b : p.cbits) {
+                if (is_local(b)) {
+                    lins.push_back(lpos(b));
+                    if ((p.cval >> b) & 1U) {
+                        o.lcval |= 1u << lpos(b);
+                    }
+                } else {
+                    o.gcmask |= u64{1} << b;
+                    o.gcval |= p.cval & (u64{1} << b);
+                }
+            }
+            std::sort(lins.begin(), lins.end());
+            PLGB_REQUIRE(lins.size() <= 12, "fusion: too many local bits in one op");
+            o.nlins = static_cast<int>(lins.size());
+            for (size_t i = 0; i < lins.size(); i++) {
+                o.lins[i] = lins[i];
+            }
+            if (p.kind == Prim<T>::Pair) {
+                o.lo0 = local_mask(p.o0);
+                o.lo1 = local_mask(p.o1);
+                if (p.mode == kModeSrotA || p.mode == kModeSrotB) {
+                    o.kind = TK_SROT;
+                    o.mode = p.mode == kModeSrotA ? 0 : 1;
+                    o.m[0] = p.m[0];
+                    d.pass_scale *= static_cast<double>(p.c);
+                } else {
+                    o.kind = TK_PAIR;
+                    o.mode = p.mode;
+                    for (int i = 0; i < 4; i++) {
+                        o.m[i] = p.m[static_cast<size_t>(i)];
+                    }
+                }
+            } else { // Dense2
+                o.kind = TK_DENSE2;
+                o.lo0 = 1u << lpos(p.tbits[0]);
+                o.lo1 = 1u << lpos(p.tbits[1]);
+                for (int i = 0; i < 16; i++) {
+                    o.m[i] = p.m[static_cast<size_t>(i)];
+                }
+            }
+            ops.push_back(o);
+        }
+        flush();
+        d.nops = static_cast<int>(ops.size()) - d.op_begin;
+        prog->segs.push_back(std::move(seg));
+        prog->passes++;
+    }
+
+    // ---- upload
+    const size_t b_ops = align_up(std::max<size_t>(1, ops.size()) * sizeof(TileOp<T>));
+    const size_t b_forms = align_up(std::max<size_t>(1, forms.size()) * sizeof(DiagForm<T>));
+    const size_t b_tab = align_up(std::max<size_t>(1, tables.size()) * sizeof(cx<T>));
+    cuda_check(cudaMalloc(&prog->dev, b_ops + b_forms + b_tab), "cudaMalloc(fused program)");
+    char *base = static_cast<char *>(prog->dev);
+    prog->d_ops = reinterpret_cast<TileOp<T> *>(base);
+    prog->d_forms = reinterpret_cast<DiagForm<T> *>(base + b_ops);
+    prog->d_tables = reinterpret_cast<cx<T> *>(base + b_ops + b_forms);
+    if (!ops.empty()) {
+        cuda_check(cudaMemcpy(prog->d_ops, ops.data(), ops.size() * sizeof(TileOp<T>), cudaMemcpyHostToDevice), "H2D");
+    }
+    if (!forms.empty()) {
+        cuda_check(cudaMemcpy(prog->d_forms, forms.data(), forms.size() * sizeof(DiagForm<T>), cudaMemcpyHostToDevice),
+                   "H2D");
+    }
+    if (!tables.empty()) {
+        cuda_check(cudaMemcpy(prog->d_tables, tables.data(), tables.size() * sizeof(cx<T>), cudaMemcpyHostToDevice),
+                   "H2D");
+    }
+    return prog;
+}
+
+template <class T> void run_fused(StateVector<T> &sv, const FusedProgram<T> &prog) {
+    PLGB_REQUIRE(prog.n == sv.num_qubits(), "fused program compiled for a different register size");
+    for (const auto &seg : prog.segs) {
+        if (seg.tile) {
+            launch_tile_pass<T>(sv.stream(), sv.data(), seg.desc, prog.d_ops, prog.d_forms, prog.d_tables);
+        } else {
+            sv.run_prim(seg.prim);
+        }
+    }
+}
+
+template <class T>
+void StateVector<T>::apply_prims_fused(const std::vector<Prim<T>> &prims, int tile_bits) {
+    auto prog = compile_fused<T>(n_, prims, tile_bits);
+    run_fused<T>(*this, *prog);
+    synchronize(); // the program's device buffer is freed on return
+}
+
+template <class T> FusedStats fused_stats(const FusedProgram<T> &prog) {
+    return FusedStats{prog.passes, prog.unfused, prog.prims};
+}
+template FusedStats fused_stats<float>(const FusedProgram<float> &);
+template FusedStats fused_stats<double>(const FusedProgram<double> &);
+
+template struct FusedProgram<float>;
+template struct FusedProgram<double>;
+template std::shared_ptr<FusedProgram<float>> compile_fused<float>(int, const std::vector<Prim<float>> &, int);
+template std::shared_ptr<FusedProgram<double>> compile_fused<double>(int, const std::vector<Prim<double>> &, int);
+template void run_fused<float>(StateVector<float> &, const FusedProgram<float> &);
+template void run_fused<double>(StateVector<double> &, const FusedProgram<double> &);
+template void StateVector<float>::apply_prims_fused(const std::vector<Prim<float>> &, int);
+template void StateVector<double>::apply_prims_fused(const std::vector<Prim<double>> &, int);
+
+} // namespace plgb

@@ -318,16 +318,155 @@ template <class T> void StateVector<T>::scale_add(const StateVector &x, cd facto
 }
 
 // ---------------------------------------------------------------------------
-// primitives
+// primitives: emitted into the fusion sink when one is set, launched otherwise
 // ---------------------------------------------------------------------------
+template <class T> u64 Prim<T>::touched() const {
+    u64 t = cmask | pmask | my | mz;
+    for (int b : tbits) {
+        t |= u64{1} << b;
+    }
+    return t;
+}
+template <class T> bool Prim<T>::diagonal() const {
+    return kind == DiagK || kind == Parity || kind == Scale ||
+           (kind == Pair && (mode == M1_DIAG || mode == M1_PHASE1 || mode == M1_NEG1));
+}
+
+template <class T> void StateVector<T>::emit_(Prim<T> &&p) {
+    if (sink_) {
+        sink_->push_back(std::move(p));
+    } else {
+        run_prim(p);
+    }
+}
+
+template <class T> static void set_controls(Prim<T> &p, const StateVector<T> &sv, const std::vector<int64_t> &cw,
+                                            const std::vector<bool> &cv) {
+    PLGB_REQUIRE(cw.size() == cv.size(), "`controlled_wires` must have the same size as `controlled_values`.");
+    for (size_t i = 0; i < cw.size(); i++) {
+        const int b = sv.bit_of(cw[i]);
+        p.cbits.push_back(b);
+        p.cmask |= u64{1} << b;
+        if (cv[i]) {
+            p.cval |= u64{1} << b;
+        }
+    }
+}
+
+template <class T> void StateVector<T>::run_prim(const Prim<T> &p) {
+    auto geom = [&](const std::vector<int> &tb) {
+        GroupGeom g{};
+        std::vector<int> ins(tb);
+        ins.insert(ins.end(), p.cbits.begin(), p.cbits.end());
+        std::sort(ins.begin(), ins.end());
+        PLGB_REQUIRE(static_cast<int>(ins.size()) <= PLGB_MAX_INS && static_cast<int>(ins.size()) <= n_,
+                     "too many wires for the register");
+        g.nins = static_cast<int>(ins.size());
+        for (int i = 0; i < g.nins; i++) {
+            g.ins[i] = ins[static_cast<size_t>(i)];
+        }
+        g.cval = p.cval;
+        g.ngroups = N_ >> g.nins;
+        return g;
+    };
+    switch (p.kind) {
+    case Prim<T>::Pair: {
+        Mat1<T> m{};
+        for (size_t i = 0; i < 4 && i < p.m.size(); i++) {
+            m.m[i] = p.m[i];
+        }
+        const GroupGeom g = geom(p.tbits);
+        if (g.ngroups > 0) {
+            launch_1q<T>(s_, d_, g, p.o0, p.o1, p.mode, m);
+        }
+        return;
+    }
+    case Prim<T>::Dense2: {
+        Mat2<T> m{};
+        for (size_t i = 0; i < 16; i++) {
+            m.m[i] = p.m[i];
+        }
+        launch_2q<T>(s_, d_, geom(p.tbits), p.tbits[0], p.tbits[1], false, m);
+        return;
+    }
+    case Prim<T>::DenseK: {
+        const size_t k = p.tbits.size();
+        const size_t D = size_t{1} << k;
+        LocalOffsets lo{};
+        std::vector<u64> loc(D);
+        for (size_t j = 0; j < D; j++) {
+            u64 o = 0;
+            for (size_t b = 0; b < k; b++) {
+                if ((j >> (k - 1 - b)) & 1U) {
+                    o |= u64{1} << p.tbits[b];
+                }
+            }
+            loc[j] = o;
+            if (j < 32) {
+                lo.off[j] = o;
+            }
+        }
+        const size_t mbytes = D * D * sizeof(CT);
+        const auto bufs = scratch_.carve({mbytes, D * sizeof(u64)});
+        CT *dm = reinterpret_cast<CT *>(bufs[0]);
+        u64 *dloc = reinterpret_cast<u64 *>(bufs[1]);
+        cuda_check(cudaMemcpyAsync(dm, p.m.data(), mbytes, cudaMemcpyHostToDevice, s_), "H2D matrix");
+        cuda_check(cudaMemcpyAsync(dloc, loc.data(), D * sizeof(u64), cudaMemcpyHostToDevice, s_), "H2D offsets");
+        launch_kq<T>(s_, d_, geom(p.tbits), static_cast<int>(k), lo, dm, dloc);
+        synchronize(); // the scratch matrix is reused by the next call
+        return;
+    }
+    case Prim<T>::DiagK: {
+        const size_t k = p.tbits.size();
+        if (k == 2) {
+            Mat2<T> m{};
+            m.m[0] = p.m[0];
+            m.m[5] = p.m[1];
+            m.m[10] = p.m[2];
+            m.m[15] = p.m[3];
+            launch_2q<T>(s_, d_, geom(p.tbits), p.tbits[0], p.tbits[1], true, m);
+            return;
+        }
+        TBits tb{};
+        for (size_t b = 0; b < k; b++) {
+            tb.b[b] = p.tbits[b];
+        }
+        scratch_.ensure_mat(p.m.size() * sizeof(CT));
+        CT *dd = static_cast<CT *>(scratch_.mat);
+        cuda_check(cudaMemcpyAsync(dd, p.m.data(), p.m.size() * sizeof(CT), cudaMemcpyHostToDevice, s_), "H2D diag");
+        launch_diag<T>(s_, d_, N_, p.cmask, p.cval, static_cast<int>(k), tb, dd);
+        synchronize();
+        return;
+    }
+    case Prim<T>::Parity:
+        launch_parity<T>(s_, d_, N_, p.pmask, p.cmask, p.cval, p.m[0], p.m[1], p.zero_outside);
+        return;
+    case Prim<T>::Scale:
+        launch_scale<T>(s_, d_, N_, p.m[0], p.cmask, p.cval);
+        return;
+    case Prim<T>::PauliRot:
+        launch_pauli_rot<T>(s_, d_, n_, p.pmask, p.my, p.mz, p.c, p.m[0]);
+        return;
+    case Prim<T>::ZeroOut:
+        if (p.cmask) {
+            launch_zero_outside<T>(s_, d_, N_, p.cmask, p.cval);
+        }
+        return;
+    }
+}
+
 template <class T>
 void StateVector<T>::prim_pair(const std::vector<int> &ins_bits, u64 o0, u64 o1, const std::vector<int64_t> &cwires,
                                const std::vector<bool> &cvals, int mode, const Mat1<T> &m) {
-    const GroupGeom g = geom_(ins_bits, cwires, cvals);
-    if (g.ngroups == 0) {
-        return;
-    }
-    launch_1q<T>(s_, d_, g, o0, o1, mode, m);
+    Prim<T> p;
+    p.kind = Prim<T>::Pair;
+    p.mode = mode;
+    p.tbits = ins_bits;
+    p.o0 = o0;
+    p.o1 = o1;
+    set_controls(p, *this, cwires, cvals);
+    p.m.assign(m.m, m.m + 4);
+    emit_(std::move(p));
 }
 
 template <class T>
@@ -353,44 +492,15 @@ void StateVector<T>::prim_dense(const std::vector<int64_t> &wires, const std::ve
         prim_1q(wires[0], cwires, cvals, M1_DENSE, m);
         return;
     }
-    std::vector<int> tb;
-    for (auto w : wires) {
-        tb.push_back(bit_of(w));
-    }
-    const GroupGeom g = geom_(tb, cwires, cvals);
-    if (k == 2) {
-        Mat2<T> m{};
-        for (int i = 0; i < 16; i++) {
-            m.m[i] = mat[static_cast<size_t>(i)];
-        }
-        launch_2q<T>(s_, d_, g, tb[0], tb[1], false, m);
-        return;
-    }
     PLGB_REQUIRE(k <= 12, "dense matrices act on at most 12 wires");
-    const size_t D = size_t{1} << k;
-    LocalOffsets lo{};
-    std::vector<u64> loc(D);
-    for (size_t j = 0; j < D; j++) {
-        u64 o = 0;
-        for (size_t m = 0; m < k; m++) {
-            if ((j >> (k - 1 - m)) & 1U) {
-                o |= u64{1} << tb[m];
-            }
-        }
-        loc[j] = o;
-        if (j < 32) {
-            lo.off[j] = o;
-        }
+    Prim<T> p;
+    p.kind = k == 2 ? Prim<T>::Dense2 : Prim<T>::DenseK;
+    for (auto w : wires) {
+        p.tbits.push_back(bit_of(w));
     }
-    const size_t mbytes = D * D * sizeof(CT);
-    const auto bufs = scratch_.carve({mbytes, D * sizeof(u64)});
-    CT *dm = reinterpret_cast<CT *>(bufs[0]);
-    u64 *dloc = reinterpret_cast<u64 *>(bufs[1]);
-    cuda_check(cudaMemcpyAsync(dm, mat.data(), mbytes, cudaMemcpyHostToDevice, s_), "H2D matrix");
-    cuda_check(cudaMemcpyAsync(dloc, loc.data(), D * sizeof(u64), cudaMemcpyHostToDevice, s_), "H2D offsets");
-    launch_kq<T>(s_, d_, g, static_cast<int>(k), lo, dm, dloc);
-    // the scratch matrix may be overwritten by the next call: order it
-    synchronize();
+    set_controls(p, *this, cwires, cvals);
+    p.m = mat;
+    emit_(std::move(p));
 }
 
 template <class T>
@@ -399,23 +509,14 @@ void StateVector<T>::prim_diag(const std::vector<int64_t> &wires, const std::vec
     const size_t k = wires.size();
     PLGB_REQUIRE(k >= 1 && k <= 16, "diagonal gates act on 1..16 wires");
     check_wires_(wires, cwires);
-    TBits tb{};
-    for (size_t m = 0; m < k; m++) {
-        tb.b[m] = bit_of(wires[m]);
+    Prim<T> p;
+    p.kind = Prim<T>::DiagK;
+    for (auto w : wires) {
+        p.tbits.push_back(bit_of(w));
     }
-    u64 cmask = 0, cval = 0;
-    for (size_t i = 0; i < cwires.size(); i++) {
-        const u64 b = u64{1} << bit_of(cwires[i]);
-        cmask |= b;
-        if (cvals[i]) {
-            cval |= b;
-        }
-    }
-    scratch_.ensure_mat(diag.size() * sizeof(CT));
-    CT *dd = static_cast<CT *>(scratch_.mat);
-    cuda_check(cudaMemcpyAsync(dd, diag.data(), diag.size() * sizeof(CT), cudaMemcpyHostToDevice, s_), "H2D diag");
-    launch_diag<T>(s_, d_, N_, cmask, cval, static_cast<int>(k), tb, dd);
-    synchronize();
+    set_controls(p, *this, cwires, cvals);
+    p.m = diag;
+    emit_(std::move(p));
 }
 
 template <class T>
@@ -423,15 +524,24 @@ void StateVector<T>::prim_zero_outside(const std::vector<int64_t> &cwires, const
     if (cwires.empty()) {
         return;
     }
-    u64 cmask = 0, cval = 0;
-    for (size_t i = 0; i < cwires.size(); i++) {
-        const u64 b = u64{1} << bit_of(cwires[i]);
-        cmask |= b;
-        if (cvals[i]) {
-            cval |= b;
-        }
+    Prim<T> p;
+    p.kind = Prim<T>::ZeroOut;
+    set_controls(p, *this, cwires, cvals);
+    emit_(std::move(p));
+}
+
+template <class T> std::vector<Prim<T>> StateVector<T>::lower_op(const OpRec &op, bool inverse) {
+    std::vector<Prim<T>> out;
+    auto *saved = sink_;
+    sink_ = &out;
+    try {
+        apply_op(op, inverse);
+    } catch (...) {
+        sink_ = saved;
+        throw;
     }
-    launch_zero_outside<T>(s_, d_, N_, cmask, cval);
+    sink_ = saved;
+    return out;
 }
 
 // ---------------------------------------------------------------------------
@@ -478,18 +588,17 @@ void StateVector<T>::global_phase_(const std::vector<int64_t> &cw, const std::ve
     if (n_ == 1 && cw.size() == 1 && !cv[0]) {
         const CT s = inverse ? cexp_i<T>(-angle) : cexp_i<T>(angle);
         prim_1q(cw[0], {}, {}, M1_PHASE1, m1<T>(C<T>(1, 0), C<T>(0, 0), C<T>(0, 0), s));
-        launch_scale<T>(s_, d_, N_, phase, 0, 0);
+        Prim<T> p;
+        p.kind = Prim<T>::Scale;
+        p.m = {phase};
+        emit_(std::move(p));
         return;
     }
-    u64 cmask = 0, cval = 0;
-    for (size_t i = 0; i < cw.size(); i++) {
-        const u64 b = u64{1} << bit_of(cw[i]);
-        cmask |= b;
-        if (cv[i]) {
-            cval |= b;
-        }
-    }
-    launch_scale<T>(s_, d_, N_, phase, cmask, cval);
+    Prim<T> p;
+    p.kind = Prim<T>::Scale;
+    set_controls(p, *this, cw, cv);
+    p.m = {phase};
+    emit_(std::move(p));
 }
 
 template <class T>
@@ -642,14 +751,7 @@ void StateVector<T>::apply_named_(const std::string &name, std::vector<int64_t> 
         const CT first{std::cos(a / 2), -std::sin(a / 2)};
         const CT second{std::cos(a / 2), std::sin(a / 2)};
         const CT s0 = inverse ? conj(first) : first, s1 = inverse ? conj(second) : second;
-        std::vector<int> tb{bit_of(wires[0]), bit_of(wires[1])};
-        const GroupGeom g = geom_(tb, cw, cv);
-        Mat2<T> m{};
-        m.m[0] = s0;
-        m.m[5] = s1;
-        m.m[10] = s1;
-        m.m[15] = s0;
-        launch_2q<T>(s_, d_, g, tb[0], tb[1], true, m);
+        prim_diag(wires, cw, cv, {s0, s1, s1, s0});
     } else if (base == "SingleExcitation") { // LM:1613-1644: rotation on |01>,|10>
         need(2);
         const T a = P(0);
@@ -718,19 +820,14 @@ void StateVector<T>::apply_named_(const std::string &name, std::vector<int64_t> 
         const T a = P(0);
         const CT first{std::cos(a / 2), -std::sin(a / 2)};
         const CT second{std::cos(a / 2), std::sin(a / 2)};
-        u64 pm = 0, cmask = 0, cval = 0;
+        Prim<T> p;
+        p.kind = Prim<T>::Parity;
         for (auto w : wires) {
-            pm |= u64{1} << bit_of(w);
+            p.pmask |= u64{1} << bit_of(w);
         }
-        for (size_t i = 0; i < cw.size(); i++) {
-            const u64 b = u64{1} << bit_of(cw[i]);
-            cmask |= b;
-            if (cv[i]) {
-                cval |= b;
-            }
-        }
-        launch_parity<T>(s_, d_, N_, pm, cmask, cval, inverse ? conj(first) : first,
-                         inverse ? conj(second) : second, false);
+        set_controls(p, *this, cw, cv);
+        p.m = {inverse ? conj(first) : first, inverse ? conj(second) : second};
+        emit_(std::move(p));
     } else if (base == "GlobalPhase") {
         global_phase_(cw, cv, inverse, P(0));
     } else if (base == "PCPhase") { // LM:2114-2162
@@ -845,7 +942,14 @@ void StateVector<T>::apply_pauli_rot(const std::vector<int64_t> &wires, bool inv
     const T sn = std::sin(angle / 2);
     // s = (inverse ? i : -i) * sin(angle/2)
     const CT s = inverse ? CT{0, sn} : CT{0, -sn};
-    launch_pauli_rot<T>(s_, d_, n_, mxy, my, mz, c, s);
+    Prim<T> p;
+    p.kind = Prim<T>::PauliRot;
+    p.pmask = mxy;
+    p.my = my;
+    p.mz = mz;
+    p.c = c;
+    p.m = {s};
+    emit_(std::move(p));
 }
 
 // ---------------------------------------------------------------------------
@@ -874,18 +978,15 @@ double StateVector<T>::apply_generator(const std::string &name, const std::vecto
         return -1.0;
     }
     if (base == "MultiRZ") {
-        u64 pm = 0, cmask = 0, cval = 0;
+        Prim<T> p;
+        p.kind = Prim<T>::Parity;
         for (auto w : wires) {
-            pm |= u64{1} << bit_of(w);
+            p.pmask |= u64{1} << bit_of(w);
         }
-        for (size_t i = 0; i < cw.size(); i++) {
-            const u64 b = u64{1} << bit_of(cw[i]);
-            cmask |= b;
-            if (cv[i]) {
-                cval |= b;
-            }
-        }
-        launch_parity<T>(s_, d_, N_, pm, cmask, cval, O1, M1, true);
+        set_controls(p, *this, cw, cv);
+        p.m = {O1, M1};
+        p.zero_outside = true;
+        emit_(std::move(p));
         return -0.5;
     }
     prim_zero_outside(cw, cv);
@@ -1000,6 +1101,8 @@ template <class T> void StateVector<T>::apply_op(const OpRec &op, bool inverse) 
     apply_matrix(op.matrix.data(), op.wires, inverse, op.cwires, op.cvals);
 }
 
+template struct Prim<float>;
+template struct Prim<double>;
 template class StateVector<float>;
 template class StateVector<double>;
 

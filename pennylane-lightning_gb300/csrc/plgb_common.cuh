@@ -16,6 +16,7 @@
 namespace plgb {
 
 using u64 = unsigned long long;
+using u32 = unsigned int;
 
 template <class T> struct alignas(2 * sizeof(T)) cx {
     T x, y;

@@ -233,6 +233,16 @@ class _StateVectorBase:
             raise LightningException(f"Operation {name} is not supported and no matrix was given")
         return self.applyMatrix(matrix, wires, inverse)
 
+    def applyOperations(self, ops, tile_bits: int = 0) -> int:
+        """Apply an OpsStruct list (StateVectorBase::applyOperations).
+
+        tile_bits = 0 runs one kernel per gate; tile_bits = t > 0 fuses the
+        list into shared-memory tile passes of 2^t amplitudes.  Returns the
+        number of kernel passes the call issued."""
+        passes = C.c_int()
+        call("plgb_sv_apply_operations", self._h, ops._h, int(tile_bits), C.byref(passes))
+        return passes.value
+
     def applyMatrix(self, matrix, wires, inverse: bool = False) -> None:
         m = _cmat(matrix)
         w, nw = _i64(wires)

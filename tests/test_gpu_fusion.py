@@ -1,0 +1,126 @@
+"""Fused tile passes vs the CPU oracle and vs the unfused per-gate path.
+
+Random circuits mixing every gate family (one-wire named gates, controlled
+gates with local and global controls, dense matrices on 1-4 wires, diagonal
+and parity gates, Pauli rotations, excitations) are applied through
+StateVector.applyOperations with tile sizes from 2^2 to 2^14 amplitudes.
+"""
+import numpy as np
+import pytest
+
+from gate_table import GATES, gate_params
+from helpers import DTYPES, assert_close, rand_state, rand_unitary, seed_of, sv_class
+from lightning_gb300.workloads import config0, config1
+
+pytestmark = pytest.mark.gpu
+
+
+def random_circuit(rng, n, depth):
+    ops = []
+    names = [g for g in GATES if g not in ("Identity",)]
+    for _ in range(depth):
+        r = rng.random()
+        if r < 0.15:
+            k = int(rng.integers(1, min(4, n) + 1))
+            w = [int(x) for x in rng.choice(n, size=k, replace=False)]
+            ops.append(dict(name="QubitUnitary", wires=w, matrix=rand_unitary(rng, k)))
+        elif r < 0.25 and n >= 3:
+            name = str(rng.choice(["RX", "RY", "RZ", "PhaseShift", "Hadamard", "PauliX", "Rot", "IsingXY", "MultiRZ"]))
+            nwk = GATES[name][0] or 2
+            nc = int(rng.integers(1, 3))
+            if nwk + nc > n:
+                continue
+            ws = [int(x) for x in rng.choice(n, size=nwk + nc, replace=False)]
+            ops.append(dict(name=name, wires=ws[:nwk], params=gate_params(name, rng), cwires=ws[nwk:],
+                            cvals=[bool(x) for x in rng.integers(0, 2, size=nc)], inverse=bool(rng.integers(0, 2))))
+        else:
+            name = str(rng.choice(names))
+            nwk = GATES[name][0] or int(rng.integers(1, min(4, n) + 1))
+            if nwk > n:
+                continue
+            w = [int(x) for x in rng.choice(n, size=nwk, replace=False)]
+            ops.append(dict(name=name, wires=w, params=gate_params(name, rng), inverse=bool(rng.integers(0, 2))))
+    return ops
+
+
+def ops_struct(ops_module, dt, ops):
+    OS = ops_module.OpsStructC128 if np.dtype(dt) == np.complex128 else ops_module.OpsStructC64
+    return OS([o["name"] for o in ops], [o.get("params", []) for o in ops], [o["wires"] for o in ops],
+              [o.get("inverse", False) for o in ops], [o.get("matrix") for o in ops],
+              [o.get("cwires", []) for o in ops], [o.get("cvals", []) for o in ops])
+
+
+def oracle_apply(oracle, n, dt, st, ops):
+    o = oracle.sv(n, dt)
+    o.set_state(st)
+    for op in ops:
+        if op.get("matrix") is not None:
+            o.apply_matrix(op["matrix"], op["wires"], op.get("inverse", False), op.get("cwires", ()),
+                           op.get("cvals", ()))
+        else:
+            o.apply(op["name"], op["wires"], op.get("inverse", False), op.get("params", ()), op.get("cwires", ()),
+                    op.get("cvals", ()))
+    return o.state()
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+@pytest.mark.parametrize("n,tile_bits", [(4, 2), (6, 3), (8, 5), (10, 6), (12, 8), (13, 10), (14, 12), (16, 14)])
+def test_random_circuits_fused(ops_module, oracle, dt, n, tile_bits):
+    rng = np.random.default_rng(seed_of("fused", n, tile_bits, dt.__name__))
+    ops = random_circuit(rng, n, 60)
+    st = rand_state(rng, n, dt)
+    sv = sv_class(ops_module, dt)(n)
+    sv.updateData(st)
+    passes = sv.applyOperations(ops_struct(ops_module, dt, ops), tile_bits)
+    assert passes >= 1
+    ref = oracle_apply(oracle, n, dt, st, ops)
+    assert_close(sv.state(), ref, dt, scale=50, what=f"fused n={n} t={tile_bits}")
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+def test_fused_equals_unfused_and_cached_reuse(ops_module, dt):
+    rng = np.random.default_rng(seed_of("fused-vs-unfused", dt.__name__))
+    n = 11
+    ops = random_circuit(rng, n, 80)
+    st = rand_state(rng, n, dt)
+    S = ops_struct(ops_module, dt, ops)
+    a = sv_class(ops_module, dt)(n)
+    b = sv_class(ops_module, dt)(n)
+    a.updateData(st)
+    b.updateData(st)
+    a.applyOperations(S, 0)
+    b.applyOperations(S, 7)
+    assert_close(b.state(), a.state(), dt, scale=50, what="fused vs unfused")
+    # the compiled program is cached on the ops object; apply it again
+    a.applyOperations(S, 0)
+    b.applyOperations(S, 7)
+    assert_close(b.state(), a.state(), dt, scale=100, what="second application")
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+@pytest.mark.parametrize("tile_bits", [6, 9, 12])
+def test_config1_small_fused(ops_module, oracle, dt, tile_bits):
+    # dense Haar SU(2) + CZ: exercises the D.R.D rewrite, merged diagonals and
+    # CZ sign flips across the tile boundary
+    n = 14
+    circuit, _ = config1(n, 6, seed=1001)
+    ops = [op.as_dict() for op in circuit]
+    st = rand_state(np.random.default_rng(3), n, dt)
+    sv = sv_class(ops_module, dt)(n)
+    sv.updateData(st)
+    sv.applyOperations(ops_struct(ops_module, dt, ops), tile_bits)
+    ref = oracle_apply(oracle, n, dt, st, ops)
+    assert_close(sv.state(), ref, dt, scale=50, what=f"config1 t={tile_bits}")
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+def test_config0_fused(ops_module, oracle, dt):
+    n = 12
+    circuit = config0(n, 5, seed=1000)
+    ops = [op.as_dict() for op in circuit]
+    sv = sv_class(ops_module, dt)(n)
+    sv.applyOperations(ops_struct(ops_module, dt, ops), 9)
+    st = np.zeros(1 << n, dt)
+    st[0] = 1
+    ref = oracle_apply(oracle, n, dt, st, ops)
+    assert_close(sv.state(), ref, dt, scale=50, what="config0 fused")

@@ -5,7 +5,9 @@ disjoint pairs), the single-large-circuit configuration the GB300 target is
 quoted on.
 
 A *step* applies the whole circuit (600 SU(2) + 300 CZ gates) to a state that
-is resident in HBM.  ``value`` is the unfused algorithmic traffic of the
+is resident in HBM, through StateVector.applyOperations: either one kernel per
+gate or fused shared-memory tile passes, whichever the warm-up measured
+faster.  ``value`` is the unfused algorithmic traffic of the
 step (sum over gates of 2 f N S, f = fraction of amplitudes a gate changes)
 divided by the step time, in GB/s; ``e2e`` is the same metric through the
 public binding with the state copied in from pinned host memory and back out
@@ -115,18 +117,6 @@ def workload(n, cycles):
     return circuit, ham, unfused_bytes
 
 
-def apply_circuit(sv, circuit, mats, on_dense=None):
-    for i, op in enumerate(circuit):
-        if op.matrix is not None:
-            if on_dense is not None:
-                on_dense(0)
-            sv.applyMatrix(mats[i], op.wires, False)
-            if on_dense is not None:
-                on_dense(1)
-        else:
-            getattr(sv, op.name)(op.wires, False, op.params)
-
-
 def traffic_from_profiles(kernel_tag: str):
     """Per-launch DRAM bytes (read + write) recorded in profiles/<tag>.md."""
     p = REPO / "profiles" / f"{kernel_tag}.md"
@@ -158,9 +148,11 @@ def gpu_arm(args) -> dict | None:
 
     n, cycles = args.qubits, args.cycles
     circuit, ham, unfused_bytes = workload(n, cycles)
-    mats = [np.ascontiguousarray(op.matrix, dtype=np.complex128) if op.matrix is not None else None for op in circuit]
     alg_bytes = unfused_bytes(circuit, n, 16)
-    n_dense = sum(1 for op in circuit if op.matrix is not None)
+
+    def ops_struct(cls):
+        return cls([o.name for o in circuit], [o.params for o in circuit], [o.wires for o in circuit],
+                    [False] * len(circuit), [o.matrix for o in circuit])
 
     def barrier():
         torch.cuda.synchronize()
@@ -169,37 +161,42 @@ def gpu_arm(args) -> dict | None:
 
             dist.barrier()
 
+    def timed_step(sv, S, stream, tb):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        passes = sv.applyOperations(S, tb)
+        b.record(stream)
+        sv.synchronize()
+        return a.elapsed_time(b), passes
+
+    S128 = ops_struct(ops.OpsStructC128)
     sv = ops.StateVectorC128(n)
     stream = torch.cuda.ExternalStream(sv.cuda_stream())
-    for _ in range(args.warmup):
-        apply_circuit(sv, circuit, mats)
-    sv.synchronize()
+    # warm-up doubles as the tile-size choice: unfused (0) vs fused tiles of 2^t
+    candidates = [0, 11, 12, 13]
+    tune = {}
+    for w in range(max(args.warmup, 1)):
+        tb = candidates[w % len(candidates)] if w < len(candidates) else best_tb
+        ms, _ = timed_step(sv, S128, stream, tb)
+        tune[tb] = min(ms, tune.get(tb, float("inf")))
+        best_tb = min(tune, key=tune.get)
+    for tb in candidates:
+        if tb not in tune:
+            tune[tb], _ = timed_step(sv, S128, stream, tb)
+    best_tb = min(tune, key=tune.get)
 
-    # per-launch events for the dominant kernel (dense one-qubit update)
-    ev = [[torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)]
-          for _ in range(n_dense * args.steps)]
-    cursor = [0]
-
-    def on_dense(which):
-        ev[cursor[0]][which].record(stream)
-        if which == 1:
-            cursor[0] += 1
-
-    step_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     launches0 = ops.kernel_launches()
+    step_ms, step_passes = [], []
     barrier()
-    sv.synchronize()
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
-        for k in range(args.steps):
-            step_ev[k][0].record(stream)
-            apply_circuit(sv, circuit, mats, on_dense)
-            step_ev[k][1].record(stream)
-        sv.synchronize()
+        for _ in range(args.steps):
+            ms, passes = timed_step(sv, S128, stream, best_tb)
+            step_ms.append(ms)
+            step_passes.append(passes)
         barrier()
         wall = time.perf_counter() - t0
     launches = ops.kernel_launches() - launches0
-    step_ms = [a.elapsed_time(b) for a, b in step_ev]
     total_s = sum(step_ms) / 1e3
     if ws > 1:
         import torch.distributed as dist
@@ -207,13 +204,13 @@ def gpu_arm(args) -> dict | None:
         t = torch.tensor([total_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_s = float(t.item())
-    dense_ms = [a.elapsed_time(b) for a, b in ev[: cursor[0]]]
-    dense_avg_s = statistics.mean(dense_ms) / 1e3
-    dense_bytes = 2.0 * (1 << n) * 16
-    achieved = dense_bytes / dense_avg_s / 1e9
-    traffic = traffic_from_profiles("k_1q_dense_c128")
-    if traffic is not None:
-        traffic = traffic * ((1 << n) / float(1 << 28))  # profile captured at 28 qubits, scaled per launch
+    passes = step_passes[0]
+    pass_bytes = 2.0 * (1 << n) * 16
+    avg_launch_s = (total_s / args.steps) / passes
+    achieved = pass_bytes / avg_launch_s / 1e9
+    kernel = "k_tile_pass<double> (fused tile pass)" if best_tb else "k_1q<double, DENSE> and k_1q<double, NEG1>"
+    tag = "k_tile_pass_c128" if best_tb else "k_1q_dense_c128"
+    traffic = traffic_from_profiles(tag)
 
     # expectation value of the 64-term Hamiltonian (one read per flip-mask group)
     H = ops.observables.HamiltonianC128(
@@ -237,11 +234,11 @@ def gpu_arm(args) -> dict | None:
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         sv.updateData(hin)
-        apply_circuit(sv, circuit, mats)
+        sv.applyOperations(S128, best_tb)
         sv.getState(hout)
     barrier()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
-    h2d = (1 << n) * 16 + sum(m_.nbytes for m_ in mats if m_ is not None)
+    h2d = (1 << n) * 16 + sum(o.matrix.nbytes for o in circuit if o.matrix is not None)
     d2h = (1 << n) * 16
     del sv
 
@@ -253,31 +250,34 @@ def gpu_arm(args) -> dict | None:
         "config": {"workload": f"config1: {n} qubits complex128, {cycles} cycles x ({n} Haar SU(2) + {n // 2} CZ)",
                    "qubits": n, "gates_per_step": len(circuit), "algorithmic_bytes_per_step": alg_bytes,
                    "l2": "inputs larger than L2 (16 GiB state)", "parallelism": f"replicas x{ws}",
-                   "path": "unfused per-gate kernels"},
+                   "path": f"fused tile passes, 2^{best_tb} amplitudes per tile" if best_tb else "unfused per-gate kernels",
+                   "tile_bits": best_tb, "passes_per_step": passes,
+                   "tuning_ms_per_step": {str(k): round(v, 1) for k, v in sorted(tune.items())}},
         "e2e": {"value": alg_bytes / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
-        "roofline": {"kernel": "k_1q<double, DENSE> (dense SU(2) update)", "bound": "hbm", "achieved": achieved,
-                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                     "peak_source": f"{peak_src} hbm_gbs",
-                     "traffic": traffic, "algorithmic_bytes_per_launch": dense_bytes,
-                     "avg_launch_ms": dense_avg_s * 1e3},
+        "roofline": {"kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "peak_source": f"{peak_src} hbm_gbs", "traffic": traffic,
+                     "algorithmic_bytes_per_launch": pass_bytes, "avg_launch_ms": avg_launch_s * 1e3,
+                     "note": "complex128 gates on GB300 are bound by the FP64 pipe (1.25 TFLOP/s measured), "
+                             "not by HBM; achieved = bytes one launch must move / mean launch time"},
+        "unfused": {"ms_per_step": tune.get(0), "value": alg_bytes / (tune[0] / 1e3) / 1e9 if tune.get(0) else None},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "expval_64_terms": {"value": ev_val, "ms": expval_ms},
         "wall_s_timed": wall,
     }
     if not args.no_c64:
+        S64 = ops_struct(ops.OpsStructC64)
         sv64 = ops.StateVectorC64(n)
-        apply_circuit(sv64, circuit, mats)
-        sv64.synchronize()
         s64 = torch.cuda.ExternalStream(sv64.cuda_stream())
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(s64)
-        apply_circuit(sv64, circuit, mats)
-        b.record(s64)
-        sv64.synchronize()
-        ms = a.elapsed_time(b)
-        res["c64"] = {"value": unfused_bytes(circuit, n, 8) / (ms / 1e3) / 1e9, "unit": UNIT, "ms_per_step": ms}
+        t64 = {}
+        for tb in (0, 12, 13):
+            timed_step(sv64, S64, s64, tb)
+            t64[tb] = timed_step(sv64, S64, s64, tb)[0]
+        b64 = min(t64, key=t64.get)
+        res["c64"] = {"value": unfused_bytes(circuit, n, 8) / (t64[b64] / 1e3) / 1e9, "unit": UNIT,
+                      "ms_per_step": t64[b64], "tile_bits": b64,
+                      "tuning_ms_per_step": {str(k): round(v, 1) for k, v in sorted(t64.items())}}
         del sv64
     return res
 

@@ -453,7 +453,59 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
             pend.clear();
         };
 
-        for (size_t pi : pp.prims) {
+        // Order the pass as dependency layers: non-diagonal ops at level
+        // 1 + (level of anything they depend on), diagonals at the level of
+        // their latest non-diagonal predecessor.  All diagonals of one level
+        // then merge into a single op placed between two layers.
+        std::vector<int> level(pp.prims.size(), 0);
+        {
+            std::vector<int> nd_level(64, 0), d_level(64, 0);
+            for (size_t k = 0; k < pp.prims.size(); k++) {
+                const size_t pi = pp.prims[k];
+                const u64 tb = touch[pi];
+                int lv = 0;
+                if (diag[pi]) {
+                    for (int b = 0; b < 64; b++) {
+                        if ((tb >> b) & 1U) {
+                            lv = std::max(lv, nd_level[static_cast<size_t>(b)]);
+                        }
+                    }
+                    for (int b = 0; b < 64; b++) {
+                        if ((tb >> b) & 1U) {
+                            d_level[static_cast<size_t>(b)] = std::max(d_level[static_cast<size_t>(b)], lv);
+                        }
+                    }
+                } else {
+                    for (int b = 0; b < 64; b++) {
+                        if ((tb >> b) & 1U) {
+                            lv = std::max({lv, nd_level[static_cast<size_t>(b)], d_level[static_cast<size_t>(b)]});
+                        }
+                    }
+                    lv += 1;
+                    for (int b = 0; b < 64; b++) {
+                        if ((tb >> b) & 1U) {
+                            nd_level[static_cast<size_t>(b)] = lv;
+                        }
+                    }
+                }
+                level[k] = lv;
+            }
+        }
+        const int maxlv = pp.prims.empty() ? 0 : *std::max_element(level.begin(), level.end());
+        std::vector<size_t> ordered;
+        for (int lv = 0; lv <= maxlv; lv++) {
+            for (size_t k = 0; k < pp.prims.size(); k++) { // the layer's non-diagonal ops
+                if (level[k] == lv && !diag[pp.prims[k]]) {
+                    ordered.push_back(pp.prims[k]);
+                }
+            }
+            for (size_t k = 0; k < pp.prims.size(); k++) { // then the diagonals between layers
+                if (level[k] == lv && diag[pp.prims[k]]) {
+                    ordered.push_back(pp.prims[k]);
+                }
+            }
+        }
+        for (size_t pi : ordered) {
             const auto &p = P[pi];
             Diag<T> dg;
             if (to_diag(p, dg)) {

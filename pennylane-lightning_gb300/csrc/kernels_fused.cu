@@ -37,7 +37,19 @@ __device__ __forceinline__ u32 insert_zeros32(u32 k, const int *ins, int nins) {
     return k;
 }
 
-template <class T> __device__ __forceinline__ cx<T> flip(cx<T> v, bool neg) { return neg ? cx<T>{-v.x, -v.y} : v; }
+// sign flip on the integer pipe (no floating-point instruction)
+__device__ __forceinline__ double flip_sign(double x, unsigned neg) {
+    return __longlong_as_double(__double_as_longlong(x) ^ (static_cast<long long>(neg) << 63));
+}
+__device__ __forceinline__ float flip_sign(float x, unsigned neg) {
+    return __int_as_float(__float_as_int(x) ^ static_cast<int>(neg << 31));
+}
+template <class T> __device__ __forceinline__ cx<T> flip(cx<T> v, unsigned neg) {
+    return cx<T>{flip_sign(v.x, neg), flip_sign(v.y, neg)};
+}
+template <class T> __device__ __forceinline__ cx<T> shfl_xor(cx<T> v, int m) {
+    return cx<T>{__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m)};
+}
 
 // Evaluate a small diagonal form on the global bits of a tile base.
 template <class T> __device__ cx<T> form_value(const DiagForm<T> &f, u64 gbase) {
@@ -167,34 +179,52 @@ __global__ void __launch_bounds__(kTileThreads) k_tile_pass(cx<T> *__restrict__ 
                 break;
             }
             case TK_DIAGTAB: {
-                if (threadIdx.x == 0) {
+                // warp 0 evaluates the tile-uniform parts in parallel: the
+                // product of the global-bit factors, and per cross-boundary
+                // two-bit factor either a scalar, a sign flip of one local
+                // bit, or a general one-bit local factor
+                if (threadIdx.x < 32) {
+                    const int lane = threadIdx.x;
                     cx<T> sc{1, 0};
-                    for (int f = 0; f < op.ngforms; f++) {
+                    for (int f = lane; f < op.ngforms; f += 32) {
                         sc = sc * form_value(forms[op.gform_begin + f], gbase);
                     }
                     u32 zl = 0;
-                    int ngen = 0;
-                    for (int f = 0; f < op.nmforms; f++) {
-                        // mixed form: bits[0] global, local bit op.mbit[f]
-                        const DiagForm<T> &mf = forms[op.mform_begin + f];
+                    bool gen = false;
+                    cx<T> d0{1, 0}, d1{1, 0};
+                    int lb = 0;
+                    if (lane < op.nmforms) {
+                        const DiagForm<T> &mf = forms[op.mform_begin + lane];
                         const unsigned gb = static_cast<unsigned>((gbase >> mf.bits[0]) & 1u);
-                        const cx<T> d0 = mf.tab[2 * gb], d1 = mf.tab[2 * gb + 1];
-                        const int lb = mf.local_bit;
+                        d0 = mf.tab[2 * gb];
+                        d1 = mf.tab[2 * gb + 1];
+                        lb = mf.local_bit;
                         if (d1.x == d0.x && d1.y == d0.y) {
                             sc = sc * d0;
                         } else if (d1.x == -d0.x && d1.y == -d0.y) {
                             sc = sc * d0;
-                            zl ^= 1u << lb;
+                            zl = 1u << lb;
                         } else {
-                            s_gen_bit[ngen] = lb;
-                            s_gen_d0[ngen] = d0;
-                            s_gen_d1[ngen] = d1;
-                            ngen++;
+                            gen = true;
                         }
                     }
-                    s_tile_factor = s_tile_factor * sc;
-                    s_sign_mask = zl;
-                    s_ngen = ngen;
+#pragma unroll
+                    for (int m = 16; m > 0; m >>= 1) {
+                        sc = sc * shfl_xor(sc, m);
+                        zl ^= __shfl_xor_sync(0xffffffffu, zl, m);
+                    }
+                    const unsigned genmask = __ballot_sync(0xffffffffu, gen);
+                    if (gen) {
+                        const int slot = __popc(genmask & ((1u << lane) - 1u));
+                        s_gen_bit[slot] = lb;
+                        s_gen_d0[slot] = d0;
+                        s_gen_d1[slot] = d1;
+                    }
+                    if (lane == 0) {
+                        s_tile_factor = s_tile_factor * sc;
+                        s_sign_mask = zl;
+                        s_ngen = __popc(genmask);
+                    }
                 }
                 __syncthreads();
                 const u32 zl = s_sign_mask;
@@ -205,7 +235,7 @@ __global__ void __launch_bounds__(kTileThreads) k_tile_pass(cx<T> *__restrict__ 
                     for (int f = 0; f < ngen; f++) {
                         v = (((j >> s_gen_bit[f]) & 1u) ? s_gen_d1[f] : s_gen_d0[f]) * v;
                     }
-                    tile[j] = flip(v, __popc(j & zl) & 1);
+                    tile[j] = flip(v, static_cast<unsigned>(__popc(j & zl) & 1));
                 }
                 break;
             }

@@ -178,6 +178,10 @@ int plgb_ops_num_par_ops(const plgb_ops *ops, int *out);
  * passes are cached on `ops` per register size, precision and t).
  * *passes_out (optional) receives the number of kernel passes per call. */
 int plgb_sv_apply_operations(plgb_sv *sv, plgb_ops *ops, int tile_bits, int *passes_out);
+/* Plan introspection (no device needed): the tile passes plgb_sv_apply_operations
+ * would run for `ops` on num_qubits at precision / tile_bits, as a JSON array
+ * with one object per pass (tile size, op counts, execution stages). */
+int plgb_ops_fusion_plan(const plgb_ops *ops, int num_qubits, int precision, int tile_bits, char *buf, size_t len);
 /* AdjointJacobianC*.__call__(sv, observables, ops, trainable_params):
  * jac_out holds nobs * ntp doubles, row-major [obs][param].  With apply_ops
  * the operations are first applied to a copy of the state. */

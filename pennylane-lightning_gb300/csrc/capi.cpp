@@ -633,6 +633,34 @@ int plgb_sv_apply_operations(plgb_sv *sv, plgb_ops *ops, int tile_bits, int *pas
     });
 }
 
+int plgb_ops_fusion_plan(const plgb_ops *ops, int num_qubits, int precision, int tile_bits, char *buf, size_t len) {
+    std::string js;
+    const int rc = guard([&] {
+        need(ops, "ops");
+        PLGB_REQUIRE(precision == 64 || precision == 128, "precision must be 64 or 128");
+        PLGB_REQUIRE(tile_bits >= 1 && tile_bits <= 14, "tile_bits must be in 1..14");
+        auto plan = [&](auto tag) {
+            using T = decltype(tag);
+            StateVector<T> reg(num_qubits, LowerOnly{});
+            std::vector<Prim<T>> prims;
+            for (const auto &op : ops->list.ops) {
+                auto p = reg.lower_op(op, op.inverse);
+                prims.insert(prims.end(), std::make_move_iterator(p.begin()), std::make_move_iterator(p.end()));
+            }
+            js = fused_plan_json<T>(*compile_fused<T>(num_qubits, prims, tile_bits, false));
+        };
+        if (precision == 128) {
+            plan(double{});
+        } else {
+            plan(float{});
+        }
+    });
+    if (rc != PLGB_OK) {
+        return rc;
+    }
+    return copy_text(js, buf, len);
+}
+
 int plgb_adjoint_jacobian(plgb_sv *sv, plgb_obs *const *obs, int nobs, const plgb_ops *ops, const int64_t *trainable,
                           int ntp, int apply_ops, double *jac_out) {
     return with_sv(sv, [&](auto &s) {

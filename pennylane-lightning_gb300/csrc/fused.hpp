@@ -17,6 +17,10 @@ enum TileKind : int {
     TK_PARITY = 4,  // parity phase on the full index (MultiRZ and its generator)
 };
 
+constexpr int kRegBits = 4;              // amplitudes per thread in register stages: 2^4
+constexpr int kMinRegTileBits = 9;       // register kernel needs >= 32 threads
+constexpr int kMaxDiagOpsPerPass = 48;   // merged diagonals evaluated per tile
+
 struct TilePassDesc {
     int t;          // local bits in a tile
     int L;          // the lowest L bits are always local
@@ -25,6 +29,20 @@ struct TilePassDesc {
     u64 ntiles;     // 2^(n - t)
     int op_begin, nops;
     double pass_scale; // product of the scalars factored out of rotations
+    // register-blocked execution (t >= kMinRegTileBits): stages over the op list
+    int stage_begin, nstages;
+    int ndiag;      // merged-diagonal ops in the pass (prologue slots)
+};
+
+// A stage of a register-blocked pass.  REG: ops [op_begin, op_begin+nops)
+// run on amplitudes held in registers, register bit k being local bit rb[k]
+// and thread-index bit m local bit tb[m].  SMEM: the ops run on the tile in
+// shared memory (two-target ops).
+struct StageDesc {
+    int kind; // 0 = REG, 1 = SMEM
+    int op_begin, nops;
+    int rb[kRegBits];
+    int tb[kMaxTileBits];
 };
 
 template <class T> struct TileOp {
@@ -43,6 +61,11 @@ template <class T> struct TileOp {
     // PARITY (full index)
     u64 pmask{0}, cmask{0}, cval{0};
     int zero_outside{0};
+    // register stages: target register bit, control predicates over the
+    // register index and the thread index, slot of a merged diagonal
+    int rk{0};
+    u32 rcmask{0}, rcval{0}, tcmask{0}, tcval{0};
+    int diag_slot{0};
     cx<T> m[16]{};
 };
 
@@ -59,5 +82,11 @@ template <class T> struct DiagForm {
 template <class T>
 void launch_tile_pass(cudaStream_t s, cx<T> *sv, const TilePassDesc &d, const TileOp<T> *ops, const DiagForm<T> *forms,
                       const cx<T> *tables);
+template <class T>
+void launch_tile_pass_reg(cudaStream_t s, cx<T> *sv, const TilePassDesc &d, const TileOp<T> *ops,
+                          const DiagForm<T> *forms, const cx<T> *tables, const StageDesc *stages);
+
+// register-stage op codes (TileOp::mode when executed in registers)
+enum RegMode : int { RM_SROT_A = 0, RM_SROT_B = 1, RM_SWAP = 2, RM_DENSE = 3 };
 
 } // namespace plgb

@@ -99,10 +99,13 @@ template <class T> struct Prim {
     bool diagonal() const;    // multiplies each amplitude by a factor (no mixing)
 };
 
+struct LowerOnly {}; // a register description for lowering gates without device memory
+
 template <class T> class StateVector {
   public:
     using CT = cx<T>;
     explicit StateVector(int num_qubits, cudaStream_t stream = nullptr);
+    StateVector(int num_qubits, LowerOnly); // no device memory: only lower_op() may be used
     StateVector(CT *external, int num_qubits, cudaStream_t stream = nullptr); // non-owning
     StateVector(const StateVector &other);                                     // deep copy, same stream
     StateVector &operator=(const StateVector &) = delete;
@@ -195,7 +198,10 @@ template <class T> class StateVector {
 // ---------------------------------------------------------------------------
 template <class T> struct FusedProgram;
 template <class T>
-std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>> &prims, int tile_bits);
+std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>> &prims, int tile_bits,
+                                               bool upload = true);
+// JSON description of a compiled program's passes (plan introspection)
+template <class T> std::string fused_plan_json(const FusedProgram<T> &prog);
 template <class T> void run_fused(StateVector<T> &sv, const FusedProgram<T> &prog);
 struct FusedStats {
     size_t passes, unfused, prims;

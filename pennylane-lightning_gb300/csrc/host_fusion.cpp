@@ -26,6 +26,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <map>
 
 namespace plgb {
@@ -59,10 +61,13 @@ template <class T> std::vector<Prim<T>> rewrite(const std::vector<Prim<T>> &in) 
             out.push_back(std::move(r));
             continue;
         }
-        if (single && p.mode == M1_DENSE) {
+        if (single && (p.mode == M1_DENSE || p.mode == M1_RXF)) {
             // U = diag(e^{i a0}, e^{i a1}) [[c, -s], [s, c]] diag(e^{i b0}, e^{i b1}), b0 = 0
-            const std::complex<double> u00(p.m[0].x, p.m[0].y), u01(p.m[1].x, p.m[1].y), u10(p.m[2].x, p.m[2].y),
-                u11(p.m[3].x, p.m[3].y);
+            // RX-form coefficients are stored as (c, s): U = [[c, i s], [i s, c]]
+            const bool rxf = p.mode == M1_RXF;
+            const std::complex<double> u00(p.m[0].x, rxf ? 0.0 : p.m[0].y),
+                u01(rxf ? 0.0 : p.m[1].x, p.m[1].y), u10(rxf ? 0.0 : p.m[2].x, rxf ? p.m[1].y : p.m[2].y),
+                u11(p.m[rxf ? 0 : 3].x, rxf ? 0.0 : p.m[3].y);
             const double cm = std::abs(u00), sm = std::abs(u10);
             const double a0 = std::arg(u00), a1 = std::arg(u10);
             const double b1 = cm >= sm ? std::arg(u11) - a1 : std::arg(-u01) - a0;
@@ -155,6 +160,7 @@ struct PassPlan {
 template <class T> struct FusedProgram {
     struct Seg {
         bool tile{false};
+        bool reg{false}; // register-blocked kernel
         TilePassDesc desc{};
         Prim<T> prim; // unfused segment
     };
@@ -163,8 +169,10 @@ template <class T> struct FusedProgram {
     TileOp<T> *d_ops{nullptr};
     DiagForm<T> *d_forms{nullptr};
     cx<T> *d_tables{nullptr};
+    StageDesc *d_stages{nullptr};
     int n{0};
     size_t passes{0}, unfused{0}, prims{0};
+    std::string plan; // JSON lines of the segments
     ~FusedProgram() {
         if (dev) {
             cudaFree(dev);
@@ -172,8 +180,172 @@ template <class T> struct FusedProgram {
     }
 };
 
+// Split a pass's op range into register / shared-memory stages for the
+// register-blocked kernel and rewrite the ops' modes for it.  Returns false
+// when the pass needs the plain tile kernel.
 template <class T>
-std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>> &in, int tile_bits) {
+bool plan_stages(std::vector<TileOp<T>> &ops, const std::vector<DiagForm<T>> &forms, TilePassDesc &d,
+                 std::vector<StageDesc> &stages) {
+    if (d.t < kMinRegTileBits || d.t > 12) { // 2^(t-4) <= 256 threads
+        return false;
+    }
+    const int begin = d.op_begin, end = d.op_begin + d.nops;
+    auto single_target = [&](const TileOp<T> &op, int &q) {
+        if ((op.kind != TK_PAIR && op.kind != TK_SROT) || op.lo0 != 0 || __builtin_popcount(op.lo1) != 1) {
+            return false;
+        }
+        q = __builtin_ctz(op.lo1);
+        return true;
+    };
+    auto is_diag = [](const TileOp<T> &op) { return op.kind == TK_DIAGTAB || op.kind == TK_PARITY; };
+    // limits of the register kernel's per-tile prologue
+    int ndiag = 0;
+    for (int i = begin; i < end; i++) {
+        if (ops[static_cast<size_t>(i)].kind != TK_DIAGTAB) {
+            continue;
+        }
+        const auto &op = ops[static_cast<size_t>(i)];
+        int general = 0;
+        for (int f = 0; f < op.nmforms; f++) {
+            const auto &mf = forms[static_cast<size_t>(op.mform_begin + f)];
+            for (int gb = 0; gb < 2; gb++) {
+                const cx<T> d0 = mf.tab[2 * gb], d1 = mf.tab[2 * gb + 1];
+                const bool same = d1.x == d0.x && d1.y == d0.y;
+                const bool neg = d1.x == -d0.x && d1.y == -d0.y;
+                if (!same && !neg) {
+                    general++;
+                    break;
+                }
+            }
+        }
+        if (general > 4) {
+            return false;
+        }
+        ndiag++;
+    }
+    if (ndiag > kMaxDiagOpsPerPass) {
+        return false;
+    }
+    const int w = d.t - kRegBits;
+    auto layout_from = [&](int i0, int first_q) {
+        StageDesc st{};
+        st.kind = 0;
+        std::vector<int> rb;
+        if (first_q >= 0) {
+            rb.push_back(first_q);
+        }
+        for (int i = i0; i < end && static_cast<int>(rb.size()) < kRegBits; i++) {
+            const auto &op = ops[static_cast<size_t>(i)];
+            int q;
+            if (single_target(op, q)) {
+                if (std::find(rb.begin(), rb.end(), q) == rb.end()) {
+                    rb.push_back(q);
+                }
+            } else if (!is_diag(op)) {
+                break;
+            }
+        }
+        for (int b = d.t - 1; b >= 0 && static_cast<int>(rb.size()) < kRegBits; b--) {
+            if (std::find(rb.begin(), rb.end(), b) == rb.end()) {
+                rb.push_back(b);
+            }
+        }
+        for (int k = 0; k < kRegBits; k++) {
+            st.rb[k] = rb[static_cast<size_t>(k)];
+        }
+        int m = 0;
+        for (int b = 0; b < d.t; b++) {
+            if (std::find(rb.begin(), rb.end(), b) == rb.end()) {
+                st.tb[m++] = b;
+            }
+        }
+        (void)w;
+        return st;
+    };
+    std::vector<StageDesc> local;
+    int cur = -1;
+    int slot = 0;
+    for (int i = begin; i < end; i++) {
+        auto &op = ops[static_cast<size_t>(i)];
+        int q;
+        if (is_diag(op)) {
+            if (cur < 0 || local[static_cast<size_t>(cur)].kind != 0) {
+                local.push_back(layout_from(i, -1));
+                local.back().op_begin = i;
+                cur = static_cast<int>(local.size()) - 1;
+            }
+            if (op.kind == TK_DIAGTAB) {
+                op.diag_slot = slot++;
+            }
+        } else if (single_target(op, q)) {
+            bool in = false;
+            if (cur >= 0 && local[static_cast<size_t>(cur)].kind == 0) {
+                for (int k = 0; k < kRegBits; k++) {
+                    in = in || local[static_cast<size_t>(cur)].rb[k] == q;
+                }
+            }
+            if (!in) {
+                local.push_back(layout_from(i, q));
+                local.back().op_begin = i;
+                cur = static_cast<int>(local.size()) - 1;
+            }
+            const auto &st = local[static_cast<size_t>(cur)];
+            for (int k = 0; k < kRegBits; k++) {
+                if (st.rb[k] == q) {
+                    op.rk = k;
+                }
+            }
+            // controls: every local insert bit except the target
+            op.rcmask = 0;
+            for (int k = 0; k < op.nlins; k++) {
+                if (op.lins[k] != q) {
+                    op.rcmask |= 1u << op.lins[k];
+                }
+            }
+            op.rcval = op.lcval;
+        } else {
+            if (cur < 0 || local[static_cast<size_t>(cur)].kind != 1) {
+                StageDesc st{};
+                st.kind = 1;
+                st.op_begin = i;
+                local.push_back(st);
+                cur = static_cast<int>(local.size()) - 1;
+            }
+        }
+        local[static_cast<size_t>(cur)].nops = i - local[static_cast<size_t>(cur)].op_begin + 1;
+        // register-kernel mode codes
+        if (op.kind == TK_SROT) {
+            op.mode = op.mode == 0 ? RM_SROT_A : RM_SROT_B;
+        } else if (op.kind == TK_PAIR) {
+            if (op.mode == M1_SWAP) {
+                op.mode = RM_SWAP;
+            } else {
+                if (op.mode == M1_NEG1) {
+                    op.m[0] = cx<T>{1, 0};
+                    op.m[1] = op.m[2] = cx<T>{0, 0};
+                    op.m[3] = cx<T>{-1, 0};
+                } else if (op.mode == M1_PHASE1) {
+                    op.m[0] = cx<T>{1, 0};
+                    op.m[1] = op.m[2] = cx<T>{0, 0};
+                } else if (op.mode == M1_DIAG) {
+                    op.m[1] = op.m[2] = cx<T>{0, 0};
+                } else if (op.mode == M1_SWAP) {
+                    op.m[0] = op.m[3] = cx<T>{0, 0};
+                    op.m[1] = op.m[2] = cx<T>{1, 0};
+                }
+                op.mode = RM_DENSE;
+            }
+        }
+    }
+    d.stage_begin = static_cast<int>(stages.size());
+    d.nstages = static_cast<int>(local.size());
+    d.ndiag = ndiag;
+    stages.insert(stages.end(), local.begin(), local.end());
+    return true;
+}
+
+template <class T>
+std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>> &in, int tile_bits, bool upload) {
     auto prog = std::make_shared<FusedProgram<T>>();
     prog->n = n;
     const int tmax = std::max(1, std::min({tile_bits, n, kMaxTileBits}));
@@ -258,7 +430,9 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
                             }
                         }
                         ok = nglob == 0 || (nloc == 0 && nglob <= 4) || (nglob == 1 && nloc == 1);
-                        if (ok) {
+                        // one- and two-bit diagonals stay valid when a bit turns
+                        // local; wider ones pin their global bits
+                        if (ok && dd.bits.size() >= 3) {
                             frozen |= gbits;
                         }
                     }
@@ -271,6 +445,12 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
                     blocked_d |= touch[i];
                 } else {
                     blocked_nd |= touch[i];
+                }
+            }
+            // full tiles: pad the local set with free (non-frozen) bits
+            for (int b = L; b < n && __builtin_popcountll(pp.local) < tmax; b++) {
+                if (!((pp.local >> b) & 1U) && !((frozen >> b) & 1U)) {
+                    pp.local |= u64{1} << b;
                 }
             }
             if (pp.prims.empty()) {
@@ -303,6 +483,7 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
     std::vector<TileOp<T>> ops;
     std::vector<DiagForm<T>> forms;
     std::vector<cx<T>> tables;
+    std::vector<StageDesc> stages;
     for (auto &pp : plan) {
         typename FusedProgram<T>::Seg seg;
         if (!pp.fused) {
@@ -575,19 +756,61 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
         }
         flush();
         d.nops = static_cast<int>(ops.size()) - d.op_begin;
+        seg.reg = plan_stages<T>(ops, forms, d, stages);
         prog->segs.push_back(std::move(seg));
         prog->passes++;
+    }
+
+    // plan description: one JSON object per segment
+    {
+        std::string js = "[";
+        for (size_t si = 0; si < prog->segs.size(); si++) {
+            const auto &seg = prog->segs[si];
+            char buf[256];
+            if (!seg.tile) {
+                std::snprintf(buf, sizeof(buf), "%s{\"tile\": false, \"prim\": %d}", si ? ", " : "",
+                              static_cast<int>(seg.prim.kind));
+                js += buf;
+                continue;
+            }
+            const auto &d = seg.desc;
+            int nreg = 0, nsm = 0, ndg = 0, nrot = 0, npair = 0;
+            for (int i = d.op_begin; i < d.op_begin + d.nops; i++) {
+                const int k = ops[static_cast<size_t>(i)].kind;
+                ndg += (k == TK_DIAGTAB || k == TK_PARITY) ? 1 : 0;
+                nrot += (k == TK_SROT) ? 1 : 0;
+                npair += (k == TK_PAIR || k == TK_DENSE2) ? 1 : 0;
+            }
+            for (int sidx = d.stage_begin; seg.reg && sidx < d.stage_begin + d.nstages; sidx++) {
+                (stages[static_cast<size_t>(sidx)].kind == 0 ? nreg : nsm)++;
+            }
+            std::snprintf(buf, sizeof(buf),
+                          "%s{\"tile\": true, \"t\": %d, \"ops\": %d, \"rotations\": %d, \"pairs\": %d, "
+                          "\"diagonals\": %d, \"register_kernel\": %s, \"reg_stages\": %d, \"smem_stages\": %d}",
+                          si ? ", " : "", d.t, d.nops, nrot, npair, ndg, seg.reg ? "true" : "false", nreg, nsm);
+            js += buf;
+        }
+        prog->plan = js + "]";
+    }
+    if (!upload) {
+        return prog;
     }
 
     // ---- upload
     const size_t b_ops = align_up(std::max<size_t>(1, ops.size()) * sizeof(TileOp<T>));
     const size_t b_forms = align_up(std::max<size_t>(1, forms.size()) * sizeof(DiagForm<T>));
     const size_t b_tab = align_up(std::max<size_t>(1, tables.size()) * sizeof(cx<T>));
-    cuda_check(cudaMalloc(&prog->dev, b_ops + b_forms + b_tab), "cudaMalloc(fused program)");
+    const size_t b_st = align_up(std::max<size_t>(1, stages.size()) * sizeof(StageDesc));
+    cuda_check(cudaMalloc(&prog->dev, b_ops + b_forms + b_tab + b_st), "cudaMalloc(fused program)");
     char *base = static_cast<char *>(prog->dev);
     prog->d_ops = reinterpret_cast<TileOp<T> *>(base);
     prog->d_forms = reinterpret_cast<DiagForm<T> *>(base + b_ops);
     prog->d_tables = reinterpret_cast<cx<T> *>(base + b_ops + b_forms);
+    prog->d_stages = reinterpret_cast<StageDesc *>(base + b_ops + b_forms + b_tab);
+    if (!stages.empty()) {
+        cuda_check(cudaMemcpy(prog->d_stages, stages.data(), stages.size() * sizeof(StageDesc),
+                              cudaMemcpyHostToDevice), "H2D");
+    }
     if (!ops.empty()) {
         cuda_check(cudaMemcpy(prog->d_ops, ops.data(), ops.size() * sizeof(TileOp<T>), cudaMemcpyHostToDevice), "H2D");
     }
@@ -605,7 +828,10 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
 template <class T> void run_fused(StateVector<T> &sv, const FusedProgram<T> &prog) {
     PLGB_REQUIRE(prog.n == sv.num_qubits(), "fused program compiled for a different register size");
     for (const auto &seg : prog.segs) {
-        if (seg.tile) {
+        if (seg.tile && seg.reg) {
+            launch_tile_pass_reg<T>(sv.stream(), sv.data(), seg.desc, prog.d_ops, prog.d_forms, prog.d_tables,
+                                    prog.d_stages);
+        } else if (seg.tile) {
             launch_tile_pass<T>(sv.stream(), sv.data(), seg.desc, prog.d_ops, prog.d_forms, prog.d_tables);
         } else {
             sv.run_prim(seg.prim);
@@ -620,6 +846,10 @@ void StateVector<T>::apply_prims_fused(const std::vector<Prim<T>> &prims, int ti
     synchronize(); // the program's device buffer is freed on return
 }
 
+template <class T> std::string fused_plan_json(const FusedProgram<T> &prog) { return prog.plan; }
+template std::string fused_plan_json<float>(const FusedProgram<float> &);
+template std::string fused_plan_json<double>(const FusedProgram<double> &);
+
 template <class T> FusedStats fused_stats(const FusedProgram<T> &prog) {
     return FusedStats{prog.passes, prog.unfused, prog.prims};
 }
@@ -628,8 +858,9 @@ template FusedStats fused_stats<double>(const FusedProgram<double> &);
 
 template struct FusedProgram<float>;
 template struct FusedProgram<double>;
-template std::shared_ptr<FusedProgram<float>> compile_fused<float>(int, const std::vector<Prim<float>> &, int);
-template std::shared_ptr<FusedProgram<double>> compile_fused<double>(int, const std::vector<Prim<double>> &, int);
+template std::shared_ptr<FusedProgram<float>> compile_fused<float>(int, const std::vector<Prim<float>> &, int, bool);
+template std::shared_ptr<FusedProgram<double>> compile_fused<double>(int, const std::vector<Prim<double>> &, int,
+                                                                     bool);
 template void run_fused<float>(StateVector<float> &, const FusedProgram<float> &);
 template void run_fused<double>(StateVector<double> &, const FusedProgram<double> &);
 template void StateVector<float>::apply_prims_fused(const std::vector<Prim<float>> &, int);

@@ -123,6 +123,12 @@ template <class T> StateVector<T>::StateVector(int num_qubits, cudaStream_t stre
     reset();
 }
 
+template <class T> StateVector<T>::StateVector(int num_qubits, LowerOnly) : n_(num_qubits) {
+    PLGB_REQUIRE(n_ >= 0 && n_ <= 40, "number of qubits out of range");
+    N_ = u64{1} << n_;
+    owns_ = false;
+}
+
 template <class T> StateVector<T>::StateVector(CT *external, int num_qubits, cudaStream_t stream) : n_(num_qubits) {
     owns_ = false;
     d_ = external;
@@ -149,6 +155,7 @@ template <class T> StateVector<T>::~StateVector() {
         cudaStreamDestroy(s_);
     }
 }
+
 
 template <class T> void StateVector<T>::synchronize() const {
     cuda_check(cudaStreamSynchronize(s_), "stream synchronize");

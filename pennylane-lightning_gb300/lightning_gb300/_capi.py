@@ -73,6 +73,7 @@ SIGNATURES = {
     "plgb_ops_destroy": (C.c_int, [VP]),
     "plgb_ops_num_par_ops": (C.c_int, [VP, IP]),
     "plgb_sv_apply_operations": (C.c_int, [VP, VP, C.c_int, IP]),
+    "plgb_ops_fusion_plan": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_char_p, C.c_size_t]),
     "plgb_adjoint_jacobian": (C.c_int, [VP, C.POINTER(VP), C.c_int, VP, I64P, C.c_int, C.c_int, DP]),
 }
 

@@ -612,6 +612,13 @@ class _OpsStructBase:
                 pass
             self._h = None
 
+    def fusion_plan(self, num_qubits: int, tile_bits: int) -> list:
+        """The tile passes applyOperations(tile_bits) would run (no GPU needed)."""
+        prec = 64 if isinstance(self, OpsStructC64) else 128
+        buf = C.create_string_buffer(1 << 22)
+        call("plgb_ops_fusion_plan", self._h, int(num_qubits), prec, int(tile_bits), buf, len(buf))
+        return json.loads(buf.value.decode())
+
     def num_par_ops(self) -> int:
         k = C.c_int()
         call("plgb_ops_num_par_ops", self._h, C.byref(k))

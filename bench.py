@@ -173,7 +173,7 @@ def gpu_arm(args) -> dict | None:
     sv = ops.StateVectorC128(n)
     stream = torch.cuda.ExternalStream(sv.cuda_stream())
     # warm-up doubles as the tile-size choice: unfused (0) vs fused tiles of 2^t
-    candidates = [0, 11, 12, 13]
+    candidates = [0, 10, 11, 12]
     tune = {}
     for w in range(max(args.warmup, 1)):
         tb = candidates[w % len(candidates)] if w < len(candidates) else best_tb
@@ -208,8 +208,12 @@ def gpu_arm(args) -> dict | None:
     pass_bytes = 2.0 * (1 << n) * 16
     avg_launch_s = (total_s / args.steps) / passes
     achieved = pass_bytes / avg_launch_s / 1e9
-    kernel = "k_tile_pass<double> (fused tile pass)" if best_tb else "k_1q<double, DENSE> and k_1q<double, NEG1>"
-    tag = "k_tile_pass_c128" if best_tb else "k_1q_dense_c128"
+    if best_tb >= 9:
+        kernel, tag = "k_tile_reg<double> (register-blocked fused tile pass)", "k_tile_reg_c128"
+    elif best_tb:
+        kernel, tag = "k_tile_pass<double> (fused tile pass)", "k_tile_pass_c128"
+    else:
+        kernel, tag = "k_1q<double, DENSE> and k_1q<double, NEG1>", "k_1q_dense_c128"
     traffic = traffic_from_profiles(tag)
 
     # expectation value of the 64-term Hamiltonian (one read per flip-mask group)
@@ -271,7 +275,7 @@ def gpu_arm(args) -> dict | None:
         sv64 = ops.StateVectorC64(n)
         s64 = torch.cuda.ExternalStream(sv64.cuda_stream())
         t64 = {}
-        for tb in (0, 12, 13):
+        for tb in (0, 11, 12):
             timed_step(sv64, S64, s64, tb)
             t64[tb] = timed_step(sv64, S64, s64, tb)[0]
         b64 = min(t64, key=t64.get)

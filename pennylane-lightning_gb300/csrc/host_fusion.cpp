@@ -348,7 +348,10 @@ template <class T>
 std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>> &in, int tile_bits, bool upload) {
     auto prog = std::make_shared<FusedProgram<T>>();
     prog->n = n;
-    const int tmax = std::max(1, std::min({tile_bits, n, kMaxTileBits}));
+    // a tile of 2^t amplitudes must fit the 200 KiB of shared memory the tile
+    // kernel requests: t <= 13 for complex128, t <= 14 for complex64
+    const int tsmem = sizeof(T) == 8 ? 13 : 14;
+    const int tmax = std::max(1, std::min({tile_bits, n, kMaxTileBits, tsmem}));
     const int Lbase = sizeof(T) == 8 ? 4 : 5;
     const int L = std::min(Lbase, tmax);
     const u64 lowmask = (u64{1} << L) - 1;

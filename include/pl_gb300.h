@@ -188,6 +188,17 @@ int plgb_ops_fusion_plan(const plgb_ops *ops, int num_qubits, int precision, int
 int plgb_adjoint_jacobian(plgb_sv *sv, plgb_obs *const *obs, int nobs, const plgb_ops *ops, const int64_t *trainable,
                           int ntp, int apply_ops, double *jac_out);
 
+/* expval(matrix, wires) for at most 5 wires without any device allocation.
+ * No counterpart in the reference: plgb_meas_expval_matrix may grow device
+ * scratch with cudaMalloc (after a cudaFree, which waits for the device);
+ * this variant uses one fixed device array per device instead, for callers
+ * that have filled the device up to a memory budget.  Same result as
+ * plgb_meas_expval_matrix.  nw > 5 returns PLGB_ERR_INVALID.  The first call
+ * on a device resolves the array's address (make it before any stream
+ * capture).  Overlapping calls on one device race on the shared array:
+ * serialise them. */
+int plgb_meas_expval_matrix_noalloc(plgb_sv *sv, const double *matrix, const int64_t *wires, int nw, double *out);
+
 #ifdef __cplusplus
 }
 #endif

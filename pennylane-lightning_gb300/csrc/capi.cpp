@@ -374,6 +374,18 @@ int plgb_meas_expval_matrix(plgb_sv *sv, const double *matrix, const int64_t *wi
         *out = Measure<T>::expval_matrix(s, m.data(), vec(wires, nw));
     });
 }
+int plgb_meas_expval_matrix_noalloc(plgb_sv *sv, const double *matrix, const int64_t *wires, int nw, double *out) {
+    // no host containers on the success path: the matrix and wires are read
+    // in place (noalloc.cu)
+    return with_sv(sv, [&](auto &s) {
+        need(out, "out");
+        need(matrix, "matrix");
+        if (nw > 0) {
+            need(wires, "wires");
+        }
+        *out = expval_matrix_noalloc(s, matrix, wires, nw);
+    });
+}
 int plgb_meas_expval_sparse(plgb_sv *sv, const int64_t *indptr, int64_t nptr, const int64_t *indices,
                             const double *data, int64_t nnz, double *out) {
     return with_sv(sv, [&](auto &s) {

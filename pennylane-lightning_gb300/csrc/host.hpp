@@ -211,6 +211,11 @@ template <class T> FusedStats fused_stats(const FusedProgram<T> &prog);
 // ---------------------------------------------------------------------------
 // Measurements (MeasurementsLQubit.hpp) and sampling.
 // ---------------------------------------------------------------------------
+// expval(matrix, wires), at most 5 wires, with fixed device scratch and no
+// allocation (noalloc.cu).
+template <class T>
+double expval_matrix_noalloc(StateVector<T> &sv, const double *matrix, const int64_t *wires, int nw);
+
 template <class T> struct Measure {
     static std::vector<double> probs(StateVector<T> &sv, const std::vector<int64_t> &wires, bool all_wires);
     static double expval_named(StateVector<T> &sv, const std::string &name, const std::vector<int64_t> &wires);

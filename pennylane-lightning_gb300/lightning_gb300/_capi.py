@@ -53,6 +53,7 @@ SIGNATURES = {
     "plgb_meas_probs": (C.c_int, [VP, I64P, C.c_int, DP]),
     "plgb_meas_expval_named": (C.c_int, [VP, C.c_char_p, I64P, C.c_int, DP]),
     "plgb_meas_expval_matrix": (C.c_int, [VP, DP, I64P, C.c_int, DP]),
+    "plgb_meas_expval_matrix_noalloc": (C.c_int, [VP, DP, I64P, C.c_int, DP]),
     "plgb_meas_expval_sparse": (C.c_int, [VP, I64P, C.c_int64, I64P, DP, C.c_int64, DP]),
     "plgb_meas_expval_obs": (C.c_int, [VP, VP, DP]),
     "plgb_meas_var_obs": (C.c_int, [VP, VP, DP]),

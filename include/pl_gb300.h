@@ -188,6 +188,39 @@ int plgb_ops_fusion_plan(const plgb_ops *ops, int num_qubits, int precision, int
 int plgb_adjoint_jacobian(plgb_sv *sv, plgb_obs *const *obs, int nobs, const plgb_ops *ops, const int64_t *trainable,
                           int ntp, int apply_ops, double *jac_out);
 
+/* ---- batch engine (no counterpart in the reference: lightning.qubit runs
+ *      circuits one at a time, one Python -> C++ call per gate,
+ *      pennylane_lightning/lightning_qubit/_state_vector.py:220-299) ----
+ * Many independent circuits, each from |0...0> on its own register, run
+ * together: pass k of every circuit's fused program is one persistent launch
+ * over all their tiles; Pauli-sum expectation values are reduced in one
+ * batched launch.  A circuit's results do not depend on what else is in the
+ * batch (bit-identical). */
+typedef struct plgb_batch plgb_batch;
+int plgb_batch_create(int precision, plgb_batch **out);
+int plgb_batch_destroy(plgb_batch *b);
+/* tile_bits 0 = autotuned per register size (measured once per size);
+ * wave_bytes 0 = 8 GiB of registers per wave; threads 0 = all host cores */
+int plgb_batch_configure(plgb_batch *b, int tile_bits, int64_t wave_bytes, int threads);
+/* Circuits in packed arrays: circuit c has num_qubits[c] wires and ops
+ * [op_offsets[c], op_offsets[c+1]); op o is gate plgb_gate_name(op_codes[o])
+ * on wires op_wires[4o..4o+3] (-1 = unused), parameters op_params[3o..3o+2]
+ * (unused ones ignored), adjoint if op_inverse[o] (op_inverse may be NULL).
+ * Circuit c's observables are [obs_offsets[c], obs_offsets[c+1]); observable
+ * k is sum over terms [term_offsets[k], term_offsets[k+1]) of
+ * term_coeffs[t] * (X on wires term_x[t]) (Y on term_y[t]) (Z on term_z[t]),
+ * the masks holding bit w for wire w.  out receives one value per
+ * observable. */
+int plgb_batch_run(plgb_batch *b, int ncirc, const int32_t *num_qubits, const int64_t *op_offsets,
+                   const int32_t *op_codes, const int32_t *op_wires, const double *op_params, const uint8_t *op_inverse,
+                   const int64_t *obs_offsets, const int64_t *term_offsets, const double *term_coeffs,
+                   const uint64_t *term_x, const uint64_t *term_y, const uint64_t *term_z, double *out);
+/* JSON of the last run: waves, launches, tile sizes, compile and device ms,
+ * completion time of each wave and the wave of each circuit */
+int plgb_batch_stats(const plgb_batch *b, char *buf, size_t len);
+/* gate-name code table of plgb_batch_run: name of code, NULL past the end */
+const char *plgb_gate_name(int code);
+
 /* expval(matrix, wires) for at most 5 wires without any device allocation.
  * No counterpart in the reference: plgb_meas_expval_matrix may grow device
  * scratch with cudaMalloc (after a cudaFree, which waits for the device);

@@ -1,0 +1,533 @@
+// Batch engine host side (batch.hpp).
+//
+// run(): circuits are lowered and compiled into fused tile passes on a pool
+// of host threads, then executed in waves that fit a device-memory budget.
+// Within a wave all registers sit in one device arena and all compiled
+// programs in another (one host->device copy each); pass k of every circuit
+// runs as one persistent launch per tile size, the expectation values as one
+// batched reduction; one device->host copy returns the sums.
+#include "batch.hpp"
+#include "fusion.hpp"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cstring>
+#include <thread>
+
+namespace plgb {
+
+namespace {
+
+constexpr int kBatchMinQubits = kMinRegTileBits; // smaller registers run padded
+constexpr int kBatchMaxQubits = 30;
+constexpr int kMaxWiresPerOp = 4;
+
+double ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+template <class T> struct Compiled {
+    int n{0};     // register size as given
+    int ne{0};    // register size run (>= 9)
+    int t{0};     // tile bits
+    bool fast{false}; // every segment is a register-kernel tile pass of size t
+    std::shared_ptr<FusedProgram<T>> prog;
+    std::vector<std::vector<PauliGroup>> obs_groups; // per observable
+    std::string error;
+};
+
+// a small config-0-like circuit used to time tile sizes for one register size
+template <class T> std::vector<Prim<T>> tuning_circuit(int n) {
+    StateVector<T> reg(n, LowerOnly{});
+    std::vector<Prim<T>> prims;
+    for (int layer = 0; layer < 4; layer++) {
+        for (int q = 0; q < n; q++) {
+            for (const char *g : {"RX", "RY", "RZ"}) {
+                OpRec r;
+                r.name = g;
+                r.wires = {q};
+                r.params = {0.1 + 0.01 * (q + 7 * layer)};
+                auto p = reg.lower_op(r, false);
+                prims.insert(prims.end(), std::make_move_iterator(p.begin()), std::make_move_iterator(p.end()));
+            }
+        }
+        for (int q = 0; q < n; q++) {
+            OpRec r;
+            r.name = "CNOT";
+            r.wires = {q, (q + 1) % n};
+            auto p = reg.lower_op(r, false);
+            prims.insert(prims.end(), std::make_move_iterator(p.begin()), std::make_move_iterator(p.end()));
+        }
+    }
+    return prims;
+}
+
+} // namespace
+
+template <class T> BatchEngine<T>::BatchEngine() {
+    cuda_check(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking), "cudaStreamCreate");
+    cuda_check(cudaEventCreate(&ev0_), "cudaEventCreate");
+    cuda_check(cudaEventCreate(&ev1_), "cudaEventCreate");
+}
+
+template <class T> BatchEngine<T>::~BatchEngine() {
+    if (s_) {
+        cudaStreamSynchronize(s_);
+    }
+    for (void *p : {d_states_, d_prog_, d_items_, d_red_}) {
+        if (p) {
+            cudaFree(p);
+        }
+    }
+    for (void *p : {h_prog_, h_items_, h_out_}) {
+        if (p) {
+            cudaFreeHost(p);
+        }
+    }
+    if (ev0_) {
+        cudaEventDestroy(ev0_);
+    }
+    if (ev1_) {
+        cudaEventDestroy(ev1_);
+    }
+    if (s_) {
+        cudaStreamDestroy(s_);
+    }
+}
+
+template <class T> void *BatchEngine<T>::grow(void *&buf, size_t &cap, size_t need, bool pinned) {
+    if (need <= cap && buf) {
+        return buf;
+    }
+    cuda_check(cudaStreamSynchronize(s_), "cudaStreamSynchronize");
+    if (buf) {
+        pinned ? cudaFreeHost(buf) : cudaFree(buf);
+        buf = nullptr;
+        cap = 0;
+    }
+    const size_t want = std::max<size_t>(need + need / 4, 1 << 16);
+    if (pinned) {
+        cuda_check(cudaMallocHost(&buf, want), "cudaMallocHost(batch)");
+    } else {
+        cuda_check(cudaMalloc(&buf, want), "cudaMalloc(batch)");
+    }
+    cap = want;
+    return buf;
+}
+
+template <class T> int BatchEngine<T>::tile_bits_for(int n) {
+    if (fixed_tile_bits_ > 0) {
+        return std::max(kMinRegTileBits, std::min({fixed_tile_bits_, n, 12}));
+    }
+    auto it = tuned_.find(n);
+    if (it != tuned_.end()) {
+        return it->second;
+    }
+    // Autotune: time the register kernel on a tuning circuit at every
+    // candidate tile size this register supports; keep the fastest.
+    // (timed on at most 20 qubits: the choice depends on the tile, not on
+    // how many tiles there are)
+    const int tmin = kMinRegTileBits, tmax = std::min(n, 12);
+    int best = tmax;
+    if (tmin < tmax) {
+        const int nt = std::min(n, 20);
+        const auto prims = tuning_circuit<T>(nt);
+        StateVector<T> sv(nt);
+        float best_ms = 1e30f;
+        for (int t = tmin; t <= tmax; t++) {
+            auto prog = compile_fused<T>(nt, prims, t, true);
+            run_fused<T>(sv, *prog); // warm
+            cuda_check(cudaEventRecord(ev0_, sv.stream()), "event");
+            run_fused<T>(sv, *prog);
+            run_fused<T>(sv, *prog);
+            cuda_check(cudaEventRecord(ev1_, sv.stream()), "event");
+            cuda_check(cudaEventSynchronize(ev1_), "event sync");
+            float ms = 0;
+            cuda_check(cudaEventElapsedTime(&ms, ev0_, ev1_), "event time");
+            if (ms < best_ms * 0.97f) { // prefer the smaller tile unless clearly slower
+                best_ms = ms;
+                best = t;
+            }
+        }
+    }
+    tuned_[n] = best;
+    return best;
+}
+
+template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
+    std::lock_guard<std::mutex> lk(mu_);
+    const auto t_start = std::chrono::steady_clock::now();
+    stats_ = BatchStats{};
+    const int nc = in.ncirc;
+    stats_.ncirc = nc;
+    PLGB_REQUIRE(nc >= 0, "number of circuits must be non-negative");
+    if (nc == 0) {
+        return;
+    }
+    PLGB_REQUIRE(in.num_qubits && in.op_offsets && in.obs_offsets, "batch: missing circuit arrays");
+    const int64_t nops_total = in.op_offsets[nc];
+    PLGB_REQUIRE(in.op_offsets[0] == 0 && nops_total >= 0, "batch: op offsets must start at 0");
+    PLGB_REQUIRE(nops_total == 0 || (in.op_codes && in.op_wires && in.op_params), "batch: missing op arrays");
+    const int64_t nobs_total = in.obs_offsets[nc];
+    PLGB_REQUIRE(in.obs_offsets[0] == 0 && nobs_total >= 0, "batch: observable offsets must start at 0");
+    PLGB_REQUIRE(nobs_total == 0 || in.term_offsets, "batch: missing term offsets");
+    const int64_t nterms_total = nobs_total ? in.term_offsets[nobs_total] : 0;
+    PLGB_REQUIRE(nterms_total == 0 || (in.term_coeffs && in.term_x && in.term_y && in.term_z),
+                 "batch: missing term arrays");
+    for (int c = 0; c < nc; c++) {
+        const int n = in.num_qubits[c];
+        PLGB_REQUIRE(n >= 1 && n <= kBatchMaxQubits, "batch: number of qubits must be in 1..30");
+        PLGB_REQUIRE(in.op_offsets[c + 1] >= in.op_offsets[c], "batch: op offsets must not decrease");
+        PLGB_REQUIRE(in.obs_offsets[c + 1] >= in.obs_offsets[c], "batch: observable offsets must not decrease");
+    }
+
+    // tile sizes first (autotuning runs on the device, one register size at a time)
+    std::map<int, int> tsel;
+    for (int c = 0; c < nc; c++) {
+        const int ne = std::max(in.num_qubits[c], kBatchMinQubits);
+        if (!tsel.count(ne)) {
+            tsel[ne] = tile_bits_for(ne);
+        }
+    }
+    stats_.tile_bits = tsel;
+
+    // ---- lower + compile on a pool of host threads
+    const auto t_comp = std::chrono::steady_clock::now();
+    std::vector<Compiled<T>> comp(static_cast<size_t>(nc));
+    std::atomic<int> next{0};
+    auto worker = [&]() {
+        for (int c = next++; c < nc; c = next++) {
+            Compiled<T> &cc = comp[static_cast<size_t>(c)];
+            try {
+                cc.n = in.num_qubits[c];
+                cc.ne = std::max(cc.n, kBatchMinQubits);
+                cc.t = tsel.at(cc.ne);
+                StateVector<T> reg(cc.ne, LowerOnly{});
+                std::vector<Prim<T>> prims;
+                OpRec rec;
+                for (int64_t o = in.op_offsets[c]; o < in.op_offsets[c + 1]; o++) {
+                    const char *name = gate_name_of(in.op_codes[o]);
+                    PLGB_REQUIRE(name != nullptr, "batch: unknown gate code");
+                    rec.name = name;
+                    rec.wires.clear();
+                    for (int k = 0; k < kMaxWiresPerOp; k++) {
+                        const int w = in.op_wires[kMaxWiresPerOp * o + k];
+                        if (w >= 0) {
+                            PLGB_REQUIRE(w < cc.n, "batch: wire index out of range");
+                            rec.wires.push_back(w);
+                        }
+                    }
+                    rec.params.assign(in.op_params + 3 * o, in.op_params + 3 * o + 3);
+                    rec.inverse = in.op_inverse ? in.op_inverse[o] != 0 : false;
+                    auto p = reg.lower_op(rec, rec.inverse);
+                    prims.insert(prims.end(), std::make_move_iterator(p.begin()), std::make_move_iterator(p.end()));
+                }
+                cc.prog = compile_fused<T>(cc.ne, prims, cc.t, false);
+                cc.fast = true;
+                for (const auto &seg : cc.prog->segs) {
+                    if (!seg.tile || !seg.reg || seg.desc.t != cc.t) {
+                        cc.fast = false;
+                    }
+                }
+                if (!cc.fast) { // runs on its own, with its program in device memory
+                    cc.prog = compile_fused<T>(cc.ne, prims, cc.t, true);
+                }
+                for (int64_t ob = in.obs_offsets[c]; ob < in.obs_offsets[c + 1]; ob++) {
+                    PauliSum ps;
+                    for (int64_t tm = in.term_offsets[ob]; tm < in.term_offsets[ob + 1]; tm++) {
+                        const u64 X = in.term_x[tm], Y = in.term_y[tm], Z = in.term_z[tm];
+                        PLGB_REQUIRE(((X & Y) | (X & Z) | (Y & Z)) == 0, "batch: a wire has two Pauli letters");
+                        PLGB_REQUIRE(cc.n >= 64 || ((X | Y | Z) >> cc.n) == 0, "batch: term wire out of range");
+                        PauliSum::Term t{in.term_coeffs[tm], 0, 0, 0};
+                        for (u64 r = X | Y | Z; r; r &= r - 1) {
+                            const int w = __builtin_ctzll(r);
+                            const u64 b = u64{1} << (cc.ne - 1 - w);
+                            if ((X >> w) & 1U) {
+                                t.x |= b;
+                            } else if ((Y >> w) & 1U) {
+                                t.x |= b;
+                                t.yz |= b;
+                                t.ny4 = (t.ny4 + 1) & 3;
+                            } else {
+                                t.yz |= b;
+                            }
+                        }
+                        ps.terms.push_back(t);
+                    }
+                    cc.obs_groups.push_back(group_pauli(ps));
+                }
+            } catch (const std::exception &e) {
+                cc.error = e.what();
+            }
+        }
+    };
+    {
+        int nt = threads_ > 0 ? threads_ : static_cast<int>(std::thread::hardware_concurrency());
+        nt = std::max(1, std::min({nt, 64, nc}));
+        std::vector<std::thread> pool;
+        for (int i = 1; i < nt; i++) {
+            pool.emplace_back(worker);
+        }
+        worker();
+        for (auto &th : pool) {
+            th.join();
+        }
+    }
+    for (auto &cc : comp) {
+        if (!cc.error.empty()) {
+            throw PLError(cc.error);
+        }
+    }
+    stats_.compile_ms = ms_since(t_comp);
+
+    // ---- waves
+    stats_.wave_of.assign(static_cast<size_t>(nc), 0);
+    float dev_ms_total = 0;
+    int c0 = 0;
+    while (c0 < nc) {
+        // registers of this wave
+        int c1 = c0;
+        size_t sv_bytes = 0;
+        std::vector<size_t> sv_off;
+        while (c1 < nc) {
+            const size_t b = align_up(sizeof(cx<T>) << comp[static_cast<size_t>(c1)].ne);
+            if (c1 > c0 && sv_bytes + b > wave_bytes_) {
+                break;
+            }
+            sv_off.push_back(sv_bytes);
+            sv_bytes += b;
+            c1++;
+        }
+        const int wn = c1 - c0;
+        for (int c = c0; c < c1; c++) {
+            stats_.wave_of[static_cast<size_t>(c)] = stats_.waves;
+        }
+        grow(d_states_, c_states_, sv_bytes, false);
+        char *states = static_cast<char *>(d_states_);
+
+        // programs: one arena, 256-byte aligned blocks per circuit
+        struct ProgOff {
+            size_t ops, forms, tables, stages;
+        };
+        std::vector<ProgOff> po(static_cast<size_t>(wn));
+        size_t pbytes = 0;
+        for (int i = 0; i < wn; i++) {
+            const auto &pr = *comp[static_cast<size_t>(c0 + i)].prog;
+            po[static_cast<size_t>(i)].ops = pbytes;
+            pbytes += align_up(pr.h_ops.size() * sizeof(TileOp<T>));
+            po[static_cast<size_t>(i)].forms = pbytes;
+            pbytes += align_up(pr.h_forms.size() * sizeof(DiagForm<T>));
+            po[static_cast<size_t>(i)].tables = pbytes;
+            pbytes += align_up(pr.h_tables.size() * sizeof(cx<T>));
+            po[static_cast<size_t>(i)].stages = pbytes;
+            pbytes += align_up(pr.h_stages.size() * sizeof(StageDesc));
+        }
+        pbytes = std::max<size_t>(pbytes, 256);
+        grow(h_prog_, ch_prog_, pbytes, true);
+        grow(d_prog_, c_prog_, pbytes, false);
+        char *hp = static_cast<char *>(h_prog_);
+        for (int i = 0; i < wn; i++) {
+            const auto &pr = *comp[static_cast<size_t>(c0 + i)].prog;
+            const auto &o = po[static_cast<size_t>(i)];
+            std::memcpy(hp + o.ops, pr.h_ops.data(), pr.h_ops.size() * sizeof(TileOp<T>));
+            std::memcpy(hp + o.forms, pr.h_forms.data(), pr.h_forms.size() * sizeof(DiagForm<T>));
+            std::memcpy(hp + o.tables, pr.h_tables.data(), pr.h_tables.size() * sizeof(cx<T>));
+            std::memcpy(hp + o.stages, pr.h_stages.data(), pr.h_stages.size() * sizeof(StageDesc));
+        }
+        char *dp = static_cast<char *>(d_prog_);
+
+        // launch plan: pass k of every fast circuit, grouped by tile size
+        struct Launch {
+            int t;
+            size_t item0;
+            int nitems;
+            u64 tiles;
+        };
+        std::vector<BatchTileItem<T>> titems;
+        std::vector<Launch> launches;
+        int maxp = 0;
+        for (int i = 0; i < wn; i++) {
+            const auto &cc = comp[static_cast<size_t>(c0 + i)];
+            if (cc.fast) {
+                maxp = std::max(maxp, static_cast<int>(cc.prog->segs.size()));
+            }
+        }
+        stats_.max_passes = std::max(stats_.max_passes, maxp);
+        for (int k = 0; k < maxp; k++) {
+            std::map<int, std::vector<int>> by_t;
+            for (int i = 0; i < wn; i++) {
+                const auto &cc = comp[static_cast<size_t>(c0 + i)];
+                if (cc.fast && k < static_cast<int>(cc.prog->segs.size())) {
+                    by_t[cc.t].push_back(i);
+                }
+            }
+            for (auto &kv : by_t) {
+                Launch L{kv.first, titems.size(), 0, 0};
+                for (int i : kv.second) {
+                    const auto &cc = comp[static_cast<size_t>(c0 + i)];
+                    const auto &o = po[static_cast<size_t>(i)];
+                    BatchTileItem<T> it{};
+                    it.sv = reinterpret_cast<cx<T> *>(states + sv_off[static_cast<size_t>(i)]);
+                    it.ops = reinterpret_cast<const TileOp<T> *>(dp + o.ops);
+                    it.forms = reinterpret_cast<const DiagForm<T> *>(dp + o.forms);
+                    it.tables = reinterpret_cast<const cx<T> *>(dp + o.tables);
+                    it.stages = reinterpret_cast<const StageDesc *>(dp + o.stages);
+                    it.desc = cc.prog->segs[static_cast<size_t>(k)].desc;
+                    it.tile_begin = L.tiles;
+                    L.tiles += it.desc.ntiles;
+                    titems.push_back(it);
+                    L.nitems++;
+                }
+                launches.push_back(L);
+            }
+        }
+
+        // reductions: one item per (register, observable, flip-mask group)
+        std::vector<PauliGroup> groups;
+        std::vector<BatchRedItem<T>> ritems;
+        std::vector<std::pair<int64_t, size_t>> obs_item; // (observable index, item index)
+        u64 rblocks = 0;
+        for (int i = 0; i < wn; i++) {
+            const auto &cc = comp[static_cast<size_t>(c0 + i)];
+            const int64_t ob0 = in.obs_offsets[c0 + i];
+            for (size_t ob = 0; ob < cc.obs_groups.size(); ob++) {
+                for (const auto &g : cc.obs_groups[ob]) {
+                    BatchRedItem<T> r{};
+                    r.sv = reinterpret_cast<const cx<T> *>(states + sv_off[static_cast<size_t>(i)]);
+                    r.group = reinterpret_cast<const PauliGroup *>(groups.size()); // index, fixed below
+                    const u64 N = u64{1} << cc.ne;
+                    r.work = g.x == 0 ? N : N >> 1;
+                    r.block_begin = rblocks;
+                    rblocks += (r.work + kBatchRedChunk - 1) / kBatchRedChunk;
+                    obs_item.emplace_back(ob0 + static_cast<int64_t>(ob), ritems.size());
+                    ritems.push_back(r);
+                    groups.push_back(g);
+                }
+            }
+        }
+
+        // one staging block: [tile items][set-one pointers][red items][groups]
+        const size_t b_titems = align_up(std::max<size_t>(1, titems.size()) * sizeof(BatchTileItem<T>));
+        const size_t b_ptrs = align_up(static_cast<size_t>(wn) * sizeof(cx<T> *));
+        const size_t b_ritems = align_up(std::max<size_t>(1, ritems.size()) * sizeof(BatchRedItem<T>));
+        const size_t b_groups = align_up(std::max<size_t>(1, groups.size()) * sizeof(PauliGroup));
+        const size_t ibytes = b_titems + b_ptrs + b_ritems + b_groups;
+        grow(h_items_, ch_items_, ibytes, true);
+        grow(d_items_, c_items_, ibytes, false);
+        char *hi = static_cast<char *>(h_items_);
+        char *di = static_cast<char *>(d_items_);
+        auto *d_titems = reinterpret_cast<BatchTileItem<T> *>(di);
+        auto *d_ptrs = reinterpret_cast<cx<T> **>(di + b_titems);
+        auto *d_ritems = reinterpret_cast<BatchRedItem<T> *>(di + b_titems + b_ptrs);
+        auto *d_groups = reinterpret_cast<PauliGroup *>(di + b_titems + b_ptrs + b_ritems);
+        for (auto &r : ritems) {
+            r.group = d_groups + reinterpret_cast<size_t>(r.group);
+        }
+        std::memcpy(hi, titems.data(), titems.size() * sizeof(BatchTileItem<T>));
+        auto *h_ptrs = reinterpret_cast<cx<T> **>(hi + b_titems);
+        for (int i = 0; i < wn; i++) {
+            h_ptrs[i] = reinterpret_cast<cx<T> *>(states + sv_off[static_cast<size_t>(i)]);
+        }
+        std::memcpy(hi + b_titems + b_ptrs, ritems.data(), ritems.size() * sizeof(BatchRedItem<T>));
+        std::memcpy(hi + b_titems + b_ptrs + b_ritems, groups.data(), groups.size() * sizeof(PauliGroup));
+
+        const size_t nred = std::max<size_t>(1, ritems.size());
+        grow(d_red_, c_red_, (rblocks + nred) * sizeof(double), false);
+        grow(h_out_, ch_out_, nred * sizeof(double), true);
+        double *partials = static_cast<double *>(d_red_);
+        double *item_sums = partials + rblocks;
+
+        // ---- device work of the wave
+        cuda_check(cudaEventRecord(ev0_, s_), "event");
+        cuda_check(cudaMemcpyAsync(dp, hp, pbytes, cudaMemcpyHostToDevice, s_), "H2D programs");
+        cuda_check(cudaMemcpyAsync(di, hi, ibytes, cudaMemcpyHostToDevice, s_), "H2D items");
+        cuda_check(cudaMemsetAsync(states, 0, sv_bytes, s_), "memset registers");
+        launch_batch_set_one<T>(s_, d_ptrs, wn);
+        stats_.launches += 1;
+        for (const auto &L : launches) {
+            launch_tile_reg_batch<T>(s_, L.t, d_titems + L.item0, L.nitems, L.tiles);
+            stats_.launches++;
+        }
+        // circuits the batched kernel cannot take run pass by pass on their own
+        for (int i = 0; i < wn; i++) {
+            auto &cc = comp[static_cast<size_t>(c0 + i)];
+            if (cc.fast) {
+                continue;
+            }
+            stats_.fallback++;
+            StateVector<T> view(reinterpret_cast<cx<T> *>(states + sv_off[static_cast<size_t>(i)]), cc.ne, s_);
+            const auto l0 = launch_count();
+            run_fused<T>(view, *cc.prog);
+            stats_.launches += static_cast<int>(launch_count() - l0);
+        }
+        if (!ritems.empty()) {
+            launch_pauli_batch<T>(s_, d_ritems, static_cast<int>(ritems.size()), rblocks, partials, item_sums);
+            stats_.launches += 2;
+            cuda_check(cudaMemcpyAsync(h_out_, item_sums, ritems.size() * sizeof(double), cudaMemcpyDeviceToHost, s_),
+                       "D2H sums");
+        }
+        cuda_check(cudaEventRecord(ev1_, s_), "event");
+        cuda_check(cudaEventSynchronize(ev1_), "wave sync");
+        float wms = 0;
+        cuda_check(cudaEventElapsedTime(&wms, ev0_, ev1_), "event time");
+        dev_ms_total += wms;
+        stats_.wave_done_ms.push_back(ms_since(t_start));
+
+        // observable sums in a fixed order
+        const double *sums = static_cast<const double *>(h_out_);
+        int64_t ob_last = -1;
+        for (const auto &oi : obs_item) {
+            if (oi.first != ob_last) {
+                out[oi.first] = 0.0;
+                ob_last = oi.first;
+            }
+            out[oi.first] += sums[oi.second];
+        }
+        // observables without terms
+        for (int i = 0; i < wn; i++) {
+            for (int64_t ob = in.obs_offsets[c0 + i]; ob < in.obs_offsets[c0 + i + 1]; ob++) {
+                if (in.term_offsets[ob + 1] == in.term_offsets[ob]) {
+                    out[ob] = 0.0;
+                }
+            }
+        }
+        stats_.waves++;
+        c0 = c1;
+    }
+    for (const auto &cc : comp) {
+        stats_.padded += cc.ne != cc.n ? 1 : 0;
+    }
+    stats_.device_ms = dev_ms_total;
+    stats_.total_ms = ms_since(t_start);
+}
+
+template <class T> std::string BatchEngine<T>::stats_json() const {
+    std::string js = "{\"circuits\": " + std::to_string(stats_.ncirc) + ", \"waves\": " + std::to_string(stats_.waves) +
+                     ", \"launches\": " + std::to_string(stats_.launches) +
+                     ", \"max_passes\": " + std::to_string(stats_.max_passes) +
+                     ", \"padded\": " + std::to_string(stats_.padded) +
+                     ", \"fallback\": " + std::to_string(stats_.fallback) +
+                     ", \"compile_ms\": " + std::to_string(stats_.compile_ms) +
+                     ", \"device_ms\": " + std::to_string(stats_.device_ms) +
+                     ", \"total_ms\": " + std::to_string(stats_.total_ms) + ", \"tile_bits\": {";
+    bool first = true;
+    for (const auto &kv : stats_.tile_bits) {
+        js += (first ? "\"" : ", \"") + std::to_string(kv.first) + "\": " + std::to_string(kv.second);
+        first = false;
+    }
+    js += "}, \"wave_done_ms\": [";
+    for (size_t i = 0; i < stats_.wave_done_ms.size(); i++) {
+        js += (i ? ", " : "") + std::to_string(stats_.wave_done_ms[i]);
+    }
+    js += "], \"wave_of\": [";
+    for (size_t i = 0; i < stats_.wave_of.size(); i++) {
+        js += (i ? ", " : "") + std::to_string(stats_.wave_of[i]);
+    }
+    return js + "]}";
+}
+
+template class BatchEngine<float>;
+template class BatchEngine<double>;
+
+} // namespace plgb

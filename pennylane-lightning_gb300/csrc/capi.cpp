@@ -1,6 +1,7 @@
 // extern "C" boundary (include/pl_gb300.h) over the C++ host layer.
 #include "pl_gb300.h"
 
+#include "batch.hpp"
 #include "host.hpp"
 
 #include <algorithm>
@@ -20,6 +21,11 @@ struct plgb_sv {
 };
 struct plgb_obs {
     ObsPtr node;
+};
+struct plgb_batch {
+    int precision;
+    std::unique_ptr<BatchEngine<float>> f;
+    std::unique_ptr<BatchEngine<double>> d;
 };
 struct plgb_ops {
     OpsList list;
@@ -374,6 +380,76 @@ int plgb_meas_expval_matrix(plgb_sv *sv, const double *matrix, const int64_t *wi
         *out = Measure<T>::expval_matrix(s, m.data(), vec(wires, nw));
     });
 }
+int plgb_batch_create(int precision, plgb_batch **out) {
+    return guard([&] {
+        need(out, "out");
+        PLGB_REQUIRE(precision == 64 || precision == 128, "precision must be 64 or 128");
+        auto b = std::make_unique<plgb_batch>();
+        b->precision = precision;
+        if (precision == 128) {
+            b->d = std::make_unique<BatchEngine<double>>();
+        } else {
+            b->f = std::make_unique<BatchEngine<float>>();
+        }
+        *out = b.release();
+    });
+}
+int plgb_batch_destroy(plgb_batch *b) {
+    delete b;
+    return PLGB_OK;
+}
+int plgb_batch_configure(plgb_batch *b, int tile_bits, int64_t wave_bytes, int threads) {
+    return guard([&] {
+        need(b, "batch");
+        PLGB_REQUIRE(tile_bits == 0 || (tile_bits >= 9 && tile_bits <= 12), "tile_bits must be 0 or in 9..12");
+        PLGB_REQUIRE(wave_bytes >= 0 && threads >= 0, "wave_bytes and threads must be non-negative");
+        auto cfg = [&](auto &e) {
+            e.set_tile_bits(tile_bits);
+            e.set_wave_bytes(wave_bytes > 0 ? static_cast<size_t>(wave_bytes) : size_t{8} << 30);
+            e.set_threads(threads);
+        };
+        b->precision == 128 ? cfg(*b->d) : cfg(*b->f);
+    });
+}
+int plgb_batch_run(plgb_batch *b, int ncirc, const int32_t *num_qubits, const int64_t *op_offsets,
+                   const int32_t *op_codes, const int32_t *op_wires, const double *op_params, const uint8_t *op_inverse,
+                   const int64_t *obs_offsets, const int64_t *term_offsets, const double *term_coeffs,
+                   const uint64_t *term_x, const uint64_t *term_y, const uint64_t *term_z, double *out) {
+    return guard([&] {
+        need(b, "batch");
+        BatchInput in;
+        in.ncirc = ncirc;
+        in.num_qubits = num_qubits;
+        in.op_offsets = op_offsets;
+        in.op_codes = op_codes;
+        in.op_wires = op_wires;
+        in.op_params = op_params;
+        in.op_inverse = op_inverse;
+        in.obs_offsets = obs_offsets;
+        in.term_offsets = term_offsets;
+        in.term_coeffs = term_coeffs;
+        in.term_x = term_x;
+        in.term_y = term_y;
+        in.term_z = term_z;
+        if (ncirc > 0) {
+            need(obs_offsets, "obs_offsets");
+            if (obs_offsets[ncirc] > 0) {
+                need(out, "out");
+            }
+        }
+        b->precision == 128 ? b->d->run(in, out) : b->f->run(in, out);
+    });
+}
+int plgb_batch_stats(const plgb_batch *b, char *buf, size_t len) {
+    std::string js;
+    const int rc = guard([&] {
+        need(b, "batch");
+        js = b->precision == 128 ? b->d->stats_json() : b->f->stats_json();
+    });
+    return rc != PLGB_OK ? rc : copy_text(js, buf, len);
+}
+const char *plgb_gate_name(int code) { return gate_name_of(code); }
+
 int plgb_meas_expval_matrix_noalloc(plgb_sv *sv, const double *matrix, const int64_t *wires, int nw, double *out) {
     // no host containers on the success path: the matrix and wires are read
     // in place (noalloc.cu)

@@ -1,0 +1,43 @@
+// The compiled form of a fused primitive list (host_fusion.cpp), shared by
+// the single-register path and the batch engine (batch.cpp).
+#pragma once
+
+#include "fused.hpp"
+#include "host.hpp"
+
+namespace plgb {
+
+template <class T> struct FusedProgram {
+    struct Seg {
+        bool tile{false};
+        bool reg{false}; // register-blocked kernel
+        TilePassDesc desc{};
+        Prim<T> prim; // unfused segment
+    };
+    std::vector<Seg> segs;
+    // device copies (compile_fused with upload)
+    void *dev{nullptr};
+    TileOp<T> *d_ops{nullptr};
+    DiagForm<T> *d_forms{nullptr};
+    cx<T> *d_tables{nullptr};
+    StageDesc *d_stages{nullptr};
+    // host copies (compile_fused without upload); indices in the segments'
+    // descriptors are relative to these arrays
+    std::vector<TileOp<T>> h_ops;
+    std::vector<DiagForm<T>> h_forms;
+    std::vector<cx<T>> h_tables;
+    std::vector<StageDesc> h_stages;
+    int n{0};
+    size_t passes{0}, unfused{0}, prims{0};
+    std::string plan; // JSON lines of the segments
+    FusedProgram() = default;
+    FusedProgram(const FusedProgram &) = delete;
+    FusedProgram &operator=(const FusedProgram &) = delete;
+    ~FusedProgram() {
+        if (dev) {
+            cudaFree(dev);
+        }
+    }
+};
+
+} // namespace plgb

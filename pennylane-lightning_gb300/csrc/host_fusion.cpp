@@ -21,8 +21,7 @@
 // Primitives a tile cannot run (dense blocks on 3+ wires, Pauli rotations,
 // projections, wide diagonals across the tile boundary) run unfused
 // between passes.
-#include "fused.hpp"
-#include "host.hpp"
+#include "fusion.hpp"
 
 #include <algorithm>
 #include <cmath>
@@ -155,30 +154,115 @@ struct PassPlan {
     u64 local{0};
 };
 
-} // namespace
-
-template <class T> struct FusedProgram {
-    struct Seg {
-        bool tile{false};
-        bool reg{false}; // register-blocked kernel
-        TilePassDesc desc{};
-        Prim<T> prim; // unfused segment
-    };
-    std::vector<Seg> segs;
-    void *dev{nullptr};
-    TileOp<T> *d_ops{nullptr};
-    DiagForm<T> *d_forms{nullptr};
-    cx<T> *d_tables{nullptr};
-    StageDesc *d_stages{nullptr};
-    int n{0};
-    size_t passes{0}, unfused{0}, prims{0};
-    std::string plan; // JSON lines of the segments
-    ~FusedProgram() {
-        if (dev) {
-            cudaFree(dev);
+// Order the primitives of one pass as dependency layers (see the comment
+// inside); returns them in execution order with, per position, its level.
+std::vector<size_t> order_by_levels(const std::vector<size_t> &prims, const std::vector<u64> &touch,
+                                    const std::vector<char> &diag, std::vector<int> *levels_out) {
+    // Order the pass as dependency layers.  Non-diagonal ops go to the
+    // first level after everything they depend on.  A diagonal may sit at
+    // any level from its last non-diagonal predecessor up to just before
+    // the next non-diagonal op on its bits; diagonals on two or more
+    // bits also hold later non-diagonal ops on their bits behind them,
+    // which keeps every such range non-empty.  The diagonals are then
+    // packed onto as few levels as possible (interval point cover,
+    // greedy by right end); all diagonals of one level merge into one
+    // op placed after that level's non-diagonal ops.
+    const size_t np = prims.size();
+    std::vector<int> level(np, 0), dlo(np, 0), dhi(np, 0);
+    int maxlv = 0;
+    {
+        int ndl[64] = {0}, floor_lv[64] = {0};
+        for (size_t k = 0; k < np; k++) {
+            const size_t pi = prims[k];
+            const u64 tb = touch[pi];
+            int lv = 0;
+            if (diag[pi]) {
+                for (u64 r = tb; r; r &= r - 1) {
+                    lv = std::max(lv, ndl[__builtin_ctzll(r)]);
+                }
+                dlo[k] = lv;
+                if (__builtin_popcountll(tb) >= 2) {
+                    for (u64 r = tb; r; r &= r - 1) {
+                        const int b = __builtin_ctzll(r);
+                        floor_lv[b] = std::max(floor_lv[b], lv);
+                    }
+                }
+            } else {
+                for (u64 r = tb; r; r &= r - 1) {
+                    const int b = __builtin_ctzll(r);
+                    lv = std::max({lv, ndl[b], floor_lv[b]});
+                }
+                lv += 1;
+                for (u64 r = tb; r; r &= r - 1) {
+                    ndl[__builtin_ctzll(r)] = lv;
+                }
+                level[k] = lv;
+                maxlv = std::max(maxlv, lv);
+            }
+        }
+        int next_lv[64];
+        std::fill(next_lv, next_lv + 64, maxlv + 1);
+        for (size_t k = np; k-- > 0;) {
+            const size_t pi = prims[k];
+            const u64 tb = touch[pi];
+            if (diag[pi]) {
+                int h = maxlv;
+                for (u64 r = tb; r; r &= r - 1) {
+                    h = std::min(h, next_lv[__builtin_ctzll(r)] - 1);
+                }
+                dhi[k] = h;
+            } else {
+                for (u64 r = tb; r; r &= r - 1) {
+                    next_lv[__builtin_ctzll(r)] = level[k];
+                }
+            }
+        }
+        std::vector<size_t> dk;
+        for (size_t k = 0; k < np; k++) {
+            if (diag[prims[k]]) {
+                dk.push_back(k);
+            }
+        }
+        std::stable_sort(dk.begin(), dk.end(), [&](size_t a, size_t b) { return dhi[a] < dhi[b]; });
+        int point = -1;
+        for (size_t k : dk) {
+            if (point < dlo[k]) {
+                point = dhi[k];
+            }
+            level[k] = point;
         }
     }
-};
+    // bucket by (level, non-diagonal first), keeping program order inside
+    std::vector<size_t> ordered;
+    ordered.reserve(np);
+    {
+        std::vector<size_t> cnt(2 * static_cast<size_t>(maxlv + 1) + 1, 0);
+        auto key = [&](size_t k) { return 2 * static_cast<size_t>(level[k]) + (diag[prims[k]] ? 1 : 0); };
+        for (size_t k = 0; k < np; k++) {
+            cnt[key(k) + 1]++;
+        }
+        for (size_t q = 1; q < cnt.size(); q++) {
+            cnt[q] += cnt[q - 1];
+        }
+        ordered.resize(np);
+        for (size_t k = 0; k < np; k++) {
+            ordered[cnt[key(k)]++] = prims[k];
+        }
+    }
+    if (levels_out) {
+        levels_out->clear();
+        std::vector<int> lv_of(touch.size(), 0);
+        for (size_t k = 0; k < np; k++) {
+            lv_of[prims[k]] = level[k];
+        }
+        for (size_t pi : ordered) {
+            levels_out->push_back(lv_of[pi]);
+        }
+    }
+    return ordered;
+}
+
+} // namespace
 
 // Split a pass's op range into register / shared-memory stages for the
 // register-blocked kernel and rewrite the ops' modes for it.  Returns false
@@ -482,6 +566,45 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
         seg_start = seg_end;
     }
 
+    // Split passes whose merged diagonals would outgrow the tile prologue:
+    // a prefix of a pass's level order is itself a valid pass on the same
+    // local bits.
+    {
+        constexpr int kDiagLevelsPerPass = kMaxDiagOpsPerPass - 8; // slack for split form lists
+        std::vector<PassPlan> split;
+        for (auto &pp : plan) {
+            if (!pp.fused) {
+                split.push_back(std::move(pp));
+                continue;
+            }
+            std::vector<int> lv;
+            const std::vector<size_t> ord = order_by_levels(pp.prims, touch, diag, &lv);
+            PassPlan cur;
+            cur.fused = true;
+            cur.local = pp.local;
+            int ndl = 0, last_dl = -1;
+            for (size_t k = 0; k < ord.size(); k++) {
+                const bool dg = diag[ord[k]] != 0;
+                if (dg && lv[k] != last_dl) {
+                    if (ndl == kDiagLevelsPerPass) {
+                        split.push_back(std::move(cur));
+                        cur = PassPlan{};
+                        cur.fused = true;
+                        cur.local = pp.local;
+                        ndl = 0;
+                    }
+                    ndl++;
+                    last_dl = lv[k];
+                }
+                cur.prims.push_back(ord[k]);
+            }
+            if (!cur.prims.empty()) {
+                split.push_back(std::move(cur));
+            }
+        }
+        plan.swap(split);
+    }
+
     // ---- translate
     std::vector<TileOp<T>> ops;
     std::vector<DiagForm<T>> forms;
@@ -556,10 +679,45 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
             std::vector<std::complex<double>> tab;
             bool has_table = false;
             std::vector<DiagForm<T>> gforms, mforms;
+            // one-bit local factors collapse to one 2-entry factor per local
+            // bit; the table is then their tensor product, built by doubling
+            std::complex<double> bitf[kMaxTileBits][2];
+            u32 bitf_used = 0;
+            for (auto &dg : pend) {
+                if (dg.bits.size() == 1 && is_local(dg.bits[0])) {
+                    const int lp = lpos(dg.bits[0]);
+                    if (!((bitf_used >> lp) & 1U)) {
+                        bitf[lp][0] = bitf[lp][1] = {1.0, 0.0};
+                        bitf_used |= 1u << lp;
+                    }
+                    bitf[lp][0] *= dg.tab[0];
+                    bitf[lp][1] *= dg.tab[1];
+                }
+            }
+            if (bitf_used) {
+                tab.assign(size_t{1} << d.t, {1.0, 0.0});
+                has_table = true;
+                size_t len = 1;
+                for (int lp = 0; lp < d.t; lp++) {
+                    if ((bitf_used >> lp) & 1U) {
+                        for (size_t j = 0; j < len; j++) {
+                            tab[j + len] = tab[j] * bitf[lp][1];
+                            tab[j] *= bitf[lp][0];
+                        }
+                    } else {
+                        std::copy(tab.begin(), tab.begin() + static_cast<std::ptrdiff_t>(len),
+                                  tab.begin() + static_cast<std::ptrdiff_t>(len));
+                    }
+                    len <<= 1;
+                }
+            }
             for (auto &dg : pend) {
                 int nloc = 0, nglob = 0;
                 for (int b : dg.bits) {
                     is_local(b) ? nloc++ : nglob++;
+                }
+                if (nglob == 0 && dg.bits.size() == 1) {
+                    continue; // in the per-bit factors above
                 }
                 if (nglob == 0) {
                     if (!has_table) {
@@ -637,58 +795,7 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
             pend.clear();
         };
 
-        // Order the pass as dependency layers: non-diagonal ops at level
-        // 1 + (level of anything they depend on), diagonals at the level of
-        // their latest non-diagonal predecessor.  All diagonals of one level
-        // then merge into a single op placed between two layers.
-        std::vector<int> level(pp.prims.size(), 0);
-        {
-            std::vector<int> nd_level(64, 0), d_level(64, 0);
-            for (size_t k = 0; k < pp.prims.size(); k++) {
-                const size_t pi = pp.prims[k];
-                const u64 tb = touch[pi];
-                int lv = 0;
-                if (diag[pi]) {
-                    for (int b = 0; b < 64; b++) {
-                        if ((tb >> b) & 1U) {
-                            lv = std::max(lv, nd_level[static_cast<size_t>(b)]);
-                        }
-                    }
-                    for (int b = 0; b < 64; b++) {
-                        if ((tb >> b) & 1U) {
-                            d_level[static_cast<size_t>(b)] = std::max(d_level[static_cast<size_t>(b)], lv);
-                        }
-                    }
-                } else {
-                    for (int b = 0; b < 64; b++) {
-                        if ((tb >> b) & 1U) {
-                            lv = std::max({lv, nd_level[static_cast<size_t>(b)], d_level[static_cast<size_t>(b)]});
-                        }
-                    }
-                    lv += 1;
-                    for (int b = 0; b < 64; b++) {
-                        if ((tb >> b) & 1U) {
-                            nd_level[static_cast<size_t>(b)] = lv;
-                        }
-                    }
-                }
-                level[k] = lv;
-            }
-        }
-        const int maxlv = pp.prims.empty() ? 0 : *std::max_element(level.begin(), level.end());
-        std::vector<size_t> ordered;
-        for (int lv = 0; lv <= maxlv; lv++) {
-            for (size_t k = 0; k < pp.prims.size(); k++) { // the layer's non-diagonal ops
-                if (level[k] == lv && !diag[pp.prims[k]]) {
-                    ordered.push_back(pp.prims[k]);
-                }
-            }
-            for (size_t k = 0; k < pp.prims.size(); k++) { // then the diagonals between layers
-                if (level[k] == lv && diag[pp.prims[k]]) {
-                    ordered.push_back(pp.prims[k]);
-                }
-            }
-        }
+        const std::vector<size_t> ordered = order_by_levels(pp.prims, touch, diag, nullptr);
         for (size_t pi : ordered) {
             const auto &p = P[pi];
             Diag<T> dg;
@@ -796,6 +903,10 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
         prog->plan = js + "]";
     }
     if (!upload) {
+        prog->h_ops = std::move(ops);
+        prog->h_forms = std::move(forms);
+        prog->h_tables = std::move(tables);
+        prog->h_stages = std::move(stages);
         return prog;
     }
 

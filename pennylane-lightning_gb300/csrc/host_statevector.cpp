@@ -79,6 +79,12 @@ static const char *kGateNames[] = {
     "CRZ", "CRot", "SingleExcitation", "SingleExcitationMinus", "SingleExcitationPlus", "PSWAP", "Toffoli", "CSWAP",
     "DoubleExcitation", "DoubleExcitationMinus", "DoubleExcitationPlus", "MultiRZ", "GlobalPhase", "PCPhase"};
 
+const char *gate_name_of(int code) {
+    constexpr int k = static_cast<int>(sizeof(kGateNames) / sizeof(kGateNames[0]));
+    return code >= 0 && code < k ? kGateNames[code] : nullptr;
+}
+int gate_code_count() { return static_cast<int>(sizeof(kGateNames) / sizeof(kGateNames[0])); }
+
 bool is_named_gate(const std::string &name) {
     for (auto *g : kGateNames) {
         if (name == g) {

@@ -1,0 +1,218 @@
+// Kernels of the batch engine (batch.hpp): one persistent launch per fused
+// layer over the tiles of many registers, the |0...0> initialisation of a
+// wave of registers, and batched Pauli-sum reductions.
+#include "batch.hpp"
+#include "tile_reg.cuh"
+
+namespace plgb {
+
+template <class T>
+__global__ void __launch_bounds__(256, 1)
+    k_tile_reg_batch(const BatchTileItem<T> *__restrict__ items, int nitems, u64 total_tiles) {
+    extern __shared__ unsigned char smraw[];
+    cx<T> *tile = reinterpret_cast<cx<T> *>(smraw);
+    __shared__ TileShared<T> sh;
+    __shared__ TilePassDesc sd;
+    int cur = -1;
+    for (u64 gt = blockIdx.x; gt < total_tiles; gt += gridDim.x) {
+        // item owning global tile gt: the last one whose tile_begin <= gt
+        int lo = 0, hi = nitems - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (items[mid].tile_begin <= gt) {
+                lo = mid;
+            } else {
+                hi = mid - 1;
+            }
+        }
+        if (lo != cur) { // block-uniform: every thread found the same item
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                sd = items[lo].desc;
+            }
+            __syncthreads();
+            cur = lo;
+        }
+        const BatchTileItem<T> &it = items[lo];
+        tile_reg_run<T>(it.sv, sd, it.ops, it.forms, it.tables, it.stages, gt - it.tile_begin, tile, sh);
+    }
+}
+
+template <class T>
+void launch_tile_reg_batch(cudaStream_t s, int t, const BatchTileItem<T> *items, int nitems, u64 total_tiles) {
+    if (t < kMinRegTileBits || t > 12 || nitems < 1 || total_tiles < 1) {
+        throw std::runtime_error("batched tile pass: unsupported geometry");
+    }
+    const int threads = 1 << (t - kRegBits);
+    const size_t smem = sizeof(cx<T>) << t;
+    static bool attr = false;
+    if (!attr) {
+        cuda_check(cudaFuncSetAttribute(k_tile_reg_batch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
+                   "tile_reg_batch smem attribute");
+        attr = true;
+    }
+    int per_sm = 1;
+    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_reg_batch<T>, threads, smem),
+               "occupancy");
+    if (per_sm < 1) {
+        throw std::runtime_error("batched tile pass: tile does not fit one SM");
+    }
+    const u64 cap = static_cast<u64>(LaunchGeom::sm_count()) * static_cast<u64>(per_sm);
+    const unsigned grid = static_cast<unsigned>(total_tiles < cap ? total_tiles : cap);
+    k_tile_reg_batch<T><<<grid, threads, smem, s>>>(items, nitems, total_tiles);
+    cuda_check(cudaGetLastError(), "k_tile_reg_batch launch");
+    note_launch();
+}
+
+template <class T> __global__ void k_batch_set_one(cx<T> *const *__restrict__ svs, int n) {
+    const int i = static_cast<int>(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i < n) {
+        svs[i][0] = cx<T>{1, 0};
+    }
+}
+template <class T> void launch_batch_set_one(cudaStream_t s, cx<T> *const *svs, int n) {
+    if (n < 1) {
+        return;
+    }
+    k_batch_set_one<T><<<(n + 255) / 256, 256, 0, s>>>(svs, n);
+    cuda_check(cudaGetLastError(), "k_batch_set_one launch");
+    note_launch();
+}
+
+namespace {
+
+constexpr int kBatchRedThreads = 256;
+
+__device__ __forceinline__ double batch_term_pair(const PauliTerm &t, u64 j, u64 jp, double ar, double ai) {
+    const double s = (__popcll(j & t.yz) & 1) ? -1.0 : 1.0;
+    const double sp = (__popcll(jp & t.yz) & 1) ? -1.0 : 1.0;
+    // real part of i^ny ((s' + s) ar + i (s' - s) ai)
+    switch (t.ny4) {
+    case 0: return (sp + s) * ar;
+    case 1: return -(sp - s) * ai;
+    case 2: return -(sp + s) * ar;
+    default: return (sp - s) * ai;
+    }
+}
+
+} // namespace
+
+// Block b of item it covers work units [c0, c0 + kBatchRedChunk) with
+// c0 = (b - block_begin) * kBatchRedChunk; the partial of every block lands
+// in its own slot, summed later in a fixed order.
+template <class T>
+__global__ void __launch_bounds__(kBatchRedThreads)
+    k_pauli_batch(const BatchRedItem<T> *__restrict__ items, int nitems, double *__restrict__ partials) {
+    const u64 b = blockIdx.x;
+    int lo = 0, hi = nitems - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (items[mid].block_begin <= b) {
+            lo = mid;
+        } else {
+            hi = mid - 1;
+        }
+    }
+    const BatchRedItem<T> &it = items[lo];
+    const PauliGroup &g = *it.group;
+    const cx<T> *a = it.sv;
+    const u64 c0 = (b - it.block_begin) * kBatchRedChunk;
+    const u64 c1 = c0 + kBatchRedChunk < it.work ? c0 + kBatchRedChunk : it.work;
+    double v = 0.0;
+    if (g.x == 0) {
+        for (u64 j = c0 + threadIdx.x; j < c1; j += kBatchRedThreads) {
+            const cx<T> p = a[j];
+            const double w = static_cast<double>(p.x) * p.x + static_cast<double>(p.y) * p.y;
+            double f = 0.0;
+            for (int t = 0; t < g.nterms; t++) {
+                f += (__popcll(j & g.t[t].yz) & 1) ? -g.t[t].coeff : g.t[t].coeff;
+            }
+            v += w * f;
+        }
+    } else {
+        for (u64 k = c0 + threadIdx.x; k < c1; k += kBatchRedThreads) {
+            const u64 j = insert_zero(k, g.hb);
+            const u64 jp = j ^ g.x;
+            const cx<T> p = a[j];
+            const cx<T> q = a[jp];
+            const double ar = static_cast<double>(p.x) * q.x + static_cast<double>(p.y) * q.y;
+            const double ai = static_cast<double>(p.x) * q.y - static_cast<double>(p.y) * q.x;
+            double f = 0.0;
+            for (int t = 0; t < g.nterms; t++) {
+                f += g.t[t].coeff * batch_term_pair(g.t[t], j, jp, ar, ai);
+            }
+            v += f;
+        }
+    }
+    __shared__ double sh[kBatchRedThreads / 32];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        v += __shfl_down_sync(0xffffffffu, v, d);
+    }
+    if ((threadIdx.x & 31u) == 0) {
+        sh[threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double x = threadIdx.x < kBatchRedThreads / 32 ? sh[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            x += __shfl_down_sync(0xffffffffu, x, d);
+        }
+        if (threadIdx.x == 0) {
+            partials[b] = x;
+        }
+    }
+}
+
+// One warp per item: its blocks' partials in a fixed order.
+template <class T>
+__global__ void k_pauli_batch_items(const BatchRedItem<T> *__restrict__ items, int nitems, u64 total_blocks,
+                                    const double *__restrict__ partials, double *__restrict__ item_sums) {
+    const int it = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = static_cast<int>(threadIdx.x & 31u);
+    if (it >= nitems) {
+        return;
+    }
+    const u64 b0 = items[it].block_begin;
+    const u64 b1 = it + 1 < nitems ? items[it + 1].block_begin : total_blocks;
+    double x = 0.0;
+    for (u64 b = b0 + static_cast<u64>(lane); b < b1; b += 32) {
+        x += partials[b];
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        x += __shfl_down_sync(0xffffffffu, x, d);
+    }
+    if (lane == 0) {
+        item_sums[it] = x;
+    }
+}
+
+template <class T>
+void launch_pauli_batch(cudaStream_t s, const BatchRedItem<T> *items, int nitems, u64 total_blocks, double *partials,
+                        double *item_sums) {
+    if (nitems < 1) {
+        return;
+    }
+    if (total_blocks > 0x7fffffffULL) {
+        throw std::runtime_error("batched reduction: too many blocks");
+    }
+    k_pauli_batch<T><<<static_cast<unsigned>(total_blocks), kBatchRedThreads, 0, s>>>(items, nitems, partials);
+    cuda_check(cudaGetLastError(), "k_pauli_batch launch");
+    note_launch();
+    const unsigned warps_per_block = 8;
+    const unsigned grid = static_cast<unsigned>((static_cast<unsigned>(nitems) + warps_per_block - 1) / warps_per_block);
+    k_pauli_batch_items<T><<<grid, 32 * warps_per_block, 0, s>>>(items, nitems, total_blocks, partials, item_sums);
+    cuda_check(cudaGetLastError(), "k_pauli_batch_items launch");
+    note_launch();
+}
+
+#define PLGB_BATCH_INST(T)                                                                                        \
+    template void launch_tile_reg_batch<T>(cudaStream_t, int, const BatchTileItem<T> *, int, u64);               \
+    template void launch_batch_set_one<T>(cudaStream_t, cx<T> *const *, int);                                    \
+    template void launch_pauli_batch<T>(cudaStream_t, const BatchRedItem<T> *, int, u64, double *, double *);
+PLGB_BATCH_INST(float)
+PLGB_BATCH_INST(double)
+
+} // namespace plgb

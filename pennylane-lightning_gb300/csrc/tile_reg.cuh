@@ -1,0 +1,408 @@
+// Register-blocked fused tile pass: the per-tile body shared by the
+// single-register kernel (kernels_fused_reg.cu) and the batched kernel over
+// many registers (kernels_batch.cu).
+//
+// Same pass semantics as kernels_fused.cu, different execution: a CTA of
+// 2^(t-4) threads holds its tile of 2^t amplitudes in registers, 16 per
+// thread.  The host splits the pass into stages.  In a register stage four
+// local bits are "register bits" (amplitudes differing only in them live in
+// the same thread) and every one-target op on them is pure register
+// arithmetic: no shared memory, no index math, no barrier.  Changing the
+// register bits is one shared-memory transpose (XOR-swizzled so that strided
+// thread patterns stay conflict-free).  Two-target ops run in a shared-memory
+// stage.  Merged diagonals are evaluated per tile once, in a prologue, and
+// applied in registers from the per-pass table.
+#pragma once
+
+#include "fused.hpp"
+
+namespace plgb {
+
+namespace {
+
+constexpr int RB = kRegBits;
+constexpr int NR = 1 << RB;
+
+template <class T> __device__ __forceinline__ u32 swz(u32 j) {
+    if constexpr (sizeof(T) == 8) { // 16-byte amplitudes: 8 per 128-byte row
+        return j ^ (((j >> 3) ^ (j >> 6) ^ (j >> 9) ^ (j >> 12)) & 7u);
+    } else { // 8-byte amplitudes: 16 per row
+        return j ^ (((j >> 4) ^ (j >> 8) ^ (j >> 12)) & 15u);
+    }
+}
+
+__device__ __forceinline__ u64 local_offset_r(u32 j, const TilePassDesc &d) {
+    u64 off = j & ((1u << d.L) - 1u);
+#pragma unroll 4
+    for (int m = 0; m < d.H; m++) {
+        off |= static_cast<u64>((j >> (d.L + m)) & 1u) << d.hb[m];
+    }
+    return off;
+}
+
+__device__ __forceinline__ u32 insert_zeros_r(u32 k, const int *ins, int nins) {
+    for (int i = 0; i < nins; i++) {
+        const int p = ins[i];
+        k = ((k >> p) << (p + 1)) | (k & ((1u << p) - 1u));
+    }
+    return k;
+}
+
+__device__ __forceinline__ double sflip(double x, unsigned neg) {
+    return __longlong_as_double(__double_as_longlong(x) ^ (static_cast<long long>(neg) << 63));
+}
+__device__ __forceinline__ float sflip(float x, unsigned neg) {
+    return __int_as_float(__float_as_int(x) ^ static_cast<int>(neg << 31));
+}
+template <class T> __device__ __forceinline__ cx<T> cflip(cx<T> v, unsigned neg) {
+    return cx<T>{sflip(v.x, neg), sflip(v.y, neg)};
+}
+template <class T> __device__ __forceinline__ cx<T> shx(cx<T> v, int m) {
+    return cx<T>{__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m)};
+}
+
+// Layout of a register stage, held in registers: local index of register
+// slot i of this thread = jt | (bit k of i placed at local bit rb[k]).
+// The canonical layout (load / store) has rb = {w, w+1, w+2, w+3}, jt = tid.
+struct Layout {
+    u32 jt;
+    int rb0, rb1, rb2, rb3;
+    __device__ __forceinline__ u32 reg(int i) const {
+        return ((i & 1) ? (1u << rb0) : 0u) | ((i & 2) ? (1u << rb1) : 0u) | ((i & 4) ? (1u << rb2) : 0u) |
+               ((i & 8) ? (1u << rb3) : 0u);
+    }
+    __device__ __forceinline__ u32 at(int i) const { return jt | reg(i); }
+};
+__device__ __forceinline__ Layout canonical_layout(u32 tid, int w) { return Layout{tid, w, w + 1, w + 2, w + 3}; }
+__device__ __forceinline__ Layout stage_layout(const StageDesc *st, u32 tid, int w) {
+    u32 jt = 0;
+    for (int m = 0; m < w; m++) {
+        jt |= ((tid >> m) & 1u) << st->tb[m];
+    }
+    return Layout{jt, st->rb[0], st->rb[1], st->rb[2], st->rb[3]};
+}
+
+template <class T> __device__ __forceinline__ void to_smem(cx<T> *tile, const cx<T> (&v)[NR], const Layout &l) {
+#pragma unroll
+    for (int i = 0; i < NR; i++) {
+        tile[swz<T>(l.at(i))] = v[i];
+    }
+}
+template <class T> __device__ __forceinline__ void from_smem(const cx<T> *tile, cx<T> (&v)[NR], const Layout &l) {
+#pragma unroll
+    for (int i = 0; i < NR; i++) {
+        v[i] = tile[swz<T>(l.at(i))];
+    }
+}
+
+// One-target op on register bit K for the eight pairs of a thread, one
+// specialisation per op shape so the unrolled body has no mode branches.
+template <int MODE, bool CTRL, class T, int K>
+__device__ __forceinline__ void reg_op_k(cx<T> (&v)[NR], const TileOp<T> &op, const Layout &l) {
+    const u32 cm = op.rcmask, cv = op.rcval;
+    const T ca = op.m[0].x, cb = op.m[0].y;
+    const cx<T> m0 = op.m[0], m1 = op.m[1], m2 = op.m[2], m3 = op.m[3];
+#pragma unroll
+    for (int i = 0; i < NR; i++) {
+        if (i & (1 << K)) {
+            continue;
+        }
+        const int i1 = i | (1 << K);
+        if (CTRL && ((l.at(i) & cm) != cv)) {
+            continue;
+        }
+        const cx<T> v0 = v[i], v1 = v[i1];
+        if constexpr (MODE == RM_SROT_A) { // [[1, -b], [b, 1]]
+            v[i] = cx<T>{v0.x - cb * v1.x, v0.y - cb * v1.y};
+            v[i1] = cx<T>{cb * v0.x + v1.x, cb * v0.y + v1.y};
+        } else if constexpr (MODE == RM_SROT_B) { // [[a, -1], [1, a]]
+            v[i] = cx<T>{ca * v0.x - v1.x, ca * v0.y - v1.y};
+            v[i1] = cx<T>{v0.x + ca * v1.x, v0.y + ca * v1.y};
+        } else if constexpr (MODE == RM_SWAP) {
+            v[i] = v1;
+            v[i1] = v0;
+        } else { // general complex 2x2
+            v[i] = cfma(m1, v1, m0 * v0);
+            v[i1] = cfma(m3, v1, m2 * v0);
+        }
+    }
+}
+template <int MODE, bool CTRL, class T>
+__device__ __forceinline__ void reg_op_m(cx<T> (&v)[NR], const TileOp<T> &op, const Layout &l) {
+    switch (op.rk) {
+    case 0: reg_op_k<MODE, CTRL, T, 0>(v, op, l); break;
+    case 1: reg_op_k<MODE, CTRL, T, 1>(v, op, l); break;
+    case 2: reg_op_k<MODE, CTRL, T, 2>(v, op, l); break;
+    default: reg_op_k<MODE, CTRL, T, 3>(v, op, l); break;
+    }
+}
+template <class T> __device__ __forceinline__ void reg_op(cx<T> (&v)[NR], const TileOp<T> &op, const Layout &l) {
+    if (op.rcmask == 0) {
+        switch (op.mode) {
+        case RM_SROT_A: reg_op_m<RM_SROT_A, false>(v, op, l); break;
+        case RM_SROT_B: reg_op_m<RM_SROT_B, false>(v, op, l); break;
+        case RM_SWAP: reg_op_m<RM_SWAP, false>(v, op, l); break;
+        default: reg_op_m<RM_DENSE, false>(v, op, l); break;
+        }
+    } else {
+        switch (op.mode) {
+        case RM_SROT_A: reg_op_m<RM_SROT_A, true>(v, op, l); break;
+        case RM_SROT_B: reg_op_m<RM_SROT_B, true>(v, op, l); break;
+        case RM_SWAP: reg_op_m<RM_SWAP, true>(v, op, l); break;
+        default: reg_op_m<RM_DENSE, true>(v, op, l); break;
+        }
+    }
+}
+
+template <class T>
+__device__ __forceinline__ cx<T> form_val(const DiagForm<T> &f, u64 gbase) {
+    unsigned k = 0;
+    for (int b = 0; b < f.nb; b++) {
+        k = (k << 1) | static_cast<unsigned>((gbase >> f.bits[b]) & 1u);
+    }
+    return f.tab[k];
+}
+
+
+// Shared-memory state of the per-tile prologue (one slot per merged diagonal).
+template <class T> struct TileShared {
+    cx<T> scal[kMaxDiagOpsPerPass];
+    u32 zl[kMaxDiagOpsPerPass];
+    int ngen[kMaxDiagOpsPerPass];
+    int gbit[kMaxDiagOpsPerPass][4];
+    cx<T> gd0[kMaxDiagOpsPerPass][4];
+    cx<T> gd1[kMaxDiagOpsPerPass][4];
+    cx<T> factor;
+};
+
+// Apply pass `d` to tile g of register `a` (all threads of the CTA; the CTA
+// has 2^(d.t - 4) threads and 2^d.t amplitudes of shared memory at `tile`).
+template <class T>
+__device__ __forceinline__ void tile_reg_run(cx<T> *__restrict__ a, const TilePassDesc &d,
+                                             const TileOp<T> *__restrict__ ops, const DiagForm<T> *__restrict__ forms,
+                                             const cx<T> *__restrict__ tables, const StageDesc *__restrict__ stages,
+                                             u64 g, cx<T> *tile, TileShared<T> &sh) {
+    const int w = d.t - RB;
+    const u32 tid = threadIdx.x;
+    const int lane = static_cast<int>(tid & 31u);
+    const int warp = static_cast<int>(tid >> 5);
+    const int nwarps = static_cast<int>(blockDim.x >> 5);
+    cx<T> v[NR];
+    // global offset of canonical slot i of this thread: the local->global map
+    // is a bit deposit, so it splits into a thread part and a slot part
+    const u64 off_t = local_offset_r(tid, d);
+    // canonical slot bits are local bits w..w+3 = global bits hb[w-L .. w-L+3]
+    const int g0 = d.hb[w - d.L], g1 = d.hb[w - d.L + 1], g2 = d.hb[w - d.L + 2], g3 = d.hb[w - d.L + 3];
+    auto off_r = [&](int i) -> u64 {
+        return ((i & 1) ? (u64{1} << g0) : 0) | ((i & 2) ? (u64{1} << g1) : 0) | ((i & 4) ? (u64{1} << g2) : 0) |
+               ((i & 8) ? (u64{1} << g3) : 0);
+    };
+    const Layout canon = canonical_layout(tid, w);
+
+    u64 gbase = g << d.L;
+    for (int m = 0; m < d.H; m++) {
+        const int p = d.hb[m];
+        gbase = ((gbase >> p) << (p + 1)) | (gbase & ((u64{1} << p) - 1));
+    }
+    const u64 tbase = gbase | off_t;
+#pragma unroll
+    for (int i = 0; i < NR; i++) {
+        v[i] = a[tbase | off_r(i)];
+    }
+    // prologue: tile-uniform parts of every merged diagonal, one warp per op
+    int slot = 0;
+    for (int oi = 0; oi < d.nops; oi++) {
+        const TileOp<T> &op = ops[d.op_begin + oi];
+        if (op.kind != TK_DIAGTAB) {
+            continue;
+        }
+        if ((slot % nwarps) == warp) {
+            cx<T> sc{1, 0};
+            if ((gbase & op.gcmask) == op.gcval) {
+                for (int f = lane; f < op.ngforms; f += 32) {
+                    sc = sc * form_val(forms[op.gform_begin + f], gbase);
+                }
+            }
+            u32 zl = 0;
+            bool gen = false;
+            cx<T> d0{1, 0}, d1{1, 0};
+            int lb = 0;
+            if (lane < op.nmforms && (gbase & op.gcmask) == op.gcval) {
+                const DiagForm<T> &mf = forms[op.mform_begin + lane];
+                const unsigned gb = static_cast<unsigned>((gbase >> mf.bits[0]) & 1u);
+                d0 = mf.tab[2 * gb];
+                d1 = mf.tab[2 * gb + 1];
+                lb = mf.local_bit;
+                if (d1.x == d0.x && d1.y == d0.y) {
+                    sc = sc * d0;
+                } else if (d1.x == -d0.x && d1.y == -d0.y) {
+                    sc = sc * d0;
+                    zl = 1u << lb;
+                } else {
+                    gen = true;
+                }
+            }
+#pragma unroll
+            for (int mm = 16; mm > 0; mm >>= 1) {
+                sc = sc * shx(sc, mm);
+                zl ^= __shfl_xor_sync(0xffffffffu, zl, mm);
+            }
+            const unsigned gm = __ballot_sync(0xffffffffu, gen);
+            if (gen) {
+                const int k = __popc(gm & ((1u << lane) - 1u));
+                if (k < 4) {
+                    sh.gbit[slot][k] = lb;
+                    sh.gd0[slot][k] = d0;
+                    sh.gd1[slot][k] = d1;
+                }
+            }
+            if (lane == 0) {
+                sh.scal[slot] = sc;
+                sh.zl[slot] = zl;
+                sh.ngen[slot] = min(__popc(gm), 4);
+            }
+        }
+        slot++;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        cx<T> f{static_cast<T>(d.pass_scale), 0};
+        for (int s = 0; s < d.ndiag; s++) {
+            f = f * sh.scal[s];
+        }
+        sh.factor = f;
+    }
+
+    Layout cur = canon;
+    bool cur_canon = true;
+    int cur_stage = -1;
+    for (int si = 0; si < d.nstages; si++) {
+        const StageDesc *st = &stages[d.stage_begin + si];
+        if (st->kind == 0) {
+            if (cur_stage != si) {
+                const Layout nl = stage_layout(st, tid, w);
+                to_smem(tile, v, cur);
+                __syncthreads();
+                from_smem(tile, v, nl);
+                __syncthreads();
+                cur = nl;
+                cur_canon = false;
+                cur_stage = si;
+            }
+            for (int oi = st->op_begin; oi < st->op_begin + st->nops; oi++) {
+                const TileOp<T> &op = ops[oi];
+                if ((gbase & op.gcmask) != op.gcval) {
+                    continue;
+                }
+                if (op.kind == TK_DIAGTAB) {
+                    const int s = op.diag_slot;
+                    const u32 zl = sh.zl[s];
+                    const int ngen = sh.ngen[s];
+                    const cx<T> *tab = tables + op.table_off;
+                    if (op.has_table) {
+#pragma unroll
+                        for (int i = 0; i < NR; i++) {
+                            const u32 j = cur.at(i);
+                            v[i] = cflip(tab[j] * v[i], static_cast<unsigned>(__popc(j & zl) & 1));
+                        }
+                    } else if (zl) {
+#pragma unroll
+                        for (int i = 0; i < NR; i++) {
+                            v[i] = cflip(v[i], static_cast<unsigned>(__popc(cur.at(i) & zl) & 1));
+                        }
+                    }
+                    for (int f = 0; f < ngen; f++) {
+                        const int gb = sh.gbit[s][f];
+                        const cx<T> g0 = sh.gd0[s][f], g1 = sh.gd1[s][f];
+#pragma unroll
+                        for (int i = 0; i < NR; i++) {
+                            v[i] = (((cur.at(i) >> gb) & 1u) ? g1 : g0) * v[i];
+                        }
+                    }
+                } else if (op.kind == TK_PARITY) {
+#pragma unroll
+                    for (int i = 0; i < NR; i++) {
+                        const u64 idx = gbase | local_offset_r(cur.at(i), d);
+                        if ((idx & op.cmask) != op.cval) {
+                            if (op.zero_outside) {
+                                v[i] = cx<T>{0, 0};
+                            }
+                            continue;
+                        }
+                        v[i] = ((__popcll(idx & op.pmask) & 1) ? op.m[1] : op.m[0]) * v[i];
+                    }
+                } else {
+                    reg_op(v, op, cur);
+                }
+            }
+        } else {
+            // shared-memory stage: two-target ops on the staged tile
+            to_smem(tile, v, cur);
+            __syncthreads();
+            const u32 T_ = 1u << d.t;
+            for (int oi = st->op_begin; oi < st->op_begin + st->nops; oi++) {
+                const TileOp<T> &op = ops[oi];
+                if ((gbase & op.gcmask) == op.gcval) {
+                    if (op.kind == TK_DENSE2) {
+                        const u32 nq = T_ >> op.nlins;
+                        for (u32 p = tid; p < nq; p += blockDim.x) {
+                            const u32 j0 = insert_zeros_r(p, op.lins, op.nlins) | op.lcval;
+                            const u32 ix[4] = {swz<T>(j0), swz<T>(j0 | op.lo1), swz<T>(j0 | op.lo0),
+                                               swz<T>(j0 | op.lo0 | op.lo1)};
+                            cx<T> x[4];
+#pragma unroll
+                            for (int r = 0; r < 4; r++) {
+                                x[r] = tile[ix[r]];
+                            }
+#pragma unroll
+                            for (int r = 0; r < 4; r++) {
+                                cx<T> acc = op.m[4 * r] * x[0];
+                                acc = cfma(op.m[4 * r + 1], x[1], acc);
+                                acc = cfma(op.m[4 * r + 2], x[2], acc);
+                                acc = cfma(op.m[4 * r + 3], x[3], acc);
+                                tile[ix[r]] = acc;
+                            }
+                        }
+                    } else { // two-amplitude op with general offsets
+                        const u32 np = T_ >> op.nlins;
+                        for (u32 p = tid; p < np; p += blockDim.x) {
+                            const u32 j0 = insert_zeros_r(p, op.lins, op.nlins) | op.lcval;
+                            cx<T> &x0 = tile[swz<T>(j0 | op.lo0)];
+                            cx<T> &x1 = tile[swz<T>(j0 | op.lo1)];
+                            const cx<T> v0 = x0, v1 = x1;
+                            if (op.mode == RM_SWAP) {
+                                x0 = v1;
+                                x1 = v0;
+                            } else {
+                                x0 = cfma(op.m[1], v1, op.m[0] * v0);
+                                x1 = cfma(op.m[3], v1, op.m[2] * v0);
+                            }
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+            from_smem(tile, v, canon);
+            __syncthreads();
+            cur = canon;
+            cur_canon = true;
+            cur_stage = -1;
+        }
+    }
+    if (!cur_canon) {
+        to_smem(tile, v, cur);
+        __syncthreads();
+        from_smem(tile, v, canon);
+    }
+    __syncthreads();
+    const cx<T> f = sh.factor;
+#pragma unroll
+    for (int i = 0; i < NR; i++) {
+        a[tbase | off_r(i)] = f * v[i];
+    }
+    __syncthreads();
+}
+
+} // namespace
+
+} // namespace plgb

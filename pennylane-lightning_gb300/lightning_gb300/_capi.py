@@ -54,6 +54,12 @@ SIGNATURES = {
     "plgb_meas_expval_named": (C.c_int, [VP, C.c_char_p, I64P, C.c_int, DP]),
     "plgb_meas_expval_matrix": (C.c_int, [VP, DP, I64P, C.c_int, DP]),
     "plgb_meas_expval_matrix_noalloc": (C.c_int, [VP, DP, I64P, C.c_int, DP]),
+    "plgb_batch_create": (C.c_int, [C.c_int, C.POINTER(VP)]),
+    "plgb_batch_destroy": (C.c_int, [VP]),
+    "plgb_batch_configure": (C.c_int, [VP, C.c_int, C.c_int64, C.c_int]),
+    "plgb_batch_run": (C.c_int, [VP, C.c_int, VP, VP, VP, VP, VP, VP, VP, VP, VP, VP, VP, VP, DP]),
+    "plgb_batch_stats": (C.c_int, [VP, C.c_char_p, C.c_size_t]),
+    "plgb_gate_name": (C.c_char_p, [C.c_int]),
     "plgb_meas_expval_sparse": (C.c_int, [VP, I64P, C.c_int64, I64P, DP, C.c_int64, DP]),
     "plgb_meas_expval_obs": (C.c_int, [VP, VP, DP]),
     "plgb_meas_var_obs": (C.c_int, [VP, VP, DP]),

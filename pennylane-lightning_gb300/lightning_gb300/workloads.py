@@ -145,6 +145,52 @@ def config2(num: int = 4096, seed: int = 1002) -> list[BatchCircuit]:
     return out
 
 
+def config2_packed(num: int = 4096, seed: int = 1002):
+    """config2 in the batch engine's packed layout, built with array
+    operations (same circuits and observables as config2)."""
+    from .batch import MAX_WIRES_PER_OP, PackedBatch, code_of, pauli_masks
+
+    rx, ry, rz, cnot = code_of("RX"), code_of("RY"), code_of("RZ"), code_of("CNOT")
+    rng = np.random.default_rng(seed)
+    nq, codes, wires, params = [], [], [], []
+    op_off, term_off, coeffs, xs, ys, zs = [0], [0], [], [], [], []
+    for _ in range(num):
+        n = int(rng.integers(10, 23))
+        depth = int(rng.integers(4, 17))
+        angles = np.random.default_rng(int(rng.integers(0, 2**31 - 1))).uniform(0.0, TWO_PI, size=(depth, n, 3))
+        obs = [sum_z(n)] + [random_pauli_sum(rng, n, 1, 2, 2) for _ in range(3)]
+        per_layer = 4 * n
+        c = np.empty((depth, per_layer), np.int32)
+        c[:, :3 * n] = np.tile(np.array([rx, ry, rz], np.int32), n)
+        c[:, 3 * n:] = cnot
+        w = np.full((depth, per_layer, MAX_WIRES_PER_OP), -1, np.int32)
+        q = np.arange(n, dtype=np.int32)
+        w[:, :3 * n, 0] = np.repeat(q, 3)
+        w[:, 3 * n:, 0] = q
+        w[:, 3 * n:, 1] = (q + 1) % n
+        pr = np.zeros((depth, per_layer, 3), np.float64)
+        pr[:, :3 * n, 0] = angles.reshape(depth, 3 * n)
+        nq.append(n)
+        codes.append(c.reshape(-1))
+        wires.append(w.reshape(-1, MAX_WIRES_PER_OP))
+        params.append(pr.reshape(-1, 3))
+        op_off.append(op_off[-1] + depth * per_layer)
+        for o in obs:
+            for cf, word, ws in zip(o.coeffs, o.words, o.wires):
+                x, y, z = pauli_masks(word, ws)
+                coeffs.append(cf)
+                xs.append(x)
+                ys.append(y)
+                zs.append(z)
+            term_off.append(len(coeffs))
+    m = op_off[-1]
+    return PackedBatch(np.asarray(nq, np.int32), np.asarray(op_off, np.int64), np.concatenate(codes),
+                       np.concatenate(wires), np.concatenate(params), np.zeros(m, np.uint8),
+                       np.arange(0, 4 * num + 1, 4, dtype=np.int64), np.asarray(term_off, np.int64),
+                       np.asarray(coeffs, np.float64), np.asarray(xs, np.uint64), np.asarray(ys, np.uint64),
+                       np.asarray(zs, np.uint64))
+
+
 # --------------------------------------------------------------------- config 3
 def config3(n: int = 28, layers: int = 12, seed: int = 1003, nterms: int = 200) -> tuple[list[Op], PauliSum]:
     rng = np.random.default_rng(seed)

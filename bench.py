@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--qubits", type=int, default=30)
     ap.add_argument("--cycles", type=int, default=20)
+    ap.add_argument("--tile-bits", type=int, default=None,
+                    help="fixed fused tile size 2^t (0 = unfused); default: chosen during warm-up")
     ap.add_argument("--no-c64", action="store_true", help="skip the complex64 variant")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     return ap.parse_args()
@@ -173,7 +175,7 @@ def gpu_arm(args) -> dict | None:
     sv = ops.StateVectorC128(n)
     stream = torch.cuda.ExternalStream(sv.cuda_stream())
     # warm-up doubles as the tile-size choice: unfused (0) vs fused tiles of 2^t
-    candidates = [0, 10, 11, 12]
+    candidates = [0, 10, 11, 12] if args.tile_bits is None else [args.tile_bits]
     tune = {}
     for w in range(max(args.warmup, 1)):
         tb = candidates[w % len(candidates)] if w < len(candidates) else best_tb
@@ -275,7 +277,7 @@ def gpu_arm(args) -> dict | None:
         sv64 = ops.StateVectorC64(n)
         s64 = torch.cuda.ExternalStream(sv64.cuda_stream())
         t64 = {}
-        for tb in (0, 11, 12):
+        for tb in ((0, 11, 12) if args.tile_bits is None else (args.tile_bits,)):
             timed_step(sv64, S64, s64, tb)
             t64[tb] = timed_step(sv64, S64, s64, tb)[0]
         b64 = min(t64, key=t64.get)

@@ -187,6 +187,15 @@ int plgb_ops_fusion_plan(const plgb_ops *ops, int num_qubits, int precision, int
  * the operations are first applied to a copy of the state. */
 int plgb_adjoint_jacobian(plgb_sv *sv, plgb_obs *const *obs, int nobs, const plgb_ops *ops, const int64_t *trainable,
                           int ntp, int apply_ops, double *jac_out);
+/* The same Jacobian with apply_ops = 0, computed in place: sv holds the
+ * final state and is overwritten by the backward sweep (left holding the
+ * initial state up to rounding).  Registers held: 1 + nobs for Pauli-sum
+ * observables and Pauli-word generators, instead of 2 + nobs plus
+ * temporaries; this is what lets a 32-qubit complex128 adjoint fit on one
+ * GPU.  No counterpart in the reference (AdjointJacobianLQubit.hpp:225-491
+ * always copies the state). */
+int plgb_adjoint_jacobian_inplace(plgb_sv *sv, plgb_obs *const *obs, int nobs, const plgb_ops *ops,
+                                  const int64_t *trainable, int ntp, double *jac_out);
 
 /* ---- batch engine (no counterpart in the reference: lightning.qubit runs
  *      circuits one at a time, one Python -> C++ call per gate,

@@ -764,5 +764,20 @@ int plgb_adjoint_jacobian(plgb_sv *sv, plgb_obs *const *obs, int nobs, const plg
         std::memcpy(jac_out, j.data(), j.size() * sizeof(double));
     });
 }
+int plgb_adjoint_jacobian_inplace(plgb_sv *sv, plgb_obs *const *obs, int nobs, const plgb_ops *ops,
+                                  const int64_t *trainable, int ntp, double *jac_out) {
+    return with_sv(sv, [&](auto &s) {
+        need(ops, "ops");
+        need(jac_out, "jac_out");
+        using T = decltype(s.data()->x);
+        std::vector<ObsPtr> ob;
+        for (int i = 0; i < nobs; i++) {
+            need(obs[i], "observable");
+            ob.push_back(obs[i]->node);
+        }
+        const auto j = Adjoint<T>::jacobian(s, ob, ops->list, vec(trainable, ntp), false, true);
+        std::memcpy(jac_out, j.data(), j.size() * sizeof(double));
+    });
+}
 
 } // extern "C"

@@ -229,6 +229,9 @@ template <class T> struct Measure {
     static std::vector<int64_t> samples(StateVector<T> &sv, const std::vector<int64_t> &wires, int64_t shots,
                                         uint64_t seed);
     static void apply_obs(StateVector<T> &sv, const ObsNode &obs);
+    // dst = obs |src> (dst: same register size, any content); Pauli sums
+    // need no temporary register
+    static void apply_obs_into(const StateVector<T> &src, StateVector<T> &dst, const ObsNode &obs);
 };
 
 // Pauli-sum compilation of an observable tree.
@@ -247,8 +250,11 @@ std::vector<PauliGroup> group_pauli(const PauliSum &ps);
 // Adjoint Jacobian (AdjointJacobianLQubit.hpp:225-491).
 // ---------------------------------------------------------------------------
 template <class T> struct Adjoint {
+    // consume: sv already holds the final state and may be overwritten; the
+    // sweep then runs in place on it (registers needed: 1 + observables for
+    // Pauli-sum observables and Pauli-word generators, instead of 2 + 2x)
     static std::vector<double> jacobian(StateVector<T> &sv, const std::vector<ObsPtr> &obs, const OpsList &ops,
-                                        const std::vector<int64_t> &trainable, bool apply_ops);
+                                        const std::vector<int64_t> &trainable, bool apply_ops, bool consume = false);
 };
 
 // ---------------------------------------------------------------------------

@@ -100,7 +100,7 @@ std::optional<PauliGen> pauli_generator(const OpRec &op, int n) {
 
 template <class T>
 std::vector<double> Adjoint<T>::jacobian(StateVector<T> &sv, const std::vector<ObsPtr> &obs, const OpsList &opsl,
-                                         const std::vector<int64_t> &tp, bool apply_ops) {
+                                         const std::vector<int64_t> &tp, bool apply_ops, bool consume) {
     const auto &ops = opsl.ops;
     const size_t nobs = obs.size();
     const size_t ntp = tp.size();
@@ -115,7 +115,12 @@ std::vector<double> Adjoint<T>::jacobian(StateVector<T> &sv, const std::vector<O
     PLGB_REQUIRE(tp.back() < static_cast<int64_t>(num_param_ops), "trainable parameter index out of range");
     const int n = sv.num_qubits();
 
-    StateVector<T> lambda(sv); // same stream
+    // lambda: the caller's register when it may be consumed, else a copy
+    std::optional<StateVector<T>> own;
+    if (!consume) {
+        own.emplace(sv); // same stream
+    }
+    StateVector<T> &lambda = consume ? sv : *own;
     if (apply_ops) {
         for (const auto &op : ops) {
             lambda.apply_op(op, op.inverse);
@@ -123,8 +128,8 @@ std::vector<double> Adjoint<T>::jacobian(StateVector<T> &sv, const std::vector<O
     }
     std::vector<std::unique_ptr<StateVector<T>>> hl;
     for (size_t h = 0; h < nobs; h++) {
-        hl.emplace_back(std::make_unique<StateVector<T>>(lambda));
-        Measure<T>::apply_obs(*hl.back(), *obs[h]);
+        hl.emplace_back(std::make_unique<StateVector<T>>(n, lambda.stream()));
+        Measure<T>::apply_obs_into(lambda, *hl.back(), *obs[h]);
     }
     std::unique_ptr<StateVector<T>> mu;
 

@@ -38,6 +38,89 @@ constexpr int kModeSrotB = 101; // [[a,-1],[1,a]]
 
 bool pair_is_diag(int mode) { return mode == M1_DIAG || mode == M1_PHASE1 || mode == M1_NEG1; }
 
+// Runs of uncontrolled one-wire gates on the same bit, with nothing else
+// touching that bit in between, become one 2x2 (composed in double
+// precision).  RX RY RZ on a wire then costs one rotation instead of two.
+template <class T> std::vector<Prim<T>> merge1q(const std::vector<Prim<T>> &in) {
+    using C2 = std::complex<double>;
+    struct Pend {
+        int count{0};
+        size_t first{0}; // index in `in` of the first gate of the run
+        C2 m[4];
+    };
+    std::vector<Pend> pend(64);
+    std::vector<Prim<T>> out;
+    out.reserve(in.size());
+    auto single = [](const Prim<T> &p) {
+        return p.kind == Prim<T>::Pair && p.tbits.size() == 1 && p.cbits.empty() && p.o0 == 0 &&
+               p.o1 == (u64{1} << p.tbits[0]) && p.mode >= M1_DENSE && p.mode <= M1_NEG1;
+    };
+    auto matrix = [](const Prim<T> &p, C2 (&m)[4]) {
+        auto c = [](cx<T> v) { return C2(v.x, v.y); };
+        switch (p.mode) {
+        case M1_DENSE: m[0] = c(p.m[0]); m[1] = c(p.m[1]); m[2] = c(p.m[2]); m[3] = c(p.m[3]); break;
+        case M1_REAL: m[0] = p.m[0].x; m[1] = p.m[1].x; m[2] = p.m[2].x; m[3] = p.m[3].x; break;
+        case M1_RXF:
+            m[0] = m[3] = p.m[0].x;
+            m[1] = m[2] = C2(0, p.m[1].y);
+            break;
+        case M1_DIAG: m[0] = c(p.m[0]); m[1] = m[2] = 0; m[3] = c(p.m[3]); break;
+        case M1_PHASE1: m[0] = 1; m[1] = m[2] = 0; m[3] = c(p.m[3]); break;
+        case M1_SWAP: m[0] = m[3] = 0; m[1] = m[2] = 1; break;
+        case M1_ANTI: m[0] = m[3] = 0; m[1] = c(p.m[1]); m[2] = c(p.m[2]); break;
+        default: m[0] = 1; m[1] = m[2] = 0; m[3] = -1; break; // M1_NEG1
+        }
+    };
+    auto flush = [&](int b) {
+        Pend &pd = pend[static_cast<size_t>(b)];
+        if (pd.count == 0) {
+            return;
+        }
+        if (pd.count == 1) {
+            out.push_back(in[pd.first]);
+        } else {
+            Prim<T> p = in[pd.first];
+            auto t = [](C2 v) { return cx<T>{static_cast<T>(v.real()), static_cast<T>(v.imag())}; };
+            const bool offz = pd.m[1] == C2(0) && pd.m[2] == C2(0);
+            const bool diagz = pd.m[0] == C2(0) && pd.m[3] == C2(0);
+            p.m = {t(pd.m[0]), t(pd.m[1]), t(pd.m[2]), t(pd.m[3])};
+            p.mode = offz ? (pd.m[0] == C2(1) ? M1_PHASE1 : M1_DIAG) : diagz ? M1_ANTI : M1_DENSE;
+            out.push_back(std::move(p));
+        }
+        pd.count = 0;
+    };
+    for (size_t i = 0; i < in.size(); i++) {
+        const Prim<T> &p = in[i];
+        if (single(p)) {
+            const int b = p.tbits[0];
+            Pend &pd = pend[static_cast<size_t>(b)];
+            C2 g[4];
+            matrix(p, g);
+            if (pd.count == 0) {
+                pd.first = i;
+                std::copy(g, g + 4, pd.m);
+            } else { // later gate on the left: m <- g m
+                const C2 r0 = g[0] * pd.m[0] + g[1] * pd.m[2], r1 = g[0] * pd.m[1] + g[1] * pd.m[3];
+                const C2 r2 = g[2] * pd.m[0] + g[3] * pd.m[2], r3 = g[2] * pd.m[1] + g[3] * pd.m[3];
+                pd.m[0] = r0;
+                pd.m[1] = r1;
+                pd.m[2] = r2;
+                pd.m[3] = r3;
+            }
+            pd.count++;
+            continue;
+        }
+        for (u64 r = p.touched(); r; r &= r - 1) {
+            flush(__builtin_ctzll(r));
+        }
+        out.push_back(p);
+    }
+    for (int b = 0; b < 64; b++) {
+        flush(b);
+    }
+    return out;
+}
+
 template <class T> std::vector<Prim<T>> rewrite(const std::vector<Prim<T>> &in) {
     std::vector<Prim<T>> out;
     out.reserve(in.size() * 2);
@@ -157,13 +240,17 @@ struct PassPlan {
 // Order the primitives of one pass as dependency layers (see the comment
 // inside); returns them in execution order with, per position, its level.
 std::vector<size_t> order_by_levels(const std::vector<size_t> &prims, const std::vector<u64> &touch,
-                                    const std::vector<char> &diag, std::vector<int> *levels_out) {
+                                    const std::vector<u64> &tmask, const std::vector<char> &diag,
+                                    std::vector<int> *levels_out) {
     // Order the pass as dependency layers.  Non-diagonal ops go to the
     // first level after everything they depend on.  A diagonal may sit at
     // any level from its last non-diagonal predecessor up to just before
     // the next non-diagonal op on its bits; diagonals on two or more
     // bits also hold later non-diagonal ops on their bits behind them,
-    // which keeps every such range non-empty.  The diagonals are then
+    // which keeps every such range non-empty.  Only the bits an op acts on
+    // (tmask: touched minus control bits) order it against diagonals: a
+    // diagonal commutes with an op that only uses its bits as controls.
+    // The diagonals are then
     // packed onto as few levels as possible (interval point cover,
     // greedy by right end); all diagonals of one level merge into one
     // op placed after that level's non-diagonal ops.
@@ -171,14 +258,14 @@ std::vector<size_t> order_by_levels(const std::vector<size_t> &prims, const std:
     std::vector<int> level(np, 0), dlo(np, 0), dhi(np, 0);
     int maxlv = 0;
     {
-        int ndl[64] = {0}, floor_lv[64] = {0};
+        int ndl[64] = {0}, ndl_t[64] = {0}, floor_lv[64] = {0};
         for (size_t k = 0; k < np; k++) {
             const size_t pi = prims[k];
             const u64 tb = touch[pi];
             int lv = 0;
             if (diag[pi]) {
                 for (u64 r = tb; r; r &= r - 1) {
-                    lv = std::max(lv, ndl[__builtin_ctzll(r)]);
+                    lv = std::max(lv, ndl_t[__builtin_ctzll(r)]);
                 }
                 dlo[k] = lv;
                 if (__builtin_popcountll(tb) >= 2) {
@@ -189,12 +276,17 @@ std::vector<size_t> order_by_levels(const std::vector<size_t> &prims, const std:
                 }
             } else {
                 for (u64 r = tb; r; r &= r - 1) {
-                    const int b = __builtin_ctzll(r);
-                    lv = std::max({lv, ndl[b], floor_lv[b]});
+                    lv = std::max(lv, ndl[__builtin_ctzll(r)]);
+                }
+                for (u64 r = tmask[pi]; r; r &= r - 1) {
+                    lv = std::max(lv, floor_lv[__builtin_ctzll(r)]);
                 }
                 lv += 1;
                 for (u64 r = tb; r; r &= r - 1) {
                     ndl[__builtin_ctzll(r)] = lv;
+                }
+                for (u64 r = tmask[pi]; r; r &= r - 1) {
+                    ndl_t[__builtin_ctzll(r)] = lv;
                 }
                 level[k] = lv;
                 maxlv = std::max(maxlv, lv);
@@ -212,7 +304,7 @@ std::vector<size_t> order_by_levels(const std::vector<size_t> &prims, const std:
                 }
                 dhi[k] = h;
             } else {
-                for (u64 r = tb; r; r &= r - 1) {
+                for (u64 r = tmask[pi]; r; r &= r - 1) {
                     next_lv[__builtin_ctzll(r)] = level[k];
                 }
             }
@@ -439,16 +531,17 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
     const int Lbase = sizeof(T) == 8 ? 4 : 5;
     const int L = std::min(Lbase, tmax);
     const u64 lowmask = (u64{1} << L) - 1;
-    const std::vector<Prim<T>> P = rewrite(in);
+    const std::vector<Prim<T>> P = rewrite(merge1q(in));
     prog->prims = P.size();
 
     // per-primitive properties
     const size_t m = P.size();
-    std::vector<u64> need(m), touch(m);
+    std::vector<u64> need(m), touch(m), tmask(m);
     std::vector<char> diag(m), fusible(m);
     for (size_t i = 0; i < m; i++) {
         const auto &p = P[i];
         touch[i] = p.touched();
+        tmask[i] = touch[i] & ~p.cmask;
         Diag<T> dd;
         const bool isd = to_diag(p, dd) || p.kind == Prim<T>::Parity;
         diag[i] = isd;
@@ -578,7 +671,7 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
                 continue;
             }
             std::vector<int> lv;
-            const std::vector<size_t> ord = order_by_levels(pp.prims, touch, diag, &lv);
+            const std::vector<size_t> ord = order_by_levels(pp.prims, touch, tmask, diag, &lv);
             PassPlan cur;
             cur.fused = true;
             cur.local = pp.local;
@@ -795,7 +888,7 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
             pend.clear();
         };
 
-        const std::vector<size_t> ordered = order_by_levels(pp.prims, touch, diag, nullptr);
+        const std::vector<size_t> ordered = order_by_levels(pp.prims, touch, tmask, diag, nullptr);
         for (size_t pi : ordered) {
             const auto &p = P[pi];
             Diag<T> dg;

@@ -241,6 +241,24 @@ template <class T> void Measure<T>::apply_obs(StateVector<T> &sv, const ObsNode 
     }
 }
 
+template <class T>
+void Measure<T>::apply_obs_into(const StateVector<T> &src, StateVector<T> &dst, const ObsNode &o) {
+    PLGB_REQUIRE(src.num_qubits() == dst.num_qubits(), "observable: register sizes differ");
+    PauliSum ps;
+    if (o.kind != ObsNode::Sparse && o.kind != ObsNode::Herm && compile_pauli(o, src.num_qubits(), ps) &&
+        !ps.terms.empty()) {
+        src.synchronize();
+        const auto groups = group_pauli(ps);
+        for (size_t i = 0; i < groups.size(); i++) {
+            launch_pauli_accumulate<T>(dst.stream(), src.data(), dst.data(), dst.length(), groups[i], i == 0);
+        }
+        dst.synchronize();
+        return;
+    }
+    dst.copy_from(src);
+    apply_obs(dst, o);
+}
+
 // ---------------------------------------------------------------------------
 template <class T>
 std::vector<double> Measure<T>::probs(StateVector<T> &sv, const std::vector<int64_t> &wires, bool all_wires) {

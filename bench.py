@@ -43,13 +43,18 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference", "cpu-sample"])
     ap.add_argument("--qubits", type=int, default=30)
     ap.add_argument("--cycles", type=int, default=20)
     ap.add_argument("--tile-bits", type=int, default=None,
                     help="fixed fused tile size 2^t (0 = unfused); default: chosen during warm-up")
     ap.add_argument("--no-c64", action="store_true", help="skip the complex64 variant")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-circuits leg (config 2)")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the autograd adjoint leg (config 3)")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving leg (config 4)")
+    ap.add_argument("--serve-seconds", type=float, default=2.0,
+                    help="length of the config-4 arrival window replayed by the serving leg")
     return ap.parse_args()
 
 
@@ -217,6 +222,8 @@ def gpu_arm(args) -> dict | None:
     else:
         kernel, tag = "k_1q<double, DENSE> and k_1q<double, NEG1>", "k_1q_dense_c128"
     traffic = traffic_from_profiles(tag)
+    if traffic is not None:  # recorded for a 30-qubit launch; traffic grows with the amplitudes
+        traffic *= float(1 << n) / float(1 << 30)
 
     # expectation value of the 64-term Hamiltonian (one read per flip-mask group)
     H = ops.observables.HamiltonianC128(
@@ -285,7 +292,131 @@ def gpu_arm(args) -> dict | None:
                       "ms_per_step": t64[b64], "tile_bits": b64,
                       "tuning_ms_per_step": {str(k): round(v, 1) for k, v in sorted(t64.items())}}
         del sv64
+    if rank == 0:
+        if not args.no_batch:
+            res["batched"] = {"c128": batched_leg(ops, 128), "c64": batched_leg(ops, 64)}
+        if not args.no_adjoint:
+            res["adjoint"] = adjoint_leg()
+        if not args.no_serve:
+            res["serving"] = serve_leg(args.serve_seconds)
     return res
+
+
+# --------------------------------------------------------------------------- configs 2-4
+def _plain_circuit(ops, packed, r, names, prec):
+    """One circuit of a packed batch through the per-gate binding calls and
+    per-observable expectation values (the plain per-call path)."""
+    SV = ops.StateVectorC128 if prec == 128 else ops.StateVectorC64
+    M = ops.MeasurementsC128 if prec == 128 else ops.MeasurementsC64
+    s = "C128" if prec == 128 else "C64"
+    NO, TP, HA = (getattr(ops.observables, k + s) for k in ("NamedObs", "TensorProdObs", "Hamiltonian"))
+    n = int(packed.num_qubits[r])
+    sv = SV(n)
+    for o in range(int(packed.op_offsets[r]), int(packed.op_offsets[r + 1])):
+        name = names[int(packed.op_codes[o])]
+        w = [int(x) for x in packed.op_wires[o] if x >= 0]
+        getattr(sv, name)(w, False, [float(packed.op_params[o, 0])] if name != "CNOT" else [])
+    m = M(sv)
+    out = []
+    for ob in range(int(packed.obs_offsets[r]), int(packed.obs_offsets[r + 1])):
+        terms, coeffs = [], []
+        for t in range(int(packed.term_offsets[ob]), int(packed.term_offsets[ob + 1])):
+            fac = [NO(nm, [w]) for w in range(n) for nm, arr in (("PauliX", packed.term_x), ("PauliY", packed.term_y),
+                                                                   ("PauliZ", packed.term_z)) if (int(arr[t]) >> w) & 1]
+            terms.append(TP(fac))
+            coeffs.append(float(packed.term_coeffs[t]))
+        out.append(m.expval(HA(coeffs, terms)))
+    return out
+
+
+def batched_leg(ops, prec: int, plain_every: int = 32) -> dict:
+    """Config 2: 4096 circuits through the batch engine (packed host arrays
+    in, expectation values out: compilation, copies and device time all
+    inside the timed region) vs the plain per-call path on every
+    `plain_every`-th circuit."""
+    from lightning_gb300.batch import BatchEngine, gate_codes
+    from lightning_gb300.workloads import config2_packed
+
+    packed = config2_packed(4096, seed=1002)
+    names = {v: k for k, v in gate_codes().items()}
+    eng = BatchEngine(prec)
+    eng.run(packed.select(range(64)))  # warm-up: tile-size autotuning and device arenas
+    t = time.perf_counter()
+    eng.run(packed)
+    dt = time.perf_counter() - t
+    st = eng.stats()
+    lat = np.asarray(st["wave_done_ms"])[np.asarray(st["wave_of"], int)]
+    sample = list(range(0, packed.num_circuits, plain_every))
+    _plain_circuit(ops, packed, sample[0], names, prec)
+    plat = []
+    t = time.perf_counter()
+    for r in sample:
+        t1 = time.perf_counter()
+        _plain_circuit(ops, packed, r, names, prec)
+        plat.append(time.perf_counter() - t1)
+    pdt = time.perf_counter() - t
+    plain = len(sample) / pdt
+    return {"metric": "config2 circuits/s", "value": packed.num_circuits / dt, "unit": "circuits/s",
+            "circuits": packed.num_circuits, "seconds": dt, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "compile_ms": st["compile_ms"], "device_ms": st["device_ms"],
+            "launches": st["launches"], "waves": st["waves"], "tile_bits": st["tile_bits"],
+            "plain": {"value": plain, "unit": "circuits/s", "sample": f"every {plain_every}th circuit "
+                      f"({len(sample)})", "p50_ms": float(np.percentile(plat, 50) * 1e3),
+                      "p99_ms": float(np.percentile(plat, 99) * 1e3)},
+            "speedup_vs_plain": packed.num_circuits / dt / plain}
+
+
+def adjoint_leg(n: int = 28, layers: int = 12) -> dict:
+    """Config 3: <H> of the 200-term Hamiltonian and its gradient in all
+    1008 rotation angles through torch.autograd (checkpointed adjoint)."""
+    import torch
+
+    from lightning_gb300.torch_adjoint import config3_circuit, expval
+
+    circ, theta = config3_circuit(n=n, layers=layers)
+    t = torch.tensor(theta, requires_grad=True)
+    t0 = time.perf_counter()
+    e = expval(t, circ)
+    t1 = time.perf_counter()
+    e.backward()
+    t2 = time.perf_counter()
+    return {"metric": "config3 gradient s", "qubits": n, "params": int(theta.size), "forward_s": t1 - t0,
+            "backward_s": t2 - t1, "params_per_s": theta.size / (t2 - t0), "registers_in_backward": 2,
+            "value": float(e.item())}
+
+
+def serve_leg(seconds: float) -> dict:
+    """Config 4: the Poisson request stream (2000 requests/s, n in 8..26,
+    30 % adjoint) replayed for `seconds`, continuous batching, plus a serial
+    per-request baseline on the first 200 requests."""
+    from lightning_gb300 import lightning_gb300_ops as ops
+    from lightning_gb300.batch import gate_codes
+    from lightning_gb300.serve import Server
+    from lightning_gb300.workloads import config4_packed
+
+    packed, arrival, adjoint = config4_packed(duration=seconds)
+    srv = Server(128)
+    w = np.arange(min(64, packed.num_circuits))
+    srv.run(packed.select(w), arrival[w] - arrival[0], adjoint[w])  # warm-up
+    res = srv.run(packed, arrival, adjoint)
+    out = {"metric": "config4 requests/s", **res.summary(), "window_s": seconds,
+           "offered_per_s": packed.num_circuits / seconds}
+    names = {v: k for k, v in gate_codes().items()}
+    srv.packed, srv.adjoint = packed, adjoint
+    lat = []
+    k = min(200, packed.num_circuits)
+    t = time.perf_counter()
+    for r in range(k):
+        t1 = time.perf_counter()
+        if adjoint[r]:
+            srv.adjoint_one(r)
+        else:
+            _plain_circuit(ops, packed, r, names, 128)
+        lat.append(time.perf_counter() - t1)
+    out["serial"] = {"value": k / (time.perf_counter() - t), "unit": "requests/s", "sample": f"first {k} requests",
+                     "service_p50_ms": float(np.percentile(lat, 50) * 1e3),
+                     "service_p99_ms": float(np.percentile(lat, 99) * 1e3)}
+    return out
 
 
 # --------------------------------------------------------------------------- CPU legs
@@ -355,14 +486,21 @@ def main():
         reference_arm(args)
         return
     ws, rank, _ = dist_info()
-    cpu = None
-    if rank == 0 and not args.no_cpu:
+    if args.impl == "cpu-sample":
+        # child process of the CPU baseline: OpenMP thread binding stays out
+        # of the GPU process (its host threads compile circuits in parallel)
         orc = cpu_setup()
         n_cpu = min(args.qubits, 28)
         b, t, ng, threads = cpu_sample(orc, n_cpu)
-        cpu = {"value": b / t / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"first cycle of the config-1 circuit ({ng} gates) at {n_cpu} qubits complex128, "
-                         f"{t:.1f} s; LM-kernel restatement with OpenMP on the host cores"}
+        print(json.dumps({"value": b / t / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+                          "sample": f"first cycle of the config-1 circuit ({ng} gates) at {n_cpu} qubits "
+                                    f"complex128, {t:.1f} s; LM-kernel restatement with OpenMP on the host cores"}))
+        return
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        out = subprocess.run([sys.executable, str(Path(__file__).resolve()), "--impl", "cpu-sample", "--qubits",
+                              str(args.qubits)], capture_output=True, text=True, check=True)
+        cpu = json.loads(out.stdout.strip().splitlines()[-1])
     res = gpu_arm(args)
     if rank == 0 and res is not None:
         res["cpu_baseline"] = cpu

@@ -132,12 +132,21 @@ std::vector<double> Adjoint<T>::jacobian(StateVector<T> &sv, const std::vector<O
         Measure<T>::apply_obs_into(lambda, *hl.back(), *obs[h]);
     }
     std::unique_ptr<StateVector<T>> mu;
+    // Pauli-generator results stay on the device (two doubles per
+    // [param][obs]); one copy at the end instead of a sync per parameter
+    double *d_res = nullptr;
+    cuda_check(cudaMalloc(&d_res, 2 * nobs * ntp * sizeof(double)), "cudaMalloc(adjoint results)");
+    struct ResGuard {
+        double *p;
+        ~ResGuard() { cudaFree(p); }
+    } res_guard{d_res};
+    std::vector<char> on_device(nobs * ntp, 0);
+    std::vector<double> dev_scale(nobs * ntp, 0.0);
 
     size_t tp_num = ntp - 1;
     size_t cur = num_param_ops - 1;
     auto tp_it = tp.rbegin();
     double *red = lambda.scratch_red();
-    double *res = red + 2 * kReduceBlocks;
     for (long op_idx = static_cast<long>(ops.size()) - 1; op_idx >= 0; op_idx--) {
         const auto &op = ops[static_cast<size_t>(op_idx)];
         PLGB_REQUIRE(op.params.size() <= 1, "The operation is not supported using the adjoint differentiation method");
@@ -153,12 +162,12 @@ std::vector<double> Adjoint<T>::jacobian(StateVector<T> &sv, const std::vector<O
                 if (pg) {
                     const double scale = pg->scale * (op.inverse ? -1.0 : 1.0);
                     for (size_t h = 0; h < nobs; h++) {
+                        const size_t slot = tp_num * nobs + h;
                         reduce_pauli_transition<T>(lambda.stream(), hl[h]->data(), lambda.data(), lambda.length(),
-                                                   pg->x, pg->yz, pg->ny4, pg->pmask, pg->pval, red, res);
-                        cuda_check(cudaMemcpyAsync(lambda.host_out(), res, 2 * sizeof(double),
-                                                   cudaMemcpyDeviceToHost, lambda.stream()), "D2H");
-                        lambda.synchronize();
-                        jac[tp_num * nobs + h] = -2.0 * scale * lambda.host_out()[1];
+                                                   pg->x, pg->yz, pg->ny4, pg->pmask, pg->pval, red,
+                                                   d_res + 2 * slot);
+                        on_device[slot] = 1;
+                        dev_scale[slot] = -2.0 * scale;
                     }
                 } else {
                     if (!mu) {
@@ -181,6 +190,17 @@ std::vector<double> Adjoint<T>::jacobian(StateVector<T> &sv, const std::vector<O
         lambda.apply_op(op, !op.inverse);
         for (size_t h = 0; h < nobs; h++) {
             hl[h]->apply_op(op, !op.inverse);
+        }
+    }
+    {
+        std::vector<double> r(2 * nobs * ntp);
+        cuda_check(cudaMemcpyAsync(r.data(), d_res, r.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                   lambda.stream()), "D2H");
+        lambda.synchronize();
+        for (size_t k = 0; k < nobs * ntp; k++) {
+            if (on_device[k]) {
+                jac[k] = dev_scale[k] * r[2 * k + 1];
+            }
         }
     }
     // Transpose [param][obs] -> [obs][param] (AdjointJacobianLQubit.hpp:487-490)

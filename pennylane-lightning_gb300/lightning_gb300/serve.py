@@ -1,0 +1,269 @@
+"""Continuous-batching request server on one GB300.
+
+Requests (a circuit from |0..0>, a Pauli-sum Hamiltonian, optionally the
+adjoint Jacobian of <H> with respect to every gate parameter) arrive over
+time.  The server keeps a device-memory budget (2^n amplitudes per forward
+request, three registers per adjoint request, 150 GB by default) and several
+lanes, each a host thread with its own CUDA stream, that pull from their
+queues independently, so work of different lanes overlaps on the device:
+
+* two forward lanes (registers below / from `big_qubits`): every pass of the
+  lane takes ALL queued requests the budget admits (requests that arrived
+  while the previous batch was on the GPU join here) and runs them as one
+  batch of the batch engine;
+* `adjoint_lanes` adjoint lanes: fused forward pass, <H>, then the in-place
+  adjoint sweep, one request at a time per lane.
+
+Results of a request do not depend on what else is in flight: a forward
+request's value is bit-identical to running it alone in a batch engine with
+the same tile size, and an adjoint request runs exactly as it would alone.
+"""
+from __future__ import annotations
+
+import collections
+import ctypes as C
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import lightning_gb300_ops as ops
+from ._capi import VP, call
+from .batch import BatchEngine, PackedBatch, gate_codes
+
+
+class MemoryBudget:
+    def __init__(self, nbytes: int):
+        self.free = int(nbytes)
+        self.total = int(nbytes)
+        self.cv = threading.Condition()
+
+    def acquire(self, nbytes: int, block: bool = True) -> bool:
+        with self.cv:
+            if nbytes > self.total:
+                raise ValueError(f"request needs {nbytes} bytes, more than the whole budget {self.total}")
+            while self.free < nbytes:
+                if not block:
+                    return False
+                self.cv.wait()
+            self.free -= nbytes
+            return True
+
+    def release(self, nbytes: int):
+        with self.cv:
+            self.free += nbytes
+            self.cv.notify_all()
+
+
+@dataclass
+class ServeResult:
+    values: np.ndarray   # <H> per request
+    jacobians: dict      # request -> d<H>/d(parameter of each rotation), adjoint requests
+    arrival: np.ndarray  # seconds from the start
+    start: np.ndarray    # seconds from the start when the request's batch began
+    done: np.ndarray     # seconds from the start when its result was ready
+    lane: np.ndarray     # lane index that served it
+    batches: list = field(default_factory=list)  # (lane, size, seconds) per batch
+
+    @property
+    def latency(self) -> np.ndarray:
+        return self.done - self.arrival
+
+    def summary(self) -> dict:
+        lat = self.latency
+        span = float(self.done.max() - self.arrival.min()) if lat.size else 0.0
+        return {"requests": int(lat.size), "throughput_per_s": lat.size / span if span > 0 else 0.0,
+                "p50_ms": float(np.percentile(lat, 50) * 1e3) if lat.size else None,
+                "p99_ms": float(np.percentile(lat, 99) * 1e3) if lat.size else None,
+                "mean_batch": float(np.mean([b[1] for b in self.batches])) if self.batches else 0.0,
+                "batches": len(self.batches), "span_s": span}
+
+
+class Server:
+    def __init__(self, precision: int = 128, budget_bytes: float = 150e9, big_qubits: int = 20,
+                 adjoint_lanes: int = 4, max_batch: int = 4096, tile_bits: int = 11):
+        self.precision = int(precision)
+        self.S = 16 if self.precision == 128 else 8
+        self.budget = MemoryBudget(int(budget_bytes))
+        self.big = int(big_qubits)
+        self.max_batch = int(max_batch)
+        self.tile_bits = int(tile_bits)
+        self.adjoint_lanes = int(adjoint_lanes)
+        # forward lanes keep their engines (device arenas, tuned tile sizes)
+        self.engines = [BatchEngine(self.precision, wave_bytes=int(budget_bytes)),
+                        BatchEngine(self.precision, wave_bytes=int(budget_bytes))]
+        self._names = {v: k for k, v in gate_codes().items()}
+
+    # ---------------------------------------------------------------- helpers
+    def _bytes(self, r: int) -> int:
+        n = max(int(self.packed.num_qubits[r]), 9)
+        return (1 << n) * self.S * (3 if self.adjoint[r] else 1)
+
+    def _ops_struct(self, r: int):
+        p = self.packed
+        o0, o1 = int(p.op_offsets[r]), int(p.op_offsets[r + 1])
+        names = [self._names[int(c)] for c in p.op_codes[o0:o1]]
+        wires = [[int(x) for x in w if x >= 0] for w in p.op_wires[o0:o1]]
+        params = [[float(v)] if nm in _ONE_PARAM else [] for nm, v in zip(names, p.op_params[o0:o1, 0])]
+        OS = ops.OpsStructC128 if self.precision == 128 else ops.OpsStructC64
+        return OS(names, params, wires, [bool(x) for x in p.op_inverse[o0:o1]], [None] * len(names))
+
+    def _hamiltonian(self, r: int):
+        p = self.packed
+        s = "C128" if self.precision == 128 else "C64"
+        NO = getattr(ops.observables, "NamedObs" + s)
+        TP = getattr(ops.observables, "TensorProdObs" + s)
+        HA = getattr(ops.observables, "Hamiltonian" + s)
+        t0, t1 = int(p.term_offsets[r]), int(p.term_offsets[r + 1])
+        n = int(p.num_qubits[r])
+        terms = []
+        for t in range(t0, t1):
+            fac = []
+            for w in range(n):
+                for letter, arr in (("PauliX", p.term_x), ("PauliY", p.term_y), ("PauliZ", p.term_z)):
+                    if (int(arr[t]) >> w) & 1:
+                        fac.append(NO(letter, [w]))
+            terms.append(TP(fac) if fac else NO("Identity", [0]))
+        return HA([float(c) for c in p.term_coeffs[t0:t1]], terms)
+
+    def adjoint_one(self, r: int):
+        """<H> and its Jacobian for request r, exactly as run alone."""
+        n = int(self.packed.num_qubits[r])
+        SV = ops.StateVectorC128 if self.precision == 128 else ops.StateVectorC64
+        M = ops.MeasurementsC128 if self.precision == 128 else ops.MeasurementsC64
+        S = self._ops_struct(r)
+        H = self._hamiltonian(r)
+        sv = SV(n)
+        sv.applyOperations(S, min(self.tile_bits, n))
+        value = float(M(sv).expval(H))
+        npar = sum(1 for p in S.params if p)
+        jac = np.zeros(max(1, npar), np.float64)
+        tp = np.arange(npar, dtype=np.int64)
+        arr = (VP * 1)(H._h)
+        call("plgb_adjoint_jacobian_inplace", sv._h, arr, 1, S._h, tp.ctypes.data_as(C.POINTER(C.c_int64)), npar,
+             jac.ctypes.data_as(C.POINTER(C.c_double)))
+        return value, jac[:npar]
+
+    # ------------------------------------------------------------------- run
+    def run(self, packed: PackedBatch, arrival: np.ndarray, adjoint: np.ndarray, speed: float = 1.0) -> ServeResult:
+        """Replay the arrival schedule in real time (divided by `speed`) and
+        serve every request; returns per-request results and timings."""
+        self.packed, self.adjoint = packed, np.asarray(adjoint, bool)
+        R = packed.num_circuits
+        values = np.full(R, np.nan)
+        jacs: dict = {}
+        start = np.zeros(R)
+        done = np.zeros(R)
+        lane_of = np.zeros(R, np.int32)
+        batches: list = []
+        lock = threading.Lock()
+        nl = 2 + self.adjoint_lanes
+        queues = [collections.deque() for _ in range(nl)]
+        cvs = [threading.Condition() for _ in range(nl)]
+        closing = threading.Event()
+        errors: list = []
+        t0 = time.perf_counter()
+
+        def now():
+            return time.perf_counter() - t0
+
+        def take(li, limit):
+            """Block for the first queued request of lane li, then take every
+            queued request the budget admits, up to `limit`."""
+            with cvs[li]:
+                while not queues[li]:
+                    if closing.is_set():
+                        return []
+                    cvs[li].wait(0.05)
+                first = queues[li][0]
+            self.budget.acquire(self._bytes(first))
+            got = [first]
+            with cvs[li]:
+                queues[li].popleft()
+                while queues[li] and len(got) < limit:
+                    r = queues[li][0]
+                    if not self.budget.acquire(self._bytes(r), block=False):
+                        break
+                    got.append(queues[li].popleft())
+            return got
+
+        def forward_lane(li):
+            eng = self.engines[li]
+            try:
+                while True:
+                    got = take(li, self.max_batch)
+                    if not got:
+                        return
+                    ts = now()
+                    vals = eng.run(packed.select(got))
+                    te = now()
+                    for r in got:
+                        self.budget.release(self._bytes(r))
+                    with lock:
+                        for k, r in enumerate(got):
+                            values[r] = vals[k]
+                            start[r], done[r], lane_of[r] = ts, te, li
+                        batches.append((li, len(got), te - ts))
+            except Exception as e:  # surfaced after the run
+                errors.append(e)
+                closing.set()
+
+        def adjoint_lane(li):
+            try:
+                while True:
+                    got = take(li, 1)
+                    if not got:
+                        return
+                    r = got[0]
+                    ts = now()
+                    v, j = self.adjoint_one(r)
+                    te = now()
+                    self.budget.release(self._bytes(r))
+                    with lock:
+                        values[r], jacs[r] = v, j
+                        start[r], done[r], lane_of[r] = ts, te, li
+                        batches.append((li, 1, te - ts))
+            except Exception as e:
+                errors.append(e)
+                closing.set()
+
+        threads = [threading.Thread(target=forward_lane, args=(0,), daemon=True),
+                   threading.Thread(target=forward_lane, args=(1,), daemon=True)]
+        threads += [threading.Thread(target=adjoint_lane, args=(2 + k,), daemon=True)
+                    for k in range(self.adjoint_lanes)]
+        for th in threads:
+            th.start()
+        rr = 0  # round robin over the adjoint lanes
+        for r in range(R):
+            if errors:
+                break
+            wait = arrival[r] / speed - now()
+            if wait > 0:
+                time.sleep(wait)
+            if self.adjoint[r]:
+                li = 2 + rr
+                rr = (rr + 1) % self.adjoint_lanes
+            else:
+                li = 1 if packed.num_qubits[r] >= self.big else 0
+            with cvs[li]:
+                queues[li].append(r)
+                cvs[li].notify()
+        # drain
+        while not errors:
+            with lock:
+                finished = int(np.count_nonzero(done > 0))
+            if finished == R:
+                break
+            time.sleep(0.01)
+        closing.set()
+        for th in threads:
+            th.join()
+        if errors:
+            raise errors[0]
+        return ServeResult(values, jacs, np.asarray(arrival, float) / speed, start, done, lane_of, batches)
+
+
+_ONE_PARAM = {"PhaseShift", "RX", "RY", "RZ", "IsingXX", "IsingXY", "IsingYY", "IsingZZ", "ControlledPhaseShift",
+              "CRX", "CRY", "CRZ", "SingleExcitation", "SingleExcitationMinus", "SingleExcitationPlus", "PSWAP",
+              "DoubleExcitation", "DoubleExcitationMinus", "DoubleExcitationPlus", "MultiRZ", "GlobalPhase"}

@@ -221,22 +221,109 @@ class Request:
     adjoint: bool
 
 
-def config4(rate: float = 2000.0, duration: float = 60.0, seed: int = 1004) -> list[Request]:
+def config4_packed(rate: float = 2000.0, duration: float = 60.0, seed: int = 1004, n_max: int = 26):
+    """The request stream in the batch engine's packed layout, generated
+    with array operations.  Returns (packed, arrival seconds, adjoint flags):
+    request r is circuit r of `packed` with one observable, its Hamiltonian.
+
+    Per request: Poisson arrival at `rate`; n in 8..26 with P(n) ~ 2^(-n/4);
+    a config-0 body of depth U{2..12}; a Hamiltonian of U{1..32} Pauli terms
+    of weight U{1..min(4, n)} on distinct wires, letters U{X, Y, Z},
+    coefficients N(0, 1); 30 % of the requests ask for the adjoint Jacobian."""
+    from .batch import MAX_WIRES_PER_OP, PackedBatch, code_of
+
     rng = np.random.default_rng(seed)
-    ns = np.arange(8, 27)
-    pn = 2.0 ** (-ns / 4.0)
+    expect = int(rate * duration * 1.2) + 64
+    gaps = rng.exponential(1.0 / rate, size=expect)
+    arrival = np.cumsum(gaps)
+    arrival = arrival[arrival < duration]
+    R = arrival.size
+    ns_all = np.arange(8, 27)
+    pn = 2.0 ** (-ns_all / 4.0)
     pn /= pn.sum()
-    t = 0.0
+    ns = np.minimum(rng.choice(ns_all, size=R, p=pn), n_max).astype(np.int32)
+    depth = rng.integers(2, 13, size=R)
+    seeds = rng.integers(0, 2**31 - 1, size=R)
+    nterms = rng.integers(1, 33, size=R)
+    adjoint = rng.random(R) < 0.3
+
+    rx, ry, rz, cnot = code_of("RX"), code_of("RY"), code_of("RZ"), code_of("CNOT")
+    nops = (4 * ns * depth).astype(np.int64)
+    op_off = np.concatenate([[0], np.cumsum(nops)]).astype(np.int64)
+    M = int(op_off[-1])
+    codes = np.empty(M, np.int32)
+    wires = np.full((M, MAX_WIRES_PER_OP), -1, np.int32)
+    params = np.zeros((M, 3), np.float64)
+    # layout of a layer of an n-qubit body: 3n rotations (RX, RY, RZ per
+    # wire) then n CNOTs; build one template per n and tile it
+    tmpl = {}
+    for n in range(8, 27):
+        q = np.arange(n, dtype=np.int32)
+        c = np.concatenate([np.tile(np.array([rx, ry, rz], np.int32), n), np.full(n, cnot, np.int32)])
+        w = np.full((4 * n, MAX_WIRES_PER_OP), -1, np.int32)
+        w[:3 * n, 0] = np.repeat(q, 3)
+        w[3 * n:, 0] = q
+        w[3 * n:, 1] = (q + 1) % n
+        tmpl[n] = (c, w)
+    term_off = np.concatenate([[0], np.cumsum(nterms)]).astype(np.int64)
+    T = int(term_off[-1])
+    coeffs = np.empty(T, np.float64)
+    tx = np.zeros(T, np.uint64)
+    ty = np.zeros(T, np.uint64)
+    tz = np.zeros(T, np.uint64)
+    for r in range(R):
+        n, d = int(ns[r]), int(depth[r])
+        c, w = tmpl[n]
+        o0, o1 = int(op_off[r]), int(op_off[r + 1])
+        codes[o0:o1] = np.tile(c, d)
+        wires[o0:o1] = np.tile(w, (d, 1))
+        sub = np.random.default_rng(int(seeds[r]))
+        ang = sub.uniform(0.0, TWO_PI, size=(d, n, 3))
+        p = params[o0:o1].reshape(d, 4 * n, 3)
+        p[:, :3 * n, 0] = ang.reshape(d, 3 * n)
+        k = int(nterms[r])
+        wmax = min(4, n)
+        wt = sub.integers(1, wmax + 1, size=k)
+        perm = np.argsort(sub.random((k, n)), axis=1)[:, :wmax]
+        letters = sub.integers(0, 3, size=(k, wmax))
+        t0 = int(term_off[r])
+        coeffs[t0:t0 + k] = sub.normal(size=k)
+        bits = np.left_shift(np.uint64(1), perm.astype(np.uint64))
+        live = np.arange(wmax)[None, :] < wt[:, None]
+        for L, arr in ((0, tx), (1, ty), (2, tz)):
+            sel = live & (letters == L)
+            arr[t0:t0 + k] = np.bitwise_or.reduce(np.where(sel, bits, np.uint64(0)), axis=1)
+    packed = PackedBatch(ns, op_off, codes, wires, params, np.zeros(M, np.uint8),
+                         np.arange(R + 1, dtype=np.int64), term_off, coeffs, tx, ty, tz)
+    return packed, arrival, adjoint
+
+
+def config4(rate: float = 2000.0, duration: float = 60.0, seed: int = 1004, n_max: int = 26) -> list[Request]:
+    """config4_packed as Request objects (for small streams)."""
+    from .batch import gate_codes
+
+    packed, arrival, adjoint = config4_packed(rate, duration, seed, n_max)
+    names = {v: k for k, v in gate_codes().items()}
     reqs = []
-    rid = 0
-    while True:
-        t += float(rng.exponential(1.0 / rate))
-        if t >= duration:
-            break
-        n = int(rng.choice(ns, p=pn))
-        depth = int(rng.integers(2, 13))
-        body = config0(n, depth, seed=int(rng.integers(0, 2**31 - 1)))
-        ham = random_pauli_sum(rng, n, int(rng.integers(1, 33)))
-        reqs.append(Request(rid, t, n, body, ham, bool(rng.random() < 0.3)))
-        rid += 1
+    for r in range(packed.num_circuits):
+        o0, o1 = int(packed.op_offsets[r]), int(packed.op_offsets[r + 1])
+        ops = []
+        for o in range(o0, o1):
+            name = names[int(packed.op_codes[o])]
+            ws = [int(x) for x in packed.op_wires[o] if x >= 0]
+            ops.append(Op(name, ws, [float(packed.op_params[o, 0])] if name != "CNOT" else []))
+        t0, t1 = int(packed.term_offsets[r]), int(packed.term_offsets[r + 1])
+        coeffs, words, wires = [], [], []
+        for t in range(t0, t1):
+            word, ws = [], []
+            for w in range(int(packed.num_qubits[r])):
+                for letter, arr in (("X", packed.term_x), ("Y", packed.term_y), ("Z", packed.term_z)):
+                    if (int(arr[t]) >> w) & 1:
+                        word.append(letter)
+                        ws.append(w)
+            coeffs.append(float(packed.term_coeffs[t]))
+            words.append("".join(word))
+            wires.append(ws)
+        reqs.append(Request(r, float(arrival[r]), int(packed.num_qubits[r]), ops, PauliSum(coeffs, words, wires),
+                            bool(adjoint[r])))
     return reqs

@@ -15,7 +15,9 @@ enum TileKind : int {
     TK_DENSE2 = 2,  // dense 4x4 on two local bits
     TK_DIAGTAB = 3, // merged diagonal: local table x global scalar x local/global sign flips
     TK_PARITY = 4,  // parity phase on the full index (MultiRZ and its generator)
+    TK_REDUCE = 5,  // adjoint sweep: Im <b| P G |a> over the tile into a parameter slot
 };
+constexpr int kMaxReducePerPass = 64; // reduction slots accumulated per CTA and pass
 
 constexpr int kRegBits = 4;              // amplitudes per thread in register stages: 2^4
 constexpr int kMinRegTileBits = 9;       // register kernel needs >= 32 threads
@@ -32,6 +34,7 @@ struct TilePassDesc {
     // register-blocked execution (t >= kMinRegTileBits): stages over the op list
     int stage_begin, nstages;
     int ndiag;      // merged-diagonal ops in the pass (prologue slots)
+    int rslot_begin, nrslots; // reductions of the pass (adjoint programs): count in nrslots
 };
 
 // A stage of a register-blocked pass.  REG: ops [op_begin, op_begin+nops)
@@ -66,6 +69,11 @@ template <class T> struct TileOp {
     int rk{0};
     u32 rcmask{0}, rcval{0}, tcmask{0}, tcval{0};
     int diag_slot{0};
+    // TK_REDUCE: lo1 = local flip mask, pmask = Y|Z mask, cmask/cval =
+    // projector, mode = number of Y mod 4, result slot, and the square of
+    // the rotation scales deferred to the store at this point
+    int rslot{0};
+    double rmul{1.0};
     cx<T> m[16]{};
 };
 
@@ -82,6 +90,14 @@ template <class T> struct DiagForm {
 template <class T>
 void launch_tile_pass(cudaStream_t s, cx<T> *sv, const TilePassDesc &d, const TileOp<T> *ops, const DiagForm<T> *forms,
                       const cx<T> *tables);
+// Adjoint sweep: the pass applied to two registers (lambda and H lambda),
+// with its TK_REDUCE ops accumulated into partials[slot * G + CTA].
+template <class T>
+void launch_tile_pass_adj(cudaStream_t s, cx<T> *lam, cx<T> *hlam, const TilePassDesc &d, const TileOp<T> *ops,
+                          const DiagForm<T> *forms, const cx<T> *tables, double *partials, int G);
+int adj_grid_capacity(size_t tile_bytes_each);
+void launch_adj_sum(cudaStream_t s, const double *partials, int nslots, int G, double *out);
+
 template <class T>
 void launch_tile_pass_reg(cudaStream_t s, cx<T> *sv, const TilePassDesc &d, const TileOp<T> *ops,
                           const DiagForm<T> *forms, const cx<T> *tables, const StageDesc *stages);

@@ -84,7 +84,7 @@ inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 // launches one kernel per primitive; the fusion engine (host_fusion.cpp)
 // schedules primitives into shared-memory tile passes.
 template <class T> struct Prim {
-    enum Kind : int { Pair, Dense2, DenseK, DiagK, Parity, Scale, PauliRot, ZeroOut };
+    enum Kind : int { Pair, Dense2, DenseK, DiagK, Parity, Scale, PauliRot, ZeroOut, Reduce };
     Kind kind{Pair};
     int mode{0};              // Pair: Mode1
     std::vector<int> tbits;   // target bit positions (first = MSB of the local index)
@@ -95,6 +95,11 @@ template <class T> struct Prim {
     u64 pmask{0}, my{0}, mz{0}; // Parity mask; PauliRot x|y mask, y mask, z mask
     T c{0};                   // PauliRot cosine
     bool zero_outside{false};
+    // Reduce (adjoint sweep): Im <H lambda| P G |lambda> into slot rslot, G
+    // the Pauli word with flip mask rx, Y|Z mask ryz, ny4 Ys mod 4, P the
+    // projector (index & rpm) == rpv
+    u64 rx{0}, ryz{0}, rpm{0}, rpv{0};
+    int rny4{0}, rslot{-1};
     u64 touched() const;      // every bit the primitive reads or writes
     bool diagonal() const;    // multiplies each amplitude by a factor (no mixing)
 };
@@ -203,6 +208,11 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
 // JSON description of a compiled program's passes (plan introspection)
 template <class T> std::string fused_plan_json(const FusedProgram<T> &prog);
 template <class T> void run_fused(StateVector<T> &sv, const FusedProgram<T> &prog);
+// An adjoint program (with Reduce primitives) on lambda and H lambda (same
+// stream); reductions land in partials[slot * G + CTA].
+template <class T>
+void run_fused_adjoint(StateVector<T> &lam, StateVector<T> &hlam, const FusedProgram<T> &prog, double *partials,
+                       int G);
 struct FusedStats {
     size_t passes, unfused, prims;
 };
@@ -253,8 +263,12 @@ template <class T> struct Adjoint {
     // consume: sv already holds the final state and may be overwritten; the
     // sweep then runs in place on it (registers needed: 1 + observables for
     // Pauli-sum observables and Pauli-word generators, instead of 2 + 2x)
+    // fused_tile_bits > 0: for one observable and Pauli-word generators the
+    // backward sweep runs as fused two-register tile passes with the
+    // reductions inside (kernels_adjoint.cu); otherwise op by op.
     static std::vector<double> jacobian(StateVector<T> &sv, const std::vector<ObsPtr> &obs, const OpsList &ops,
-                                        const std::vector<int64_t> &trainable, bool apply_ops, bool consume = false);
+                                        const std::vector<int64_t> &trainable, bool apply_ops, bool consume = false,
+                                        int fused_tile_bits = 11);
 };
 
 // ---------------------------------------------------------------------------

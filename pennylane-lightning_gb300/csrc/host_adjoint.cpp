@@ -14,6 +14,7 @@
 //     controlled forms) Im<H lambda| G |lambda> is evaluated by one transition
 //     kernel that reads both states once, instead of copy + apply + dot;
 //   * other generators take the reference's route through a scratch state mu.
+#include "fusion.hpp"
 #include "host.hpp"
 
 #include <algorithm>
@@ -100,7 +101,8 @@ std::optional<PauliGen> pauli_generator(const OpRec &op, int n) {
 
 template <class T>
 std::vector<double> Adjoint<T>::jacobian(StateVector<T> &sv, const std::vector<ObsPtr> &obs, const OpsList &opsl,
-                                         const std::vector<int64_t> &tp, bool apply_ops, bool consume) {
+                                         const std::vector<int64_t> &tp, bool apply_ops, bool consume,
+                                         int fused_tile_bits) {
     const auto &ops = opsl.ops;
     const size_t nobs = obs.size();
     const size_t ntp = tp.size();
@@ -131,6 +133,82 @@ std::vector<double> Adjoint<T>::jacobian(StateVector<T> &sv, const std::vector<O
         hl.emplace_back(std::make_unique<StateVector<T>>(n, lambda.stream()));
         Measure<T>::apply_obs_into(lambda, *hl.back(), *obs[h]);
     }
+    // ---- fused sweep: the reverse program (reduction, then U^dagger, per
+    // operation, last to first) compiled into two-register tile passes
+    if (fused_tile_bits > 0 && nobs == 1) {
+        std::vector<Prim<T>> prims;
+        std::vector<double> slot_scale(ntp, 0.0);
+        bool ok = true;
+        size_t tpn = ntp - 1;
+        size_t curp = num_param_ops - 1;
+        auto it = tp.rbegin();
+        for (long op_idx = static_cast<long>(ops.size()) - 1; op_idx >= 0 && ok; op_idx--) {
+            const auto &op = ops[static_cast<size_t>(op_idx)];
+            PLGB_REQUIRE(op.params.size() <= 1,
+                         "The operation is not supported using the adjoint differentiation method");
+            if (op.name == "StatePrep" || op.name == "BasisState") {
+                continue;
+            }
+            if (it == tp.rend()) {
+                break;
+            }
+            if (!op.params.empty()) {
+                if (static_cast<int64_t>(curp) == *it) {
+                    const auto pg = pauli_generator(op, n);
+                    if (!pg) {
+                        ok = false;
+                        break;
+                    }
+                    Prim<T> r;
+                    r.kind = Prim<T>::Reduce;
+                    r.rx = pg->x;
+                    r.ryz = pg->yz;
+                    r.rny4 = pg->ny4;
+                    r.rpm = pg->pmask;
+                    r.rpv = pg->pval;
+                    r.rslot = static_cast<int>(tpn);
+                    slot_scale[tpn] = -2.0 * pg->scale * (op.inverse ? -1.0 : 1.0);
+                    prims.push_back(std::move(r));
+                    tpn--;
+                    ++it;
+                }
+                curp--;
+            }
+            auto p = lambda.lower_op(op, !op.inverse);
+            prims.insert(prims.end(), std::make_move_iterator(p.begin()), std::make_move_iterator(p.end()));
+        }
+        if (ok) {
+            // two tiles of 2^t amplitudes per CTA must fit 200 KiB of shared memory
+            const int tmax = sizeof(T) == 8 ? 12 : 13;
+            const int t = std::max(1, std::min({fused_tile_bits, n, tmax}));
+            auto prog = compile_fused<T>(n, prims, t, true);
+            const int G = adj_grid_capacity(sizeof(cx<T>) << t);
+            double *d_part = nullptr;
+            cuda_check(cudaMalloc(&d_part, (static_cast<size_t>(G) + 1) * ntp * sizeof(double)),
+                       "cudaMalloc(adjoint partials)");
+            struct Guard {
+                double *p;
+                ~Guard() { cudaFree(p); }
+            } guard{d_part};
+            double *d_out = d_part + static_cast<size_t>(G) * ntp;
+            cuda_check(cudaMemsetAsync(d_part, 0, static_cast<size_t>(G) * ntp * sizeof(double), lambda.stream()),
+                       "memset");
+            run_fused_adjoint<T>(lambda, *hl[0], *prog, d_part, G);
+            launch_adj_sum(lambda.stream(), d_part, static_cast<int>(ntp), G, d_out);
+            std::vector<double> r(ntp);
+            cuda_check(cudaMemcpyAsync(r.data(), d_out, ntp * sizeof(double), cudaMemcpyDeviceToHost,
+                                       lambda.stream()), "D2H");
+            lambda.synchronize();
+            std::vector<double> out(ntp);
+            for (size_t p = 0; p < ntp; p++) {
+                out[p] = static_cast<double>(static_cast<T>(slot_scale[p] * r[p]));
+            }
+            return out;
+        }
+        // a generator that is not a Pauli word: the op-by-op sweep below
+        // starts from the untouched registers
+    }
+
     std::unique_ptr<StateVector<T>> mu;
     // Pauli-generator results stay on the device (two doubles per
     // [param][obs]); one copy at the end instead of a sync per parameter

@@ -365,6 +365,11 @@ bool plan_stages(std::vector<TileOp<T>> &ops, const std::vector<DiagForm<T>> &fo
     if (d.t < kMinRegTileBits || d.t > 12) { // 2^(t-4) <= 256 threads
         return false;
     }
+    for (int i = d.op_begin; i < d.op_begin + d.nops; i++) {
+        if (ops[static_cast<size_t>(i)].kind == TK_REDUCE) {
+            return false; // adjoint passes run on the two-register kernel
+        }
+    }
     const int begin = d.op_begin, end = d.op_begin + d.nops;
     auto single_target = [&](const TileOp<T> &op, int &q) {
         if ((op.kind != TK_PAIR && op.kind != TK_SROT) || op.lo0 != 0 || __builtin_popcount(op.lo1) != 1) {
@@ -551,9 +556,14 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
                 nb |= u64{1} << b;
             }
         }
+        if (p.kind == Prim<T>::Reduce) {
+            nb = p.rx; // the flip bits must be local; Y|Z and projector bits may be global
+        }
         need[i] = nb;
         bool ok = false;
-        if (p.kind == Prim<T>::Pair || p.kind == Prim<T>::Dense2) {
+        if (p.kind == Prim<T>::Reduce) {
+            ok = __builtin_popcountll(nb | lowmask) <= tmax;
+        } else if (p.kind == Prim<T>::Pair || p.kind == Prim<T>::Dense2) {
             ok = __builtin_popcountll(nb | lowmask) <= tmax && p.tbits.size() <= 12;
         } else if (p.kind == Prim<T>::Parity) {
             ok = true;
@@ -675,20 +685,24 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
             PassPlan cur;
             cur.fused = true;
             cur.local = pp.local;
-            int ndl = 0, last_dl = -1;
+            int ndl = 0, last_dl = -1, nred = 0;
             for (size_t k = 0; k < ord.size(); k++) {
                 const bool dg = diag[ord[k]] != 0;
+                const bool rd = P[ord[k]].kind == Prim<T>::Reduce;
+                if ((dg && lv[k] != last_dl && ndl == kDiagLevelsPerPass) || (rd && nred == kMaxReducePerPass)) {
+                    split.push_back(std::move(cur));
+                    cur = PassPlan{};
+                    cur.fused = true;
+                    cur.local = pp.local;
+                    ndl = 0;
+                    nred = 0;
+                    last_dl = -1;
+                }
                 if (dg && lv[k] != last_dl) {
-                    if (ndl == kDiagLevelsPerPass) {
-                        split.push_back(std::move(cur));
-                        cur = PassPlan{};
-                        cur.fused = true;
-                        cur.local = pp.local;
-                        ndl = 0;
-                    }
                     ndl++;
                     last_dl = lv[k];
                 }
+                nred += rd ? 1 : 0;
                 cur.prims.push_back(ord[k]);
             }
             if (!cur.prims.empty()) {
@@ -737,6 +751,8 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
         d.ntiles = u64{1} << (n - d.t);
         d.op_begin = static_cast<int>(ops.size());
         d.pass_scale = 1.0;
+        d.rslot_begin = 0;
+        d.nrslots = 0;
         auto lpos = [&](int b) -> int {
             if (b < L) {
                 return b;
@@ -896,6 +912,33 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
                 pend.push_back(std::move(dg));
                 continue;
             }
+            if (p.kind == Prim<T>::Reduce) {
+                flush(); // diagonals before the reduction point apply first
+                TileOp<T> o;
+                o.kind = TK_REDUCE;
+                o.lo1 = local_mask(p.rx);   // flip bits (all local)
+                o.lo0 = local_mask(p.ryz);  // Y|Z bits inside the tile
+                o.pmask = p.ryz;            // with gbase: the tile's share of the sign parity
+                o.rcmask = local_mask(p.rpm);
+                o.lcval = local_mask(p.rpv);
+                {
+                    u64 gm = 0; // projector bits outside the tile gate the whole tile
+                    for (int b = 0; b < n; b++) {
+                        if (((p.rpm >> b) & 1U) && !is_local(b)) {
+                            gm |= u64{1} << b;
+                        }
+                    }
+                    o.gcmask = gm;
+                    o.gcval = p.rpv & gm;
+                }
+                o.mode = p.rny4;
+                o.rslot = p.rslot;
+                o.rmul = d.pass_scale * d.pass_scale;
+                o.diag_slot = d.nrslots++; // the CTA's accumulator for this op
+                PLGB_REQUIRE(d.nrslots <= kMaxReducePerPass, "fusion: too many reductions in one pass");
+                ops.push_back(o);
+                continue;
+            }
             if (p.kind == Prim<T>::Parity) {
                 TileOp<T> o;
                 o.kind = TK_PARITY;
@@ -1047,6 +1090,24 @@ template <class T> void run_fused(StateVector<T> &sv, const FusedProgram<T> &pro
 }
 
 template <class T>
+void run_fused_adjoint(StateVector<T> &lam, StateVector<T> &hlam, const FusedProgram<T> &prog, double *partials,
+                       int G) {
+    PLGB_REQUIRE(prog.n == lam.num_qubits() && prog.n == hlam.num_qubits(),
+                 "adjoint program compiled for a different register size");
+    PLGB_REQUIRE(lam.stream() == hlam.stream(), "adjoint registers must share a stream");
+    for (const auto &seg : prog.segs) {
+        if (seg.tile) {
+            launch_tile_pass_adj<T>(lam.stream(), lam.data(), hlam.data(), seg.desc, prog.d_ops, prog.d_forms,
+                                    prog.d_tables, partials, G);
+        } else {
+            PLGB_REQUIRE(seg.prim.kind != Prim<T>::Reduce, "adjoint program: reduction outside a tile pass");
+            lam.run_prim(seg.prim);
+            hlam.run_prim(seg.prim);
+        }
+    }
+}
+
+template <class T>
 void StateVector<T>::apply_prims_fused(const std::vector<Prim<T>> &prims, int tile_bits) {
     auto prog = compile_fused<T>(n_, prims, tile_bits);
     run_fused<T>(*this, *prog);
@@ -1068,6 +1129,10 @@ template struct FusedProgram<double>;
 template std::shared_ptr<FusedProgram<float>> compile_fused<float>(int, const std::vector<Prim<float>> &, int, bool);
 template std::shared_ptr<FusedProgram<double>> compile_fused<double>(int, const std::vector<Prim<double>> &, int,
                                                                      bool);
+template void run_fused_adjoint<float>(StateVector<float> &, StateVector<float> &, const FusedProgram<float> &,
+                                       double *, int);
+template void run_fused_adjoint<double>(StateVector<double> &, StateVector<double> &, const FusedProgram<double> &,
+                                        double *, int);
 template void run_fused<float>(StateVector<float> &, const FusedProgram<float> &);
 template void run_fused<double>(StateVector<double> &, const FusedProgram<double> &);
 template void StateVector<float>::apply_prims_fused(const std::vector<Prim<float>> &, int);

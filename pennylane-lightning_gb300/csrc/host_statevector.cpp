@@ -334,7 +334,7 @@ template <class T> void StateVector<T>::scale_add(const StateVector &x, cd facto
 // primitives: emitted into the fusion sink when one is set, launched otherwise
 // ---------------------------------------------------------------------------
 template <class T> u64 Prim<T>::touched() const {
-    u64 t = cmask | pmask | my | mz;
+    u64 t = cmask | pmask | my | mz | rx | ryz | rpm;
     for (int b : tbits) {
         t |= u64{1} << b;
     }

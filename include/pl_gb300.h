@@ -178,6 +178,11 @@ int plgb_ops_num_par_ops(const plgb_ops *ops, int *out);
  * passes are cached on `ops` per register size, precision and t).
  * *passes_out (optional) receives the number of kernel passes per call. */
 int plgb_sv_apply_operations(plgb_sv *sv, plgb_ops *ops, int tile_bits, int *passes_out);
+/* Arithmetic of fused complex128 passes (no counterpart in the reference):
+ * on = 0 (default) runs them in double-float arithmetic on the FP32 pipe
+ * (about 48 significant bits; GB300 executes FP64 at 1/64 of its FP32
+ * rate), on = 1 in FP64.  Process-wide; returns the previous setting. */
+int plgb_set_c128_fp64_passes(int on);
 /* Plan introspection (no device needed): the tile passes plgb_sv_apply_operations
  * would run for `ops` on num_qubits at precision / tile_bits, as a JSON array
  * with one object per pass (tile size, op counts, execution stages). */

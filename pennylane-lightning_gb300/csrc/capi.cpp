@@ -449,6 +449,11 @@ int plgb_batch_stats(const plgb_batch *b, char *buf, size_t len) {
     return rc != PLGB_OK ? rc : copy_text(js, buf, len);
 }
 const char *plgb_gate_name(int code) { return gate_name_of(code); }
+int plgb_set_c128_fp64_passes(int on) {
+    const bool prev = c128_fp64_passes();
+    set_c128_fp64_passes(on != 0);
+    return prev ? 1 : 0;
+}
 
 int plgb_meas_expval_matrix_noalloc(plgb_sv *sv, const double *matrix, const int64_t *wires, int nw, double *out) {
     // no host containers on the success path: the matrix and wires are read

@@ -98,6 +98,13 @@ void launch_tile_pass_adj(cudaStream_t s, cx<T> *lam, cx<T> *hlam, const TilePas
 int adj_grid_capacity(size_t tile_bytes_each);
 void launch_adj_sum(cudaStream_t s, const double *partials, int nslots, int G, double *out);
 
+struct df;
+// Complex128 passes in double-float arithmetic (df.cuh).  io: 0 = doubles in
+// and out, 1 = doubles in / df out (first pass of a program), 2 = df in and
+// out, 3 = df in / doubles out (last pass).
+void launch_tile_pass_reg_df(cudaStream_t s, void *sv, int io, const TilePassDesc &d, const TileOp<df> *ops,
+                             const DiagForm<df> *forms, const cx<df> *tables, const StageDesc *stages);
+
 template <class T>
 void launch_tile_pass_reg(cudaStream_t s, cx<T> *sv, const TilePassDesc &d, const TileOp<T> *ops,
                           const DiagForm<T> *forms, const cx<T> *tables, const StageDesc *stages);

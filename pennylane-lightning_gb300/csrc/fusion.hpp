@@ -21,6 +21,11 @@ template <class T> struct FusedProgram {
     DiagForm<T> *d_forms{nullptr};
     cx<T> *d_tables{nullptr};
     StageDesc *d_stages{nullptr};
+    // double-float copies of the op tables (complex128 programs whose every
+    // pass runs on the register kernel; df_ok tells whether they exist)
+    bool df_ok{false};
+    void *dev_df{nullptr};
+    const void *d_ops_df{nullptr}, *d_forms_df{nullptr}, *d_tables_df{nullptr};
     // host copies (compile_fused without upload); indices in the segments'
     // descriptors are relative to these arrays
     std::vector<TileOp<T>> h_ops;
@@ -36,6 +41,9 @@ template <class T> struct FusedProgram {
     ~FusedProgram() {
         if (dev) {
             cudaFree(dev);
+        }
+        if (dev_df) {
+            cudaFree(dev_df);
         }
     }
 };

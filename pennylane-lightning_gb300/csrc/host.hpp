@@ -205,6 +205,10 @@ template <class T> struct FusedProgram;
 template <class T>
 std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>> &prims, int tile_bits,
                                                bool upload = true);
+// Arithmetic of fused complex128 passes: double-float on the FP32 pipe
+// (default) or FP64.
+void set_c128_fp64_passes(bool on);
+bool c128_fp64_passes();
 // JSON description of a compiled program's passes (plan introspection)
 template <class T> std::string fused_plan_json(const FusedProgram<T> &prog);
 template <class T> void run_fused(StateVector<T> &sv, const FusedProgram<T> &prog);

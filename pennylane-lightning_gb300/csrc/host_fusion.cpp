@@ -21,9 +21,13 @@
 // Primitives a tile cannot run (dense blocks on 3+ wires, Pauli rotations,
 // projections, wide diagonals across the tile boundary) run unfused
 // between passes.
+#include "df.cuh"
 #include "fusion.hpp"
 
 #include <algorithm>
+#include <atomic>
+#include <cstring>
+#include <type_traits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -1072,11 +1076,79 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
         cuda_check(cudaMemcpy(prog->d_tables, tables.data(), tables.size() * sizeof(cx<T>), cudaMemcpyHostToDevice),
                    "H2D");
     }
+    if constexpr (std::is_same_v<T, double>) {
+        bool all_reg = !prog->segs.empty();
+        for (const auto &seg : prog->segs) {
+            all_reg = all_reg && seg.tile && seg.reg;
+        }
+        if (all_reg) {
+            // the same tables re-encoded as double-float (same 16-byte layout)
+            static_assert(sizeof(TileOp<double>) == sizeof(TileOp<df>) && sizeof(DiagForm<double>) == sizeof(DiagForm<df>),
+                          "double-float op tables must share the double layout");
+            auto cdf = [](cx<double> v) { return cx<df>{df(v.x), df(v.y)}; };
+            std::vector<TileOp<df>> ops_df(ops.size());
+            for (size_t i = 0; i < ops.size(); i++) {
+                std::memcpy(static_cast<void *>(&ops_df[i]), &ops[i], sizeof(TileOp<double>));
+                for (int k = 0; k < 16; k++) {
+                    ops_df[i].m[k] = cdf(ops[i].m[k]);
+                }
+            }
+            std::vector<DiagForm<df>> forms_df(forms.size());
+            for (size_t i = 0; i < forms.size(); i++) {
+                std::memcpy(static_cast<void *>(&forms_df[i]), &forms[i], sizeof(DiagForm<double>));
+                for (int k = 0; k < 16; k++) {
+                    forms_df[i].tab[k] = cdf(forms[i].tab[k]);
+                }
+            }
+            std::vector<cx<df>> tables_df(tables.size());
+            for (size_t i = 0; i < tables.size(); i++) {
+                tables_df[i] = cdf(tables[i]);
+            }
+            cuda_check(cudaMalloc(&prog->dev_df, b_ops + b_forms + b_tab), "cudaMalloc(fused program, df)");
+            char *bd = static_cast<char *>(prog->dev_df);
+            prog->d_ops_df = bd;
+            prog->d_forms_df = bd + b_ops;
+            prog->d_tables_df = bd + b_ops + b_forms;
+            if (!ops_df.empty()) {
+                cuda_check(cudaMemcpy(bd, ops_df.data(), ops_df.size() * sizeof(TileOp<df>), cudaMemcpyHostToDevice),
+                           "H2D");
+            }
+            if (!forms_df.empty()) {
+                cuda_check(cudaMemcpy(bd + b_ops, forms_df.data(), forms_df.size() * sizeof(DiagForm<df>),
+                                      cudaMemcpyHostToDevice), "H2D");
+            }
+            if (!tables_df.empty()) {
+                cuda_check(cudaMemcpy(bd + b_ops + b_forms, tables_df.data(), tables_df.size() * sizeof(cx<df>),
+                                      cudaMemcpyHostToDevice), "H2D");
+            }
+            prog->df_ok = true;
+        }
+    }
     return prog;
 }
 
+namespace {
+std::atomic<bool> g_c128_fp64{false};
+}
+void set_c128_fp64_passes(bool on) { g_c128_fp64 = on; }
+bool c128_fp64_passes() { return g_c128_fp64; }
+
 template <class T> void run_fused(StateVector<T> &sv, const FusedProgram<T> &prog) {
     PLGB_REQUIRE(prog.n == sv.num_qubits(), "fused program compiled for a different register size");
+    if constexpr (std::is_same_v<T, double>) {
+        if (prog.df_ok && !c128_fp64_passes()) {
+            // the register holds df values between the first and the last pass
+            const size_t np = prog.segs.size();
+            for (size_t k = 0; k < np; k++) {
+                const int io = np == 1 ? 0 : k == 0 ? 1 : k + 1 == np ? 3 : 2;
+                launch_tile_pass_reg_df(sv.stream(), sv.data(), io, prog.segs[k].desc,
+                                        static_cast<const TileOp<df> *>(prog.d_ops_df),
+                                        static_cast<const DiagForm<df> *>(prog.d_forms_df),
+                                        static_cast<const cx<df> *>(prog.d_tables_df), prog.d_stages);
+            }
+            return;
+        }
+    }
     for (const auto &seg : prog.segs) {
         if (seg.tile && seg.reg) {
             launch_tile_pass_reg<T>(sv.stream(), sv.data(), seg.desc, prog.d_ops, prog.d_forms, prog.d_tables,

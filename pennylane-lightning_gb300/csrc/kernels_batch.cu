@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(256, 1)
             cur = lo;
         }
         const BatchTileItem<T> &it = items[lo];
-        tile_reg_run<T>(it.sv, sd, it.ops, it.forms, it.tables, it.stages, gt - it.tile_begin, tile, sh);
+        tile_reg_run<T>(it.sv, it.sv, sd, it.ops, it.forms, it.tables, it.stages, gt - it.tile_begin, tile, sh);
     }
 }
 

@@ -30,7 +30,64 @@ __global__ void __launch_bounds__(256, 1) k_tile_reg(cx<T> *__restrict__ a, cons
     }
     __syncthreads();
     for (u64 g = blockIdx.x; g < sd.ntiles; g += gridDim.x) {
-        tile_reg_run<T>(a, sd, ops, forms, tables, stages, g, tile, sh);
+        tile_reg_run<T>(a, a, sd, ops, forms, tables, stages, g, tile, sh);
+    }
+}
+
+template <class SI, class SO>
+__global__ void __launch_bounds__(256, 1) k_tile_reg_df(const cx<SI> *ain, cx<SO> *aout, const TilePassDesc d,
+                                                     const TileOp<df> *__restrict__ ops,
+                                                     const DiagForm<df> *__restrict__ forms,
+                                                     const cx<df> *__restrict__ tables,
+                                                     const StageDesc *__restrict__ stages) {
+    extern __shared__ unsigned char smraw[];
+    cx<df> *tile = reinterpret_cast<cx<df> *>(smraw);
+    __shared__ TileShared<df> sh;
+    __shared__ TilePassDesc sd;
+    if (threadIdx.x == 0) {
+        sd = d;
+    }
+    __syncthreads();
+    for (u64 g = blockIdx.x; g < sd.ntiles; g += gridDim.x) {
+        tile_reg_run<df, SI, SO>(ain, aout, sd, ops, forms, tables, stages, g, tile, sh);
+    }
+}
+
+template <class SI, class SO>
+static void launch_df(cudaStream_t s, void *sv, const TilePassDesc &d, const TileOp<df> *ops, const DiagForm<df> *forms,
+                      const cx<df> *tables, const StageDesc *stages) {
+    const int threads = 1 << (d.t - kRegBits);
+    const size_t smem = sizeof(cx<df>) << d.t;
+    static bool attr = false;
+    if (!attr) {
+        cuda_check(cudaFuncSetAttribute(k_tile_reg_df<SI, SO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        200 * 1024), "tile_reg_df smem attribute");
+        attr = true;
+    }
+    int per_sm = 1;
+    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_reg_df<SI, SO>, threads, smem),
+               "occupancy");
+    if (per_sm < 1) {
+        throw std::runtime_error("register tile pass (df): tile does not fit one SM");
+    }
+    const u64 cap = static_cast<u64>(LaunchGeom::sm_count()) * static_cast<u64>(per_sm);
+    const unsigned grid = static_cast<unsigned>(d.ntiles < cap ? d.ntiles : cap);
+    k_tile_reg_df<SI, SO><<<grid, threads, smem, s>>>(static_cast<const cx<SI> *>(sv), static_cast<cx<SO> *>(sv), d,
+                                                      ops, forms, tables, stages);
+    cuda_check(cudaGetLastError(), "k_tile_reg_df launch");
+    note_launch();
+}
+
+void launch_tile_pass_reg_df(cudaStream_t s, void *sv, int io, const TilePassDesc &d, const TileOp<df> *ops,
+                             const DiagForm<df> *forms, const cx<df> *tables, const StageDesc *stages) {
+    if (d.t < kMinRegTileBits || d.t > 12 || d.ndiag > kMaxDiagOpsPerPass) {
+        throw std::runtime_error("register tile pass (df): unsupported geometry");
+    }
+    switch (io) {
+    case 0: launch_df<double, double>(s, sv, d, ops, forms, tables, stages); break;
+    case 1: launch_df<double, df>(s, sv, d, ops, forms, tables, stages); break;
+    case 2: launch_df<df, df>(s, sv, d, ops, forms, tables, stages); break;
+    default: launch_df<df, double>(s, sv, d, ops, forms, tables, stages); break;
     }
 }
 

@@ -14,6 +14,9 @@
 // applied in registers from the per-pass table.
 #pragma once
 
+#include <type_traits>
+
+#include "df.cuh"
 #include "fused.hpp"
 
 namespace plgb {
@@ -54,11 +57,41 @@ __device__ __forceinline__ double sflip(double x, unsigned neg) {
 __device__ __forceinline__ float sflip(float x, unsigned neg) {
     return __int_as_float(__float_as_int(x) ^ static_cast<int>(neg << 31));
 }
+__device__ __forceinline__ df sflip(df x, unsigned neg) { return df{sflip(x.hi, neg), sflip(x.lo, neg)}; }
 template <class T> __device__ __forceinline__ cx<T> cflip(cx<T> v, unsigned neg) {
     return cx<T>{sflip(v.x, neg), sflip(v.y, neg)};
 }
+__device__ __forceinline__ float shfl_val(float x, int m) { return __shfl_xor_sync(0xffffffffu, x, m); }
+__device__ __forceinline__ double shfl_val(double x, int m) { return __shfl_xor_sync(0xffffffffu, x, m); }
+__device__ __forceinline__ df shfl_val(df x, int m) { return df{shfl_val(x.hi, m), shfl_val(x.lo, m)}; }
 template <class T> __device__ __forceinline__ cx<T> shx(cx<T> v, int m) {
-    return cx<T>{__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m)};
+    return cx<T>{shfl_val(v.x, m), shfl_val(v.y, m)};
+}
+
+// Register <-> memory formats: complex64 / complex128 registers compute in
+// their own type; a df register reads doubles (first pass of a program) or
+// df, and writes df or doubles (last pass).
+template <class T, class S> __device__ __forceinline__ cx<T> ld_conv(const cx<S> &v) {
+    if constexpr (std::is_same_v<T, df> && std::is_same_v<S, double>) {
+        return cx<df>{df_from_bits(v.x), df_from_bits(v.y)};
+    } else {
+        return v;
+    }
+}
+template <class S, class T> __device__ __forceinline__ cx<S> st_conv(const cx<T> &v) {
+    if constexpr (std::is_same_v<T, df> && std::is_same_v<S, double>) {
+        return cx<double>{df_to_double(v.x), df_to_double(v.y)};
+    } else {
+        return v;
+    }
+}
+// a per-pass double constant in the register's type
+template <class T> __device__ __forceinline__ T from_double(double x) {
+    if constexpr (std::is_same_v<T, df>) {
+        return df(x);
+    } else {
+        return static_cast<T>(x);
+    }
 }
 
 // Layout of a register stage, held in registers: local index of register
@@ -177,8 +210,8 @@ template <class T> struct TileShared {
 
 // Apply pass `d` to tile g of register `a` (all threads of the CTA; the CTA
 // has 2^(d.t - 4) threads and 2^d.t amplitudes of shared memory at `tile`).
-template <class T>
-__device__ __forceinline__ void tile_reg_run(cx<T> *__restrict__ a, const TilePassDesc &d,
+template <class T, class SI = T, class SO = T>
+__device__ __forceinline__ void tile_reg_run(const cx<SI> *ain, cx<SO> *aout, const TilePassDesc &d,
                                              const TileOp<T> *__restrict__ ops, const DiagForm<T> *__restrict__ forms,
                                              const cx<T> *__restrict__ tables, const StageDesc *__restrict__ stages,
                                              u64 g, cx<T> *tile, TileShared<T> &sh) {
@@ -207,7 +240,7 @@ __device__ __forceinline__ void tile_reg_run(cx<T> *__restrict__ a, const TilePa
     const u64 tbase = gbase | off_t;
 #pragma unroll
     for (int i = 0; i < NR; i++) {
-        v[i] = a[tbase | off_r(i)];
+        v[i] = ld_conv<T, SI>(ain[tbase | off_r(i)]);
     }
     // prologue: tile-uniform parts of every merged diagonal, one warp per op
     int slot = 0;
@@ -266,7 +299,7 @@ __device__ __forceinline__ void tile_reg_run(cx<T> *__restrict__ a, const TilePa
     }
     __syncthreads();
     if (tid == 0) {
-        cx<T> f{static_cast<T>(d.pass_scale), 0};
+        cx<T> f{from_double<T>(d.pass_scale), from_double<T>(0.0)};
         for (int s = 0; s < d.ndiag; s++) {
             f = f * sh.scal[s];
         }
@@ -398,7 +431,7 @@ __device__ __forceinline__ void tile_reg_run(cx<T> *__restrict__ a, const TilePa
     const cx<T> f = sh.factor;
 #pragma unroll
     for (int i = 0; i < NR; i++) {
-        a[tbase | off_r(i)] = f * v[i];
+        aout[tbase | off_r(i)] = st_conv<SO, T>(f * v[i]);
     }
     __syncthreads();
 }

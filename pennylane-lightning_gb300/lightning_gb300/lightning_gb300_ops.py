@@ -74,6 +74,12 @@ def _text(fn, *args, size=4096) -> str:
 
 
 # --------------------------------------------------------------------------- module functions
+def set_c128_fp64_passes(on: bool) -> bool:
+    """Fused complex128 passes in FP64 (True) or double-float arithmetic on
+    the FP32 pipe (False, the default); returns the previous setting."""
+    return bool(lib().plgb_set_c128_fp64_passes(1 if on else 0))
+
+
 def backend_info() -> dict:
     """LQubitBindings.hpp:464-475."""
     return json.loads(_text("plgb_backend_info"))

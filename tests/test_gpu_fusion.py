@@ -124,3 +124,26 @@ def test_config0_fused(ops_module, oracle, dt):
     st[0] = 1
     ref = oracle_apply(oracle, n, dt, st, ops)
     assert_close(sv.state(), ref, dt, scale=50, what="config0 fused")
+
+
+def test_c128_double_float_passes_match_fp64(ops_module):
+    # fused complex128 passes run in double-float arithmetic by default; the
+    # FP64 passes must agree within the complex128 tolerance
+    rng = np.random.default_rng(seed_of("df-vs-fp64"))
+    n = 16
+    circuit, _ = config1(n, 12, seed=1001)
+    ops = [op.as_dict() for op in circuit]  # every pass on the register kernel
+    st = rand_state(rng, n, np.complex128)
+    S = ops_struct(ops_module, np.complex128, ops)
+    outs = {}
+    for fp64 in (False, True):
+        prev = ops_module.set_c128_fp64_passes(fp64)
+        try:
+            sv = ops_module.StateVectorC128(n)
+            sv.updateData(st)
+            sv.applyOperations(S, 11)
+            outs[fp64] = sv.state()
+        finally:
+            ops_module.set_c128_fp64_passes(prev)
+    assert_close(outs[False], outs[True], np.complex128, scale=50, what="double-float vs FP64 passes")
+    assert not np.array_equal(outs[False], outs[True])  # the two arithmetics did run

@@ -14,6 +14,7 @@
 #include <chrono>
 #include <cstring>
 #include <thread>
+#include <type_traits>
 
 namespace plgb {
 
@@ -158,7 +159,11 @@ template <class T> int BatchEngine<T>::tile_bits_for(int n) {
 template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
     std::lock_guard<std::mutex> lk(mu_);
     const auto t_start = std::chrono::steady_clock::now();
+    // complex128 batches run their fused passes in double-float arithmetic
+    // unless FP64 passes were requested
+    const bool use_df = std::is_same_v<T, double> && !c128_fp64_passes();
     stats_ = BatchStats{};
+    stats_.df = use_df;
     const int nc = in.ncirc;
     stats_.ncirc = nc;
     PLGB_REQUIRE(nc >= 0, "number of circuits must be non-negative");
@@ -334,6 +339,27 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
             std::memcpy(hp + o.forms, pr.h_forms.data(), pr.h_forms.size() * sizeof(DiagForm<T>));
             std::memcpy(hp + o.tables, pr.h_tables.data(), pr.h_tables.size() * sizeof(cx<T>));
             std::memcpy(hp + o.stages, pr.h_stages.data(), pr.h_stages.size() * sizeof(StageDesc));
+            if constexpr (std::is_same_v<T, double>) {
+                if (use_df) { // the same tables re-encoded as double-float (same layout)
+                    auto cdf = [](cx<double> v) { return cx<df>{df(v.x), df(v.y)}; };
+                    auto *od = reinterpret_cast<TileOp<df> *>(hp + o.ops);
+                    for (size_t k = 0; k < pr.h_ops.size(); k++) {
+                        for (int m = 0; m < 16; m++) {
+                            od[k].m[m] = cdf(pr.h_ops[k].m[m]);
+                        }
+                    }
+                    auto *fd = reinterpret_cast<DiagForm<df> *>(hp + o.forms);
+                    for (size_t k = 0; k < pr.h_forms.size(); k++) {
+                        for (int m = 0; m < 16; m++) {
+                            fd[k].tab[m] = cdf(pr.h_forms[k].tab[m]);
+                        }
+                    }
+                    auto *td = reinterpret_cast<cx<df> *>(hp + o.tables);
+                    for (size_t k = 0; k < pr.h_tables.size(); k++) {
+                        td[k] = cdf(pr.h_tables[k]);
+                    }
+                }
+            }
         }
         char *dp = static_cast<char *>(d_prog_);
 
@@ -399,6 +425,7 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
                     const u64 N = u64{1} << cc.ne;
                     r.work = g.x == 0 ? N : N >> 1;
                     r.block_begin = rblocks;
+                    r.df = use_df && cc.fast ? 1 : 0;
                     rblocks += (r.work + kBatchRedChunk - 1) / kBatchRedChunk;
                     obs_item.emplace_back(ob0 + static_cast<int64_t>(ob), ritems.size());
                     ritems.push_back(r);
@@ -443,10 +470,19 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
         cuda_check(cudaMemcpyAsync(dp, hp, pbytes, cudaMemcpyHostToDevice, s_), "H2D programs");
         cuda_check(cudaMemcpyAsync(di, hi, ibytes, cudaMemcpyHostToDevice, s_), "H2D items");
         cuda_check(cudaMemsetAsync(states, 0, sv_bytes, s_), "memset registers");
-        launch_batch_set_one<T>(s_, d_ptrs, wn);
+        if (use_df) { // registers stay double-float pairs from |0..0> to the reductions
+            launch_batch_set_one<df>(s_, reinterpret_cast<cx<df> *const *>(d_ptrs), wn);
+        } else {
+            launch_batch_set_one<T>(s_, d_ptrs, wn);
+        }
         stats_.launches += 1;
         for (const auto &L : launches) {
-            launch_tile_reg_batch<T>(s_, L.t, d_titems + L.item0, L.nitems, L.tiles);
+            if (use_df) {
+                launch_tile_reg_batch<df>(s_, L.t, reinterpret_cast<const BatchTileItem<df> *>(d_titems + L.item0),
+                                          L.nitems, L.tiles);
+            } else {
+                launch_tile_reg_batch<T>(s_, L.t, d_titems + L.item0, L.nitems, L.tiles);
+            }
             stats_.launches++;
         }
         // circuits the batched kernel cannot take run pass by pass on their own
@@ -457,6 +493,9 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
             }
             stats_.fallback++;
             StateVector<T> view(reinterpret_cast<cx<T> *>(states + sv_off[static_cast<size_t>(i)]), cc.ne, s_);
+            if (use_df) {
+                view.reset(); // this register stays in doubles
+            }
             const auto l0 = launch_count();
             run_fused<T>(view, *cc.prog);
             stats_.launches += static_cast<int>(launch_count() - l0);
@@ -508,6 +547,7 @@ template <class T> std::string BatchEngine<T>::stats_json() const {
                      ", \"max_passes\": " + std::to_string(stats_.max_passes) +
                      ", \"padded\": " + std::to_string(stats_.padded) +
                      ", \"fallback\": " + std::to_string(stats_.fallback) +
+                     ", \"double_float\": " + std::string(stats_.df ? "true" : "false") +
                      ", \"compile_ms\": " + std::to_string(stats_.compile_ms) +
                      ", \"device_ms\": " + std::to_string(stats_.device_ms) +
                      ", \"total_ms\": " + std::to_string(stats_.total_ms) + ", \"tile_bits\": {";

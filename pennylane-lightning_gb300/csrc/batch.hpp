@@ -11,6 +11,7 @@
 // in the batch.
 #pragma once
 
+#include "df.cuh"
 #include "fused.hpp"
 #include "host.hpp"
 
@@ -36,6 +37,7 @@ template <class T> struct BatchRedItem {
     const PauliGroup *group;
     u64 work;      // amplitudes (x == 0) or pairs (x != 0)
     u64 block_begin;
+    int df;        // complex128 register held as double-float pairs
 };
 
 constexpr u64 kBatchRedChunk = 4096; // amplitudes or pairs per reduction block
@@ -69,6 +71,7 @@ int gate_code_count();
 
 struct BatchStats {
     int ncirc{0}, waves{0}, launches{0}, max_passes{0}, padded{0}, fallback{0};
+    bool df{false};
     double compile_ms{0}, device_ms{0}, total_ms{0};
     std::map<int, int> tile_bits; // register size -> tile bits used
     std::vector<double> wave_done_ms; // completion time of each wave, from the start of run()

@@ -2,6 +2,8 @@
 // layer over the tiles of many registers, the |0...0> initialisation of a
 // wave of registers, and batched Pauli-sum reductions.
 #include "batch.hpp"
+
+#include <type_traits>
 #include "tile_reg.cuh"
 
 namespace plgb {
@@ -83,6 +85,17 @@ namespace {
 
 constexpr int kBatchRedThreads = 256;
 
+template <class T> __device__ __forceinline__ cx<double> ld_amp(const cx<T> *a, u64 j, int dfm) {
+    if constexpr (std::is_same_v<T, double>) {
+        if (dfm) {
+            const cx<df> v = reinterpret_cast<const cx<df> *>(a)[j];
+            return cx<double>{df_to_double(v.x), df_to_double(v.y)};
+        }
+    }
+    const cx<T> v = a[j];
+    return cx<double>{static_cast<double>(v.x), static_cast<double>(v.y)};
+}
+
 __device__ __forceinline__ double batch_term_pair(const PauliTerm &t, u64 j, u64 jp, double ar, double ai) {
     const double s = (__popcll(j & t.yz) & 1) ? -1.0 : 1.0;
     const double sp = (__popcll(jp & t.yz) & 1) ? -1.0 : 1.0;
@@ -121,8 +134,8 @@ __global__ void __launch_bounds__(kBatchRedThreads)
     double v = 0.0;
     if (g.x == 0) {
         for (u64 j = c0 + threadIdx.x; j < c1; j += kBatchRedThreads) {
-            const cx<T> p = a[j];
-            const double w = static_cast<double>(p.x) * p.x + static_cast<double>(p.y) * p.y;
+            const cx<double> p = ld_amp<T>(a, j, it.df);
+            const double w = p.x * p.x + p.y * p.y;
             double f = 0.0;
             for (int t = 0; t < g.nterms; t++) {
                 f += (__popcll(j & g.t[t].yz) & 1) ? -g.t[t].coeff : g.t[t].coeff;
@@ -133,10 +146,10 @@ __global__ void __launch_bounds__(kBatchRedThreads)
         for (u64 k = c0 + threadIdx.x; k < c1; k += kBatchRedThreads) {
             const u64 j = insert_zero(k, g.hb);
             const u64 jp = j ^ g.x;
-            const cx<T> p = a[j];
-            const cx<T> q = a[jp];
-            const double ar = static_cast<double>(p.x) * q.x + static_cast<double>(p.y) * q.y;
-            const double ai = static_cast<double>(p.x) * q.y - static_cast<double>(p.y) * q.x;
+            const cx<double> p = ld_amp<T>(a, j, it.df);
+            const cx<double> q = ld_amp<T>(a, jp, it.df);
+            const double ar = p.x * q.x + p.y * q.y;
+            const double ai = p.x * q.y - p.y * q.x;
             double f = 0.0;
             for (int t = 0; t < g.nterms; t++) {
                 f += g.t[t].coeff * batch_term_pair(g.t[t], j, jp, ar, ai);
@@ -214,5 +227,7 @@ void launch_pauli_batch(cudaStream_t s, const BatchRedItem<T> *items, int nitems
     template void launch_pauli_batch<T>(cudaStream_t, const BatchRedItem<T> *, int, u64, double *, double *);
 PLGB_BATCH_INST(float)
 PLGB_BATCH_INST(double)
+template void launch_tile_reg_batch<df>(cudaStream_t, int, const BatchTileItem<df> *, int, u64);
+template void launch_batch_set_one<df>(cudaStream_t, cx<df> *const *, int);
 
 } // namespace plgb

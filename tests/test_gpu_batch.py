@@ -157,3 +157,22 @@ def test_batch_rejects_bad_input():
         eng.run(bad)
     with pytest.raises(ValueError):
         pack([SimpleNamespace(n=3, ops=[Op("QubitUnitary", [0], matrix=np.eye(2))], observables=[])])
+
+
+def test_batch_double_float_vs_fp64(ops_module):
+    # complex128 batches run in double-float arithmetic by default; FP64
+    # passes give the same values within the complex128 tolerance
+    packed = config2_packed(10, seed=21)
+    a = BatchEngine(128, tile_bits=10)
+    va = a.run(packed)
+    assert a.stats()["double_float"] is True
+    prev = ops_module.set_c128_fp64_passes(True)
+    try:
+        b = BatchEngine(128, tile_bits=10)
+        vb = b.run(packed)
+        assert b.stats()["double_float"] is False
+    finally:
+        ops_module.set_c128_fp64_passes(prev)
+    norms = np.array([max(1.0, np.abs(packed.term_coeffs[packed.term_offsets[k]:packed.term_offsets[k + 1]]).sum())
+                      for k in range(packed.num_observables)])
+    assert np.all(np.abs(va - vb) <= 50e-12 * norms)

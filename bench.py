@@ -58,6 +58,26 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(seconds: float, ws: int, device: str) -> float:
+    """The slowest replica's time: every rank's timed region ends only when
+    all replicas are done (no data-path collective; the path runs as
+    independent replicas, one per GPU)."""
+    if ws <= 1:
+        return seconds
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank: float, ws: int, seconds: float) -> float:
+    """Whole-job throughput: the units all replicas processed over the
+    slowest replica's time (weak scaling)."""
+    return ws * units_per_rank / seconds
+
+
 def dist_info():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -204,13 +224,7 @@ def gpu_arm(args) -> dict | None:
         barrier()
         wall = time.perf_counter() - t0
     launches = ops.kernel_launches() - launches0
-    total_s = sum(step_ms) / 1e3
-    if ws > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([total_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
+    total_s = max_over_ranks(sum(step_ms) / 1e3, ws, "cuda")
     passes = step_passes[0]
     pass_bytes = 2.0 * (1 << n) * 16
     avg_launch_s = (total_s / args.steps) / passes
@@ -256,7 +270,7 @@ def gpu_arm(args) -> dict | None:
     del sv
 
     res = {
-        "metric": METRIC, "value": ws * alg_bytes * args.steps / total_s / 1e9, "unit": UNIT, "n_gpus": ws,
+        "metric": METRIC, "value": replica_value(alg_bytes * args.steps, ws, total_s) / 1e9, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64 arithmetic)",
         "data": "synthetic (seeded Haar SU(2) + CZ circuit, seed 1001)",

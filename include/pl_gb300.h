@@ -192,6 +192,11 @@ int plgb_ops_fusion_plan(const plgb_ops *ops, int num_qubits, int precision, int
  * the operations are first applied to a copy of the state. */
 int plgb_adjoint_jacobian(plgb_sv *sv, plgb_obs *const *obs, int nobs, const plgb_ops *ops, const int64_t *trainable,
                           int ntp, int apply_ops, double *jac_out);
+/* VectorJacobianProductC*.__call__(sv, ops, dy, trainable_params)
+ * (LQubitBindings.hpp:412-457, VectorJacobianProduct.hpp:79-160): sv holds
+ * the final state, dy the cotangent (2^n complex, interleaved re/im);
+ * out receives ntp complex values <dy | d psi / d theta_j> (interleaved). */
+int plgb_vjp(plgb_sv *sv, const plgb_ops *ops, const double *dy, const int64_t *trainable, int ntp, double *out);
 /* The same Jacobian with apply_ops = 0, computed in place: sv holds the
  * final state and is overwritten by the backward sweep (left holding the
  * initial state up to rounding).  Registers held: 1 + nobs for Pauli-sum

@@ -769,6 +769,23 @@ int plgb_adjoint_jacobian(plgb_sv *sv, plgb_obs *const *obs, int nobs, const plg
         std::memcpy(jac_out, j.data(), j.size() * sizeof(double));
     });
 }
+int plgb_vjp(plgb_sv *sv, const plgb_ops *ops, const double *dy, const int64_t *trainable, int ntp, double *out) {
+    return with_sv(sv, [&](auto &s) {
+        need(ops, "ops");
+        need(dy, "dy");
+        need(out, "out");
+        using T = decltype(s.data()->x);
+        std::vector<std::complex<T>> d(s.length());
+        for (size_t i = 0; i < d.size(); i++) {
+            d[i] = std::complex<T>(static_cast<T>(dy[2 * i]), static_cast<T>(dy[2 * i + 1]));
+        }
+        const auto w = Adjoint<T>::vjp(s, ops->list, d.data(), vec(trainable, ntp));
+        for (size_t k = 0; k < w.size(); k++) {
+            out[2 * k] = w[k].real();
+            out[2 * k + 1] = w[k].imag();
+        }
+    });
+}
 int plgb_adjoint_jacobian_inplace(plgb_sv *sv, plgb_obs *const *obs, int nobs, const plgb_ops *ops,
                                   const int64_t *trainable, int ntp, double *jac_out) {
     return with_sv(sv, [&](auto &s) {

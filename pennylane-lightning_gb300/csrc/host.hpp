@@ -264,6 +264,10 @@ std::vector<PauliGroup> group_pauli(const PauliSum &ps);
 // Adjoint Jacobian (AdjointJacobianLQubit.hpp:225-491).
 // ---------------------------------------------------------------------------
 template <class T> struct Adjoint {
+    // VectorJacobianProduct (VectorJacobianProduct.hpp:79-160): w_j =
+    // <dy | d psi / d theta_j> for the trainable parameters, sv = final state
+    static std::vector<cd> vjp(StateVector<T> &sv, const OpsList &ops, const std::complex<T> *dy,
+                               const std::vector<int64_t> &trainable);
     // consume: sv already holds the final state and may be overwritten; the
     // sweep then runs in place on it (registers needed: 1 + observables for
     // Pauli-sum observables and Pauli-word generators, instead of 2 + 2x)

@@ -292,6 +292,87 @@ std::vector<double> Adjoint<T>::jacobian(StateVector<T> &sv, const std::vector<O
     return out;
 }
 
+template <class T>
+std::vector<cd> Adjoint<T>::vjp(StateVector<T> &sv, const OpsList &opsl, const std::complex<T> *dy,
+                                const std::vector<int64_t> &tp) {
+    const auto &ops = opsl.ops;
+    const size_t ntp = tp.size();
+    std::vector<cd> out(ntp, cd{0, 0});
+    if (ntp == 0) {
+        return out;
+    }
+    for (size_t i = 1; i < ntp; i++) {
+        PLGB_REQUIRE(tp[i] > tp[i - 1], "trainable parameter indices must be sorted and unique");
+    }
+    const size_t num_param_ops = opsl.num_par_ops();
+    PLGB_REQUIRE(tp.back() < static_cast<int64_t>(num_param_ops), "trainable parameter index out of range");
+    const int n = sv.num_qubits();
+    StateVector<T> lambda(sv); // same stream
+    StateVector<T> mu(n, lambda.stream());
+    mu.update_data(dy, lambda.length());
+    std::unique_ptr<StateVector<T>> mu_d;
+    double *red = lambda.scratch_red();
+    double *d_res = nullptr;
+    cuda_check(cudaMalloc(&d_res, 2 * ntp * sizeof(double)), "cudaMalloc(vjp results)");
+    struct Guard {
+        double *p;
+        ~Guard() { cudaFree(p); }
+    } guard{d_res};
+    std::vector<double> scale(ntp, 0.0);
+    std::vector<char> on_device(ntp, 0);
+    size_t tpn = ntp - 1;
+    size_t curp = num_param_ops - 1;
+    auto it = tp.rbegin();
+    for (long op_idx = static_cast<long>(ops.size()) - 1; op_idx >= 0; op_idx--) {
+        const auto &op = ops[static_cast<size_t>(op_idx)];
+        PLGB_REQUIRE(op.params.size() <= 1, "The operation is not supported using the adjoint differentiation method");
+        if (op.name == "StatePrep" || op.name == "BasisState") {
+            continue;
+        }
+        if (it == tp.rend()) {
+            break;
+        }
+        if (!op.params.empty()) {
+            if (static_cast<int64_t>(curp) == *it) {
+                const auto pg = pauli_generator(op, n);
+                if (pg) {
+                    // <mu| P G |lambda> by the transition kernel
+                    reduce_pauli_transition<T>(lambda.stream(), mu.data(), lambda.data(), lambda.length(), pg->x,
+                                               pg->yz, pg->ny4, pg->pmask, pg->pval, red, d_res + 2 * tpn);
+                    on_device[tpn] = 1;
+                    scale[tpn] = pg->scale * (op.inverse ? -1.0 : 1.0);
+                } else {
+                    if (!mu_d) {
+                        mu_d = std::make_unique<StateVector<T>>(mu);
+                    } else {
+                        mu_d->copy_from(mu);
+                    }
+                    const double sc =
+                        mu_d->apply_generator(op.name, op.cwires, op.cvals, op.wires) * (op.inverse ? -1.0 : 1.0);
+                    const cd ip = mu_d->inner(lambda);
+                    out[tpn] = cd{0.0, sc} * ip;
+                }
+                tpn--;
+                ++it;
+            }
+            curp--;
+        }
+        lambda.apply_op(op, !op.inverse);
+        mu.apply_op(op, !op.inverse);
+    }
+    std::vector<double> r(2 * ntp);
+    cuda_check(cudaMemcpyAsync(r.data(), d_res, r.size() * sizeof(double), cudaMemcpyDeviceToHost, lambda.stream()),
+               "D2H");
+    lambda.synchronize();
+    for (size_t k = 0; k < ntp; k++) {
+        if (on_device[k]) {
+            out[k] = cd{0.0, scale[k]} * cd{r[2 * k], r[2 * k + 1]};
+        }
+        out[k] = cd{static_cast<T>(out[k].real()), static_cast<T>(out[k].imag())};
+    }
+    return out;
+}
+
 template struct Adjoint<float>;
 template struct Adjoint<double>;
 

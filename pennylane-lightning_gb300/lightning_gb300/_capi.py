@@ -83,6 +83,7 @@ SIGNATURES = {
     "plgb_sv_apply_operations": (C.c_int, [VP, VP, C.c_int, IP]),
     "plgb_ops_fusion_plan": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_char_p, C.c_size_t]),
     "plgb_adjoint_jacobian": (C.c_int, [VP, C.POINTER(VP), C.c_int, VP, I64P, C.c_int, C.c_int, DP]),
+    "plgb_vjp": (C.c_int, [VP, VP, DP, I64P, C.c_int, DP]),
     "plgb_adjoint_jacobian_inplace": (C.c_int, [VP, C.POINTER(VP), C.c_int, VP, I64P, C.c_int, DP]),
 }
 

@@ -673,8 +673,32 @@ class AdjointJacobianC64(_AdjointJacobianBase):
     pass
 
 
+class _VectorJacobianProductBase:
+    """VectorJacobianProductC*.__call__ (LQubitBindings.hpp:412-457)."""
+
+    def __call__(self, sv: _StateVectorBase, ops: _OpsStructBase, dy, trainable_params) -> np.ndarray:
+        tp = [int(t) for t in trainable_params]
+        d = np.ascontiguousarray(np.asarray(dy, dtype=np.complex128).reshape(-1))
+        if d.size != len(sv):
+            raise LightningException("the cotangent must have one entry per amplitude")
+        out = np.zeros(2 * max(1, len(tp)), dtype=np.float64)
+        t, ntp = _i64(tp)
+        call("plgb_vjp", sv._h, ops._h, _dptr(d.view(np.float64)), t, ntp, _dptr(out))
+        dt = np.complex64 if sv._precision == 64 else np.complex128
+        return out[: 2 * len(tp)].view(np.complex128).astype(dt)
+
+
+class VectorJacobianProductC128(_VectorJacobianProductBase):
+    pass
+
+
+class VectorJacobianProductC64(_VectorJacobianProductBase):
+    pass
+
+
 algorithms = types.SimpleNamespace(
     OpsStructC64=OpsStructC64, OpsStructC128=OpsStructC128, create_ops_listC64=create_ops_listC64,
     create_ops_listC128=create_ops_listC128, AdjointJacobianC64=AdjointJacobianC64,
-    AdjointJacobianC128=AdjointJacobianC128,
+    AdjointJacobianC128=AdjointJacobianC128, VectorJacobianProductC64=VectorJacobianProductC64,
+    VectorJacobianProductC128=VectorJacobianProductC128,
 )

@@ -228,7 +228,7 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
                     auto p = reg.lower_op(rec, rec.inverse);
                     prims.insert(prims.end(), std::make_move_iterator(p.begin()), std::make_move_iterator(p.end()));
                 }
-                cc.prog = compile_fused<T>(cc.ne, prims, cc.t, false);
+                cc.prog = compile_fused<T>(cc.ne, prims, cc.t, false, true);
                 cc.fast = true;
                 for (const auto &seg : cc.prog->segs) {
                     if (!seg.tile || !seg.reg || seg.desc.t != cc.t) {
@@ -319,25 +319,41 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
         size_t pbytes = 0;
         for (int i = 0; i < wn; i++) {
             const auto &pr = *comp[static_cast<size_t>(c0 + i)].prog;
+            if (!comp[static_cast<size_t>(c0 + i)].fast) { // runs its own uploaded program
+                po[static_cast<size_t>(i)] = ProgOff{pbytes, pbytes, pbytes, pbytes};
+                continue;
+            }
             po[static_cast<size_t>(i)].ops = pbytes;
             pbytes += align_up(pr.h_ops.size() * sizeof(TileOp<T>));
             po[static_cast<size_t>(i)].forms = pbytes;
             pbytes += align_up(pr.h_forms.size() * sizeof(DiagForm<T>));
             po[static_cast<size_t>(i)].tables = pbytes;
-            pbytes += align_up(pr.h_tables.size() * sizeof(cx<T>));
+            pbytes += align_up(pr.table_entries * sizeof(cx<T>));
             po[static_cast<size_t>(i)].stages = pbytes;
             pbytes += align_up(pr.h_stages.size() * sizeof(StageDesc));
         }
         pbytes = std::max<size_t>(pbytes, 256);
+        const auto t_pack = std::chrono::steady_clock::now();
+        stats_.program_bytes += static_cast<double>(pbytes);
         grow(h_prog_, ch_prog_, pbytes, true);
         grow(d_prog_, c_prog_, pbytes, false);
         char *hp = static_cast<char *>(h_prog_);
         for (int i = 0; i < wn; i++) {
             const auto &pr = *comp[static_cast<size_t>(c0 + i)].prog;
+            if (!comp[static_cast<size_t>(c0 + i)].fast) {
+                continue;
+            }
             const auto &o = po[static_cast<size_t>(i)];
+            PLGB_REQUIRE(pr.h_recipes.empty() || !pr.h_factors.empty(), "batch: table recipe without factors");
+            for (const auto &ch : pr.h_table_chunks) {
+                PLGB_REQUIRE(ch[1] + ch[2] <= pr.h_tables.size() && ch[0] + ch[2] <= pr.table_entries,
+                             "batch: table chunk out of range");
+            }
             std::memcpy(hp + o.ops, pr.h_ops.data(), pr.h_ops.size() * sizeof(TileOp<T>));
             std::memcpy(hp + o.forms, pr.h_forms.data(), pr.h_forms.size() * sizeof(DiagForm<T>));
-            std::memcpy(hp + o.tables, pr.h_tables.data(), pr.h_tables.size() * sizeof(cx<T>));
+            for (const auto &ch : pr.h_table_chunks) { // tables materialised on the host
+                std::memcpy(hp + o.tables + ch[0] * sizeof(cx<T>), pr.h_tables.data() + ch[1], ch[2] * sizeof(cx<T>));
+            }
             std::memcpy(hp + o.stages, pr.h_stages.data(), pr.h_stages.size() * sizeof(StageDesc));
             if constexpr (std::is_same_v<T, double>) {
                 if (use_df) { // the same tables re-encoded as double-float (same layout)
@@ -355,13 +371,39 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
                         }
                     }
                     auto *td = reinterpret_cast<cx<df> *>(hp + o.tables);
-                    for (size_t k = 0; k < pr.h_tables.size(); k++) {
-                        td[k] = cdf(pr.h_tables[k]);
+                    for (const auto &ch : pr.h_table_chunks) {
+                        for (size_t k = 0; k < ch[2]; k++) {
+                            td[ch[0] + k] = cdf(pr.h_tables[ch[1] + k]);
+                        }
                     }
                 }
             }
         }
         char *dp = static_cast<char *>(d_prog_);
+        // merged-diagonal tables described by their factors: expanded on the device
+        std::vector<DevRecipe> recs;
+        std::vector<TableFactor> facs;
+        u64 rec_entries = 0;
+        for (int i = 0; i < wn; i++) {
+            const auto &pr = *comp[static_cast<size_t>(c0 + i)].prog;
+            if (!comp[static_cast<size_t>(c0 + i)].fast) {
+                continue;
+            }
+            const auto &o = po[static_cast<size_t>(i)];
+            for (const auto &r : pr.h_recipes) {
+                DevRecipe d{};
+                d.dst = dp + o.tables + static_cast<size_t>(r.table_off) * sizeof(cx<T>);
+                d.fac = reinterpret_cast<const TableFactor *>(facs.size()); // index, fixed below
+                d.t = r.t;
+                d.nfac = r.nfac;
+                d.entry_begin = rec_entries;
+                rec_entries += u64{1} << r.t;
+                facs.insert(facs.end(), pr.h_factors.begin() + r.fac_begin,
+                            pr.h_factors.begin() + r.fac_begin + r.nfac);
+                recs.push_back(d);
+            }
+        }
+        stats_.pack_ms += ms_since(t_pack);
 
         // launch plan: pass k of every fast circuit, grouped by tile size
         struct Launch {
@@ -434,12 +476,14 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
             }
         }
 
-        // one staging block: [tile items][set-one pointers][red items][groups]
+        // one staging block: [tile items][set-one pointers][red items][groups][recipes][factors]
         const size_t b_titems = align_up(std::max<size_t>(1, titems.size()) * sizeof(BatchTileItem<T>));
         const size_t b_ptrs = align_up(static_cast<size_t>(wn) * sizeof(cx<T> *));
         const size_t b_ritems = align_up(std::max<size_t>(1, ritems.size()) * sizeof(BatchRedItem<T>));
         const size_t b_groups = align_up(std::max<size_t>(1, groups.size()) * sizeof(PauliGroup));
-        const size_t ibytes = b_titems + b_ptrs + b_ritems + b_groups;
+        const size_t b_recs = align_up(std::max<size_t>(1, recs.size()) * sizeof(DevRecipe));
+        const size_t b_facs = align_up(std::max<size_t>(1, facs.size()) * sizeof(TableFactor));
+        const size_t ibytes = b_titems + b_ptrs + b_ritems + b_groups + b_recs + b_facs;
         grow(h_items_, ch_items_, ibytes, true);
         grow(d_items_, c_items_, ibytes, false);
         char *hi = static_cast<char *>(h_items_);
@@ -458,6 +502,14 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
         }
         std::memcpy(hi + b_titems + b_ptrs, ritems.data(), ritems.size() * sizeof(BatchRedItem<T>));
         std::memcpy(hi + b_titems + b_ptrs + b_ritems, groups.data(), groups.size() * sizeof(PauliGroup));
+        auto *d_recs = reinterpret_cast<DevRecipe *>(di + b_titems + b_ptrs + b_ritems + b_groups);
+        auto *d_facs = reinterpret_cast<TableFactor *>(di + b_titems + b_ptrs + b_ritems + b_groups + b_recs);
+        for (auto &r : recs) {
+            r.fac = d_facs + reinterpret_cast<size_t>(r.fac);
+        }
+        std::memcpy(hi + b_titems + b_ptrs + b_ritems + b_groups, recs.data(), recs.size() * sizeof(DevRecipe));
+        std::memcpy(hi + b_titems + b_ptrs + b_ritems + b_groups + b_recs, facs.data(),
+                    facs.size() * sizeof(TableFactor));
 
         const size_t nred = std::max<size_t>(1, ritems.size());
         grow(d_red_, c_red_, (rblocks + nred) * sizeof(double), false);
@@ -470,6 +522,9 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
         cuda_check(cudaMemcpyAsync(dp, hp, pbytes, cudaMemcpyHostToDevice, s_), "H2D programs");
         cuda_check(cudaMemcpyAsync(di, hi, ibytes, cudaMemcpyHostToDevice, s_), "H2D items");
         cuda_check(cudaMemsetAsync(states, 0, sv_bytes, s_), "memset registers");
+        launch_expand_tables(s_, d_recs, static_cast<int>(recs.size()), rec_entries,
+                             use_df ? 2 : (std::is_same_v<T, float> ? 0 : 1));
+        stats_.launches += recs.empty() ? 0 : 1;
         if (use_df) { // registers stay double-float pairs from |0..0> to the reductions
             launch_batch_set_one<df>(s_, reinterpret_cast<cx<df> *const *>(d_ptrs), wn);
         } else {
@@ -550,6 +605,8 @@ template <class T> std::string BatchEngine<T>::stats_json() const {
                      ", \"double_float\": " + std::string(stats_.df ? "true" : "false") +
                      ", \"compile_ms\": " + std::to_string(stats_.compile_ms) +
                      ", \"device_ms\": " + std::to_string(stats_.device_ms) +
+                     ", \"pack_ms\": " + std::to_string(stats_.pack_ms) +
+                     ", \"program_bytes\": " + std::to_string(stats_.program_bytes) +
                      ", \"total_ms\": " + std::to_string(stats_.total_ms) + ", \"tile_bits\": {";
     bool first = true;
     for (const auto &kv : stats_.tile_bits) {

@@ -42,6 +42,16 @@ template <class T> struct BatchRedItem {
 
 constexpr u64 kBatchRedChunk = 4096; // amplitudes or pairs per reduction block
 
+// one merged-diagonal table to expand on the device (batch engine)
+struct DevRecipe {
+    void *dst;          // first entry of the table in the program arena
+    const TableFactor *fac;
+    int t, nfac;
+    u64 entry_begin;    // first global entry index of this table in the launch
+};
+// enc: 0 = complex64, 1 = complex128, 2 = complex128 as double-float pairs
+void launch_expand_tables(cudaStream_t s, const DevRecipe *recipes, int nrec, u64 total_entries, int enc);
+
 template <class T>
 void launch_tile_reg_batch(cudaStream_t s, int t, const BatchTileItem<T> *items, int nitems, u64 total_tiles);
 template <class T> void launch_batch_set_one(cudaStream_t s, cx<T> *const *svs, int n);
@@ -72,7 +82,7 @@ int gate_code_count();
 struct BatchStats {
     int ncirc{0}, waves{0}, launches{0}, max_passes{0}, padded{0}, fallback{0};
     bool df{false};
-    double compile_ms{0}, device_ms{0}, total_ms{0};
+    double compile_ms{0}, device_ms{0}, total_ms{0}, pack_ms{0}, program_bytes{0};
     std::map<int, int> tile_bits; // register size -> tile bits used
     std::vector<double> wave_done_ms; // completion time of each wave, from the start of run()
     std::vector<int> wave_of;         // wave index of each circuit

@@ -2,6 +2,7 @@
 #include "pl_gb300.h"
 
 #include "batch.hpp"
+#include "fused.hpp"
 #include "host.hpp"
 
 #include <algorithm>
@@ -449,6 +450,13 @@ int plgb_batch_stats(const plgb_batch *b, char *buf, size_t len) {
     return rc != PLGB_OK ? rc : copy_text(js, buf, len);
 }
 const char *plgb_gate_name(int code) { return gate_name_of(code); }
+int plgb_set_tile_variant(int precision, int occ) {
+    if (precision != 64 && precision != 128) {
+        set_last_error("precision must be 64 or 128");
+        return -1;
+    }
+    return set_tile_variant_occ(precision, occ != 0) ? 1 : 0;
+}
 int plgb_set_c128_fp64_passes(int on) {
     const bool prev = c128_fp64_passes();
     set_c128_fp64_passes(on != 0);

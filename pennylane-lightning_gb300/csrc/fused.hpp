@@ -98,6 +98,26 @@ void launch_tile_pass_adj(cudaStream_t s, cx<T> *lam, cx<T> *hlam, const TilePas
 int adj_grid_capacity(size_t tile_bytes_each);
 void launch_adj_sum(cudaStream_t s, const double *partials, int nslots, int G, double *out);
 
+// A merged-diagonal table of 2^t entries described by its factors instead
+// of its values (batch engine: expanded on the device).  Entry j is the
+// product over factors of val[k], k = the bits of j at pos[0..nb) (first =
+// most significant).
+struct TableFactor {
+    int nb;
+    int pos[4];
+    cx<double> val[16];
+};
+struct TableRecipe {
+    int table_off; // entry offset in the program's table area
+    int t;         // 2^t entries
+    int fac_begin, nfac;
+};
+
+// Register-tile kernel variant per precision (64 or 128): false = up to 255
+// registers per thread, true = at most 128 (twice the resident warps).
+bool tile_variant_occ(int precision);
+bool set_tile_variant_occ(int precision, bool occ);
+
 struct df;
 // Complex128 passes in double-float arithmetic (df.cuh).  io: 0 = doubles in
 // and out, 1 = doubles in / df out (first pass of a program), 2 = df in and

@@ -5,6 +5,8 @@
 #include "fused.hpp"
 #include "host.hpp"
 
+#include <array>
+
 namespace plgb {
 
 template <class T> struct FusedProgram {
@@ -32,6 +34,13 @@ template <class T> struct FusedProgram {
     std::vector<DiagForm<T>> h_forms;
     std::vector<cx<T>> h_tables;
     std::vector<StageDesc> h_stages;
+    // recipe mode (compile_fused with recipes): h_tables stays empty; the
+    // table area holds table_entries entries built from these on the device
+    std::vector<TableRecipe> h_recipes;
+    std::vector<TableFactor> h_factors;
+    size_t table_entries{0};
+    // h_tables chunks: (entry offset in the table area, offset in h_tables, count)
+    std::vector<std::array<size_t, 3>> h_table_chunks;
     int n{0};
     size_t passes{0}, unfused{0}, prims{0};
     std::string plan; // JSON lines of the segments

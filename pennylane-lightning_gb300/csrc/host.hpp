@@ -204,7 +204,7 @@ template <class T> class StateVector {
 template <class T> struct FusedProgram;
 template <class T>
 std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>> &prims, int tile_bits,
-                                               bool upload = true);
+                                               bool upload = true, bool recipes = false);
 // Arithmetic of fused complex128 passes: double-float on the FP32 pipe
 // (default) or FP64.
 void set_c128_fp64_passes(bool on);

@@ -530,7 +530,9 @@ bool plan_stages(std::vector<TileOp<T>> &ops, const std::vector<DiagForm<T>> &fo
 }
 
 template <class T>
-std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>> &in, int tile_bits, bool upload) {
+std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>> &in, int tile_bits, bool upload,
+                                               bool recipes) {
+    PLGB_REQUIRE(!(upload && recipes), "fusion: table recipes are for host-side programs");
     auto prog = std::make_shared<FusedProgram<T>>();
     prog->n = n;
     // a tile of 2^t amplitudes must fit the 200 KiB of shared memory the tile
@@ -807,6 +809,69 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
                     bitf[lp][1] *= dg.tab[1];
                 }
             }
+            // recipe mode: the table's factors instead of its 2^t values
+            // (possible while every multi-bit local factor has <= 4 bits)
+            bool as_recipe = recipes;
+            for (auto &dg : pend) {
+                bool all_local = true;
+                for (int b : dg.bits) {
+                    all_local = all_local && is_local(b);
+                }
+                if (all_local && dg.bits.size() > 4) {
+                    as_recipe = false;
+                }
+            }
+            TableRecipe rec{0, d.t, static_cast<int>(prog->h_factors.size()), 0};
+            if (as_recipe) {
+                auto C = [](std::complex<double> v) { return cx<double>{v.real(), v.imag()}; };
+                for (int lp = 0; lp < d.t; lp++) {
+                    if ((bitf_used >> lp) & 1U) {
+                        TableFactor f{};
+                        f.nb = 1;
+                        f.pos[0] = lp;
+                        f.val[0] = C(bitf[lp][0]);
+                        f.val[1] = C(bitf[lp][1]);
+                        prog->h_factors.push_back(f);
+                    }
+                }
+                for (auto &dg : pend) {
+                    bool all_local = true;
+                    for (int b : dg.bits) {
+                        all_local = all_local && is_local(b);
+                    }
+                    if (!all_local || dg.bits.size() == 1) {
+                        continue;
+                    }
+                    TableFactor f{};
+                    f.nb = static_cast<int>(dg.bits.size());
+                    for (int i = 0; i < f.nb; i++) {
+                        f.pos[i] = lpos(dg.bits[static_cast<size_t>(i)]);
+                    }
+                    for (size_t i = 0; i < dg.tab.size(); i++) {
+                        f.val[i] = C(dg.tab[i]);
+                    }
+                    prog->h_factors.push_back(f);
+                }
+                rec.nfac = static_cast<int>(prog->h_factors.size()) - rec.fac_begin;
+            }
+            const bool table_needed = [&] {
+                if (bitf_used) {
+                    return true;
+                }
+                for (auto &dg : pend) {
+                    bool all_local = true;
+                    for (int b : dg.bits) {
+                        all_local = all_local && is_local(b);
+                    }
+                    if (all_local) {
+                        return true;
+                    }
+                }
+                return false;
+            }();
+            if (as_recipe) {
+                bitf_used = 0; // nothing to materialise on the host
+            }
             if (bitf_used) {
                 tab.assign(size_t{1} << d.t, {1.0, 0.0});
                 has_table = true;
@@ -831,6 +896,9 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
                 }
                 if (nglob == 0 && dg.bits.size() == 1) {
                     continue; // in the per-bit factors above
+                }
+                if (nglob == 0 && as_recipe) {
+                    continue; // a recipe factor
                 }
                 if (nglob == 0) {
                     if (!has_table) {
@@ -881,12 +949,19 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
             bool first = true;
             while (first || gi < gforms.size() || mi < mforms.size()) {
                 TileOp<T> o = op;
-                o.has_table = first && has_table ? 1 : 0;
-                if (o.has_table) {
-                    o.table_off = static_cast<int>(tables.size());
+                o.has_table = first && (has_table || (as_recipe && table_needed)) ? 1 : 0;
+                if (o.has_table && as_recipe) {
+                    o.table_off = static_cast<int>(prog->table_entries);
+                    rec.table_off = o.table_off;
+                    prog->h_recipes.push_back(rec);
+                    prog->table_entries += size_t{1} << d.t;
+                } else if (o.has_table) {
+                    o.table_off = static_cast<int>(prog->table_entries);
+                    prog->h_table_chunks.push_back({prog->table_entries, tables.size(), tab.size()});
                     for (auto &v : tab) {
                         tables.push_back(cx<T>{static_cast<T>(v.real()), static_cast<T>(v.imag())});
                     }
+                    prog->table_entries += tab.size();
                 }
                 o.gform_begin = static_cast<int>(forms.size());
                 const size_t gtake = std::min<size_t>(gforms.size() - gi, 64);
@@ -1198,9 +1273,10 @@ template FusedStats fused_stats<double>(const FusedProgram<double> &);
 
 template struct FusedProgram<float>;
 template struct FusedProgram<double>;
-template std::shared_ptr<FusedProgram<float>> compile_fused<float>(int, const std::vector<Prim<float>> &, int, bool);
+template std::shared_ptr<FusedProgram<float>> compile_fused<float>(int, const std::vector<Prim<float>> &, int, bool,
+                                                                   bool);
 template std::shared_ptr<FusedProgram<double>> compile_fused<double>(int, const std::vector<Prim<double>> &, int,
-                                                                     bool);
+                                                                     bool, bool);
 template void run_fused_adjoint<float>(StateVector<float> &, StateVector<float> &, const FusedProgram<float> &,
                                        double *, int);
 template void run_fused_adjoint<double>(StateVector<double> &, StateVector<double> &, const FusedProgram<double> &,

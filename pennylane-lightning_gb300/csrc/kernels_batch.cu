@@ -8,8 +8,8 @@
 
 namespace plgb {
 
-template <class T>
-__global__ void __launch_bounds__(256, 1)
+template <class T, bool OCC>
+__global__ void __launch_bounds__(256, OCC ? 2 : 1)
     k_tile_reg_batch(const BatchTileItem<T> *__restrict__ items, int nitems, u64 total_tiles) {
     extern __shared__ unsigned char smraw[];
     cx<T> *tile = reinterpret_cast<cx<T> *>(smraw);
@@ -40,29 +40,81 @@ __global__ void __launch_bounds__(256, 1)
     }
 }
 
-template <class T>
-void launch_tile_reg_batch(cudaStream_t s, int t, const BatchTileItem<T> *items, int nitems, u64 total_tiles) {
-    if (t < kMinRegTileBits || t > 12 || nitems < 1 || total_tiles < 1) {
-        throw std::runtime_error("batched tile pass: unsupported geometry");
-    }
+template <class T, bool OCC>
+static void launch_batch_impl(cudaStream_t s, int t, const BatchTileItem<T> *items, int nitems, u64 total_tiles) {
     const int threads = 1 << (t - kRegBits);
     const size_t smem = sizeof(cx<T>) << t;
     static bool attr = false;
     if (!attr) {
-        cuda_check(cudaFuncSetAttribute(k_tile_reg_batch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
-                   "tile_reg_batch smem attribute");
+        cuda_check(cudaFuncSetAttribute(k_tile_reg_batch<T, OCC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        200 * 1024), "tile_reg_batch smem attribute");
         attr = true;
     }
     int per_sm = 1;
-    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_reg_batch<T>, threads, smem),
+    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_reg_batch<T, OCC>, threads, smem),
                "occupancy");
     if (per_sm < 1) {
         throw std::runtime_error("batched tile pass: tile does not fit one SM");
     }
     const u64 cap = static_cast<u64>(LaunchGeom::sm_count()) * static_cast<u64>(per_sm);
     const unsigned grid = static_cast<unsigned>(total_tiles < cap ? total_tiles : cap);
-    k_tile_reg_batch<T><<<grid, threads, smem, s>>>(items, nitems, total_tiles);
+    k_tile_reg_batch<T, OCC><<<grid, threads, smem, s>>>(items, nitems, total_tiles);
     cuda_check(cudaGetLastError(), "k_tile_reg_batch launch");
+    note_launch();
+}
+
+template <class T>
+void launch_tile_reg_batch(cudaStream_t s, int t, const BatchTileItem<T> *items, int nitems, u64 total_tiles) {
+    if (t < kMinRegTileBits || t > 12 || nitems < 1 || total_tiles < 1) {
+        throw std::runtime_error("batched tile pass: unsupported geometry");
+    }
+    if (tile_variant_occ(std::is_same_v<T, float> ? 64 : 128)) {
+        launch_batch_impl<T, true>(s, t, items, nitems, total_tiles);
+    } else {
+        launch_batch_impl<T, false>(s, t, items, nitems, total_tiles);
+    }
+}
+
+// Entry j of a table: the product of its factors' values at the bits of j.
+__global__ void k_expand_tables(const DevRecipe *__restrict__ rec, int nrec, u64 total, int enc) {
+    for (u64 e = static_cast<u64>(blockIdx.x) * blockDim.x + threadIdx.x; e < total;
+         e += static_cast<u64>(gridDim.x) * blockDim.x) {
+        int lo = 0, hi = nrec - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (rec[mid].entry_begin <= e) {
+                lo = mid;
+            } else {
+                hi = mid - 1;
+            }
+        }
+        const DevRecipe &r = rec[lo];
+        const u32 j = static_cast<u32>(e - r.entry_begin);
+        cx<double> v{1.0, 0.0};
+        for (int f = 0; f < r.nfac; f++) {
+            const TableFactor &tf = r.fac[f];
+            unsigned k = 0;
+            for (int b = 0; b < tf.nb; b++) {
+                k = (k << 1) | ((j >> tf.pos[b]) & 1u);
+            }
+            v = v * tf.val[k];
+        }
+        if (enc == 0) {
+            static_cast<cx<float> *>(r.dst)[j] = cx<float>{static_cast<float>(v.x), static_cast<float>(v.y)};
+        } else if (enc == 1) {
+            static_cast<cx<double> *>(r.dst)[j] = v;
+        } else {
+            static_cast<cx<df> *>(r.dst)[j] = cx<df>{df(v.x), df(v.y)};
+        }
+    }
+}
+
+void launch_expand_tables(cudaStream_t s, const DevRecipe *recipes, int nrec, u64 total_entries, int enc) {
+    if (nrec < 1 || total_entries == 0) {
+        return;
+    }
+    k_expand_tables<<<grid_for(total_entries, 256, 8), 256, 0, s>>>(recipes, nrec, total_entries, enc);
+    cuda_check(cudaGetLastError(), "k_expand_tables launch");
     note_launch();
 }
 

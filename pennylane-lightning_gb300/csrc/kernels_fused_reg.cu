@@ -12,14 +12,21 @@
 // applied in registers from the per-pass table.
 #include "tile_reg.cuh"
 
+#include <atomic>
+
 namespace plgb {
 
-template <class T>
-__global__ void __launch_bounds__(256, 1) k_tile_reg(cx<T> *__restrict__ a, const TilePassDesc d,
-                                                  const TileOp<T> *__restrict__ ops,
-                                                  const DiagForm<T> *__restrict__ forms,
-                                                  const cx<T> *__restrict__ tables,
-                                                  const StageDesc *__restrict__ stages) {
+// OCC: launch bounds that cap registers at 128 per thread (16 warps per SM
+// for 2^11-amplitude tiles instead of 8), trading some spills for latency
+// hiding; chosen per precision (tile_variant_occ).
+#define PLGB_TILE_BOUNDS(OCC) __launch_bounds__(256, (OCC) ? 2 : 1)
+
+template <class T, bool OCC>
+__global__ void PLGB_TILE_BOUNDS(OCC) k_tile_reg(cx<T> *__restrict__ a, const TilePassDesc d,
+                                                 const TileOp<T> *__restrict__ ops,
+                                                 const DiagForm<T> *__restrict__ forms,
+                                                 const cx<T> *__restrict__ tables,
+                                                 const StageDesc *__restrict__ stages) {
     extern __shared__ unsigned char smraw[];
     cx<T> *tile = reinterpret_cast<cx<T> *>(smraw);
     __shared__ TileShared<T> sh;
@@ -34,12 +41,12 @@ __global__ void __launch_bounds__(256, 1) k_tile_reg(cx<T> *__restrict__ a, cons
     }
 }
 
-template <class SI, class SO>
-__global__ void __launch_bounds__(256, 1) k_tile_reg_df(const cx<SI> *ain, cx<SO> *aout, const TilePassDesc d,
-                                                     const TileOp<df> *__restrict__ ops,
-                                                     const DiagForm<df> *__restrict__ forms,
-                                                     const cx<df> *__restrict__ tables,
-                                                     const StageDesc *__restrict__ stages) {
+template <class SI, class SO, bool OCC>
+__global__ void PLGB_TILE_BOUNDS(OCC) k_tile_reg_df(const cx<SI> *ain, cx<SO> *aout, const TilePassDesc d,
+                                                    const TileOp<df> *__restrict__ ops,
+                                                    const DiagForm<df> *__restrict__ forms,
+                                                    const cx<df> *__restrict__ tables,
+                                                    const StageDesc *__restrict__ stages) {
     extern __shared__ unsigned char smraw[];
     cx<df> *tile = reinterpret_cast<cx<df> *>(smraw);
     __shared__ TileShared<df> sh;
@@ -53,29 +60,52 @@ __global__ void __launch_bounds__(256, 1) k_tile_reg_df(const cx<SI> *ain, cx<SO
     }
 }
 
-template <class SI, class SO>
+namespace {
+std::atomic<int> g_occ_c64{1}, g_occ_c128{1}; // measured faster on GB300 for both
+} // namespace
+bool tile_variant_occ(int precision) { return (precision == 128 ? g_occ_c128 : g_occ_c64).load() != 0; }
+bool set_tile_variant_occ(int precision, bool occ) {
+    return (precision == 128 ? g_occ_c128 : g_occ_c64).exchange(occ ? 1 : 0) != 0;
+}
+
+// persistent grid: SMs x resident CTAs of this kernel and tile size
+template <class K> static unsigned tile_grid(K kernel, int threads, size_t smem, u64 ntiles, bool &attr) {
+    if (!attr) {
+        cuda_check(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
+                   "tile smem attribute");
+        attr = true;
+    }
+    int per_sm = 1;
+    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem), "occupancy");
+    if (per_sm < 1) {
+        throw std::runtime_error("register tile pass: tile does not fit one SM");
+    }
+    const u64 cap = static_cast<u64>(LaunchGeom::sm_count()) * static_cast<u64>(per_sm);
+    return static_cast<unsigned>(ntiles < cap ? ntiles : cap);
+}
+
+template <class SI, class SO, bool OCC>
 static void launch_df(cudaStream_t s, void *sv, const TilePassDesc &d, const TileOp<df> *ops, const DiagForm<df> *forms,
                       const cx<df> *tables, const StageDesc *stages) {
     const int threads = 1 << (d.t - kRegBits);
     const size_t smem = sizeof(cx<df>) << d.t;
     static bool attr = false;
-    if (!attr) {
-        cuda_check(cudaFuncSetAttribute(k_tile_reg_df<SI, SO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        200 * 1024), "tile_reg_df smem attribute");
-        attr = true;
-    }
-    int per_sm = 1;
-    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_reg_df<SI, SO>, threads, smem),
-               "occupancy");
-    if (per_sm < 1) {
-        throw std::runtime_error("register tile pass (df): tile does not fit one SM");
-    }
-    const u64 cap = static_cast<u64>(LaunchGeom::sm_count()) * static_cast<u64>(per_sm);
-    const unsigned grid = static_cast<unsigned>(d.ntiles < cap ? d.ntiles : cap);
-    k_tile_reg_df<SI, SO><<<grid, threads, smem, s>>>(static_cast<const cx<SI> *>(sv), static_cast<cx<SO> *>(sv), d,
-                                                      ops, forms, tables, stages);
+    const unsigned grid = tile_grid(k_tile_reg_df<SI, SO, OCC>, threads, smem, d.ntiles, attr);
+    k_tile_reg_df<SI, SO, OCC><<<grid, threads, smem, s>>>(static_cast<const cx<SI> *>(sv), static_cast<cx<SO> *>(sv),
+                                                           d, ops, forms, tables, stages);
     cuda_check(cudaGetLastError(), "k_tile_reg_df launch");
     note_launch();
+}
+
+template <bool OCC>
+static void launch_df_io(cudaStream_t s, void *sv, int io, const TilePassDesc &d, const TileOp<df> *ops,
+                         const DiagForm<df> *forms, const cx<df> *tables, const StageDesc *stages) {
+    switch (io) {
+    case 0: launch_df<double, double, OCC>(s, sv, d, ops, forms, tables, stages); break;
+    case 1: launch_df<double, df, OCC>(s, sv, d, ops, forms, tables, stages); break;
+    case 2: launch_df<df, df, OCC>(s, sv, d, ops, forms, tables, stages); break;
+    default: launch_df<df, double, OCC>(s, sv, d, ops, forms, tables, stages); break;
+    }
 }
 
 void launch_tile_pass_reg_df(cudaStream_t s, void *sv, int io, const TilePassDesc &d, const TileOp<df> *ops,
@@ -83,12 +113,23 @@ void launch_tile_pass_reg_df(cudaStream_t s, void *sv, int io, const TilePassDes
     if (d.t < kMinRegTileBits || d.t > 12 || d.ndiag > kMaxDiagOpsPerPass) {
         throw std::runtime_error("register tile pass (df): unsupported geometry");
     }
-    switch (io) {
-    case 0: launch_df<double, double>(s, sv, d, ops, forms, tables, stages); break;
-    case 1: launch_df<double, df>(s, sv, d, ops, forms, tables, stages); break;
-    case 2: launch_df<df, df>(s, sv, d, ops, forms, tables, stages); break;
-    default: launch_df<df, double>(s, sv, d, ops, forms, tables, stages); break;
+    if (tile_variant_occ(128)) {
+        launch_df_io<true>(s, sv, io, d, ops, forms, tables, stages);
+    } else {
+        launch_df_io<false>(s, sv, io, d, ops, forms, tables, stages);
     }
+}
+
+template <class T, bool OCC>
+static void launch_reg(cudaStream_t s, cx<T> *sv, const TilePassDesc &d, const TileOp<T> *ops, const DiagForm<T> *forms,
+                       const cx<T> *tables, const StageDesc *stages) {
+    const int threads = 1 << (d.t - kRegBits);
+    const size_t smem = sizeof(cx<T>) << d.t;
+    static bool attr = false;
+    const unsigned grid = tile_grid(k_tile_reg<T, OCC>, threads, smem, d.ntiles, attr);
+    k_tile_reg<T, OCC><<<grid, threads, smem, s>>>(sv, d, ops, forms, tables, stages);
+    cuda_check(cudaGetLastError(), "k_tile_reg launch");
+    note_launch();
 }
 
 template <class T>
@@ -97,24 +138,11 @@ void launch_tile_pass_reg(cudaStream_t s, cx<T> *sv, const TilePassDesc &d, cons
     if (d.t < kMinRegTileBits || d.t > 12 || d.ndiag > kMaxDiagOpsPerPass) {
         throw std::runtime_error("register tile pass: unsupported geometry");
     }
-    const int threads = 1 << (d.t - kRegBits);
-    const size_t smem = sizeof(cx<T>) << d.t;
-    static bool attr = false;
-    if (!attr) {
-        cuda_check(cudaFuncSetAttribute(k_tile_reg<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
-                   "tile_reg smem attribute");
-        attr = true;
+    if (tile_variant_occ(sizeof(T) == 8 ? 128 : 64)) {
+        launch_reg<T, true>(s, sv, d, ops, forms, tables, stages);
+    } else {
+        launch_reg<T, false>(s, sv, d, ops, forms, tables, stages);
     }
-    int per_sm = 1;
-    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_reg<T>, threads, smem), "occupancy");
-    if (per_sm < 1) {
-        throw std::runtime_error("register tile pass: tile does not fit one SM");
-    }
-    const u64 cap = static_cast<u64>(LaunchGeom::sm_count()) * static_cast<u64>(per_sm);
-    const unsigned grid = static_cast<unsigned>(d.ntiles < cap ? d.ntiles : cap);
-    k_tile_reg<T><<<grid, threads, smem, s>>>(sv, d, ops, forms, tables, stages);
-    cuda_check(cudaGetLastError(), "k_tile_reg launch");
-    note_launch();
 }
 
 template void launch_tile_pass_reg<float>(cudaStream_t, cx<float> *, const TilePassDesc &, const TileOp<float> *,

@@ -61,6 +61,7 @@ SIGNATURES = {
     "plgb_batch_stats": (C.c_int, [VP, C.c_char_p, C.c_size_t]),
     "plgb_gate_name": (C.c_char_p, [C.c_int]),
     "plgb_set_c128_fp64_passes": (C.c_int, [C.c_int]),
+    "plgb_set_tile_variant": (C.c_int, [C.c_int, C.c_int]),
     "plgb_meas_expval_sparse": (C.c_int, [VP, I64P, C.c_int64, I64P, DP, C.c_int64, DP]),
     "plgb_meas_expval_obs": (C.c_int, [VP, VP, DP]),
     "plgb_meas_var_obs": (C.c_int, [VP, VP, DP]),

@@ -74,6 +74,16 @@ def _text(fn, *args, size=4096) -> str:
 
 
 # --------------------------------------------------------------------------- module functions
+def set_tile_variant(precision: int, occ: bool) -> bool:
+    """Register-tile kernel variant for complex64 (64) or complex128 (128):
+    occ=True caps registers at 128 per thread (more resident warps);
+    returns the previous setting."""
+    rc = lib().plgb_set_tile_variant(int(precision), 1 if occ else 0)
+    if rc < 0:
+        raise LightningException("precision must be 64 or 128")
+    return bool(rc)
+
+
 def set_c128_fp64_passes(on: bool) -> bool:
     """Fused complex128 passes in FP64 (True) or double-float arithmetic on
     the FP32 pipe (False, the default); returns the previous setting."""

@@ -183,6 +183,11 @@ int plgb_sv_apply_operations(plgb_sv *sv, plgb_ops *ops, int tile_bits, int *pas
  * (about 48 significant bits; GB300 executes FP64 at 1/64 of its FP32
  * rate), on = 1 in FP64.  Process-wide; returns the previous setting. */
 int plgb_set_c128_fp64_passes(int on);
+/* Register-tile kernel variant for a precision (64 or 128): occ = 0 lets a
+ * thread use up to 255 registers, occ = 1 caps it at 128 (twice the
+ * resident warps, some spills).  Returns the previous setting, or -1 for a
+ * bad precision (no counterpart in the reference). */
+int plgb_set_tile_variant(int precision, int occ);
 /* Plan introspection (no device needed): the tile passes plgb_sv_apply_operations
  * would run for `ops` on num_qubits at precision / tile_bits, as a JSON array
  * with one object per pass (tile size, op counts, execution stages). */

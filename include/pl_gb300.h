@@ -239,6 +239,19 @@ int plgb_batch_run(plgb_batch *b, int ncirc, const int32_t *num_qubits, const in
                    const int32_t *op_codes, const int32_t *op_wires, const double *op_params, const uint8_t *op_inverse,
                    const int64_t *obs_offsets, const int64_t *term_offsets, const double *term_coeffs,
                    const uint64_t *term_x, const uint64_t *term_y, const uint64_t *term_z, double *out);
+/* Adjoint requests in the same packed layout: for each circuit, <O> of each
+ * of its observables into values (one per observable) and the Jacobian of
+ * each <O> with respect to the parameter of every parametric gate of the
+ * circuit (the in-place adjoint sweep; AdjointJacobianLQubit.hpp:225-491)
+ * into jac: circuit after circuit, per circuit one row per observable of
+ * (number of parametric gates) entries.  Circuits run concurrently on host
+ * threads, each on its own stream, three registers each within the
+ * engine's memory budget. */
+int plgb_batch_adjoint(plgb_batch *b, int ncirc, const int32_t *num_qubits, const int64_t *op_offsets,
+                       const int32_t *op_codes, const int32_t *op_wires, const double *op_params,
+                       const uint8_t *op_inverse, const int64_t *obs_offsets, const int64_t *term_offsets,
+                       const double *term_coeffs, const uint64_t *term_x, const uint64_t *term_y,
+                       const uint64_t *term_z, double *values, double *jac);
 /* JSON of the last run: waves, launches, tile sizes, compile and device ms,
  * completion time of each wave and the wave of each circuit */
 int plgb_batch_stats(const plgb_batch *b, char *buf, size_t len);

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <condition_variable>
 #include <chrono>
 #include <cstring>
 #include <thread>
@@ -593,6 +594,149 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
         stats_.padded += cc.ne != cc.n ? 1 : 0;
     }
     stats_.device_ms = dev_ms_total;
+    stats_.total_ms = ms_since(t_start);
+}
+
+template <class T> void BatchEngine<T>::run_adjoint(const BatchInput &in, double *values, double *jac) {
+    std::lock_guard<std::mutex> lk(mu_);
+    const auto t_start = std::chrono::steady_clock::now();
+    stats_ = BatchStats{};
+    const int nc = in.ncirc;
+    stats_.ncirc = nc;
+    if (nc <= 0) {
+        return;
+    }
+    PLGB_REQUIRE(in.num_qubits && in.op_offsets && in.obs_offsets && in.term_offsets, "batch: missing arrays");
+    // per circuit: its parametric-op count and where its Jacobian rows start
+    std::vector<int64_t> npar(static_cast<size_t>(nc), 0), jac_off(static_cast<size_t>(nc) + 1, 0);
+    for (int c = 0; c < nc; c++) {
+        const int n = in.num_qubits[c];
+        PLGB_REQUIRE(n >= 1 && n <= kBatchMaxQubits, "batch: number of qubits must be in 1..30");
+        for (int64_t o = in.op_offsets[c]; o < in.op_offsets[c + 1]; o++) {
+            const char *name = gate_name_of(in.op_codes[o]);
+            PLGB_REQUIRE(name != nullptr, "batch: unknown gate code");
+            npar[static_cast<size_t>(c)] += gate_param_count(name) > 0 ? 1 : 0;
+        }
+        jac_off[static_cast<size_t>(c) + 1] =
+            jac_off[static_cast<size_t>(c)] + npar[static_cast<size_t>(c)] * (in.obs_offsets[c + 1] - in.obs_offsets[c]);
+    }
+    std::mutex bmu;
+    std::condition_variable bcv;
+    size_t in_use = 0;
+    int active = 0;
+    std::atomic<int> next{0};
+    std::vector<std::string> errors(static_cast<size_t>(nc));
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    auto worker = [&]() {
+        cudaSetDevice(dev);
+        for (int c = next++; c < nc; c = next++) {
+            const int n = in.num_qubits[c];
+            const size_t need = size_t{3} * (sizeof(cx<T>) << n);
+            {
+                std::unique_lock<std::mutex> g(bmu);
+                bcv.wait(g, [&] { return active == 0 || in_use + need <= wave_bytes_; });
+                in_use += need;
+                active++;
+            }
+            try {
+                OpsList ops;
+                for (int64_t o = in.op_offsets[c]; o < in.op_offsets[c + 1]; o++) {
+                    OpRec r;
+                    r.name = gate_name_of(in.op_codes[o]);
+                    for (int k = 0; k < kMaxWiresPerOp; k++) {
+                        const int w = in.op_wires[kMaxWiresPerOp * o + k];
+                        if (w >= 0) {
+                            PLGB_REQUIRE(w < n, "batch: wire index out of range");
+                            r.wires.push_back(w);
+                        }
+                    }
+                    r.params.assign(in.op_params + 3 * o, in.op_params + 3 * o + gate_param_count(r.name));
+                    r.inverse = in.op_inverse ? in.op_inverse[o] != 0 : false;
+                    ops.ops.push_back(std::move(r));
+                }
+                std::vector<ObsPtr> obs;
+                for (int64_t ob = in.obs_offsets[c]; ob < in.obs_offsets[c + 1]; ob++) {
+                    auto h = std::make_shared<ObsNode>();
+                    h->kind = ObsNode::Ham;
+                    for (int64_t tm = in.term_offsets[ob]; tm < in.term_offsets[ob + 1]; tm++) {
+                        auto prod = std::make_shared<ObsNode>();
+                        prod->kind = ObsNode::Prod;
+                        for (int w = 0; w < n; w++) {
+                            const char *letter = ((in.term_x[tm] >> w) & 1U)   ? "PauliX"
+                                                 : ((in.term_y[tm] >> w) & 1U) ? "PauliY"
+                                                 : ((in.term_z[tm] >> w) & 1U) ? "PauliZ"
+                                                                                 : nullptr;
+                            if (letter) {
+                                auto f = std::make_shared<ObsNode>();
+                                f->kind = ObsNode::Named;
+                                f->name = letter;
+                                f->wires = {w};
+                                prod->children.push_back(f);
+                            }
+                        }
+                        if (prod->children.empty()) {
+                            auto f = std::make_shared<ObsNode>();
+                            f->kind = ObsNode::Named;
+                            f->name = "Identity";
+                            f->wires = {0};
+                            prod->children.push_back(f);
+                        }
+                        h->children.push_back(prod);
+                        h->coeffs.push_back(in.term_coeffs[tm]);
+                    }
+                    obs.push_back(h);
+                }
+                StateVector<T> sv(n);
+                std::vector<Prim<T>> prims;
+                for (const auto &op : ops.ops) {
+                    auto p = sv.lower_op(op, op.inverse);
+                    prims.insert(prims.end(), std::make_move_iterator(p.begin()), std::make_move_iterator(p.end()));
+                }
+                const int t = n >= kMinRegTileBits ? tile_bits_for(n) : n;
+                auto prog = compile_fused<T>(n, prims, t, true);
+                run_fused<T>(sv, *prog);
+                for (size_t k = 0; k < obs.size(); k++) {
+                    values[in.obs_offsets[c] + static_cast<int64_t>(k)] = Measure<T>::expval_obs(sv, *obs[k]);
+                }
+                std::vector<int64_t> tp(static_cast<size_t>(npar[static_cast<size_t>(c)]));
+                for (size_t k = 0; k < tp.size(); k++) {
+                    tp[k] = static_cast<int64_t>(k);
+                }
+                const auto j = Adjoint<T>::jacobian(sv, obs, ops, tp, false, true);
+                std::copy(j.begin(), j.end(), jac + jac_off[static_cast<size_t>(c)]);
+            } catch (const std::exception &e) {
+                errors[static_cast<size_t>(c)] = e.what();
+            }
+            {
+                std::lock_guard<std::mutex> g(bmu);
+                in_use -= need;
+                active--;
+            }
+            bcv.notify_all();
+        }
+    };
+    // tile sizes are tuned on this thread first (they time kernels on the device)
+    for (int c = 0; c < nc; c++) {
+        if (in.num_qubits[c] >= kMinRegTileBits) {
+            tile_bits_for(in.num_qubits[c]);
+        }
+    }
+    int nt = threads_ > 0 ? threads_ : static_cast<int>(std::thread::hardware_concurrency());
+    nt = std::max(1, std::min({nt, 8, nc}));
+    std::vector<std::thread> pool;
+    for (int i = 1; i < nt; i++) {
+        pool.emplace_back(worker);
+    }
+    worker();
+    for (auto &th : pool) {
+        th.join();
+    }
+    for (const auto &e : errors) {
+        if (!e.empty()) {
+            throw PLError(e);
+        }
+    }
     stats_.total_ms = ms_since(t_start);
 }
 

@@ -78,6 +78,7 @@ struct BatchInput {
 
 const char *gate_name_of(int code); // nullptr past the end
 int gate_code_count();
+int gate_param_count(const std::string &name);
 
 struct BatchStats {
     int ncirc{0}, waves{0}, launches{0}, max_passes{0}, padded{0}, fallback{0};
@@ -98,6 +99,14 @@ template <class T> class BatchEngine {
     // Run every circuit from |0...0> and write one expectation value per
     // observable (in input order) to out.
     void run(const BatchInput &in, double *out);
+
+    // Adjoint requests: per circuit, <O> for each of its observables and the
+    // Jacobian d<O>/d(parameter of each parametric gate) (the in-place
+    // adjoint sweep).  Circuits run concurrently on host threads with their
+    // own streams, within the engine's memory budget (three registers each).
+    // values: one per observable; jac: per circuit, observable-major rows of
+    // its parametric-gate count.
+    void run_adjoint(const BatchInput &in, double *values, double *jac);
 
     // Tile size for a register of n qubits: fixed, or measured once per n
     // (autotune) over the candidates the register kernel supports.

@@ -441,6 +441,34 @@ int plgb_batch_run(plgb_batch *b, int ncirc, const int32_t *num_qubits, const in
         b->precision == 128 ? b->d->run(in, out) : b->f->run(in, out);
     });
 }
+int plgb_batch_adjoint(plgb_batch *b, int ncirc, const int32_t *num_qubits, const int64_t *op_offsets,
+                       const int32_t *op_codes, const int32_t *op_wires, const double *op_params,
+                       const uint8_t *op_inverse, const int64_t *obs_offsets, const int64_t *term_offsets,
+                       const double *term_coeffs, const uint64_t *term_x, const uint64_t *term_y,
+                       const uint64_t *term_z, double *values, double *jac) {
+    return guard([&] {
+        need(b, "batch");
+        BatchInput in;
+        in.ncirc = ncirc;
+        in.num_qubits = num_qubits;
+        in.op_offsets = op_offsets;
+        in.op_codes = op_codes;
+        in.op_wires = op_wires;
+        in.op_params = op_params;
+        in.op_inverse = op_inverse;
+        in.obs_offsets = obs_offsets;
+        in.term_offsets = term_offsets;
+        in.term_coeffs = term_coeffs;
+        in.term_x = term_x;
+        in.term_y = term_y;
+        in.term_z = term_z;
+        if (ncirc > 0) {
+            need(values, "values");
+            need(jac, "jac");
+        }
+        b->precision == 128 ? b->d->run_adjoint(in, values, jac) : b->f->run_adjoint(in, values, jac);
+    });
+}
 int plgb_batch_stats(const plgb_batch *b, char *buf, size_t len) {
     std::string js;
     const int rc = guard([&] {

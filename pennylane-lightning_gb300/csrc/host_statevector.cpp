@@ -84,6 +84,22 @@ const char *gate_name_of(int code) {
     return code >= 0 && code < k ? kGateNames[code] : nullptr;
 }
 int gate_code_count() { return static_cast<int>(sizeof(kGateNames) / sizeof(kGateNames[0])); }
+int gate_param_count(const std::string &name) {
+    if (name == "Rot" || name == "CRot") {
+        return 3;
+    }
+    if (name == "PCPhase") {
+        return 2;
+    }
+    static const char *kNoParam[] = {"Identity", "PauliX", "PauliY", "PauliZ", "Hadamard", "S", "SX", "T", "CNOT",
+                                     "CY", "CZ", "SWAP", "Toffoli", "CSWAP"};
+    for (auto *g : kNoParam) {
+        if (name == g) {
+            return 0;
+        }
+    }
+    return 1;
+}
 
 bool is_named_gate(const std::string &name) {
     for (auto *g : kGateNames) {

@@ -58,6 +58,7 @@ SIGNATURES = {
     "plgb_batch_destroy": (C.c_int, [VP]),
     "plgb_batch_configure": (C.c_int, [VP, C.c_int, C.c_int64, C.c_int]),
     "plgb_batch_run": (C.c_int, [VP, C.c_int, VP, VP, VP, VP, VP, VP, VP, VP, VP, VP, VP, VP, DP]),
+    "plgb_batch_adjoint": (C.c_int, [VP, C.c_int, VP, VP, VP, VP, VP, VP, VP, VP, VP, VP, VP, VP, DP, DP]),
     "plgb_batch_stats": (C.c_int, [VP, C.c_char_p, C.c_size_t]),
     "plgb_gate_name": (C.c_char_p, [C.c_int]),
     "plgb_set_c128_fp64_passes": (C.c_int, [C.c_int]),

@@ -40,6 +40,9 @@ def gate_codes() -> dict[str, int]:
 
 
 _CODES: dict[str, int] | None = None
+_NPAR = None
+_NO_PARAM = {"Identity", "PauliX", "PauliY", "PauliZ", "Hadamard", "S", "SX", "T", "CNOT", "CY", "CZ", "SWAP",
+             "Toffoli", "CSWAP"}
 
 
 def code_of(name: str) -> int:
@@ -185,6 +188,40 @@ class BatchEngine:
         call("plgb_batch_run", self._h, p.num_circuits, *[_ptr(a) for a in arrays],
              out.ctypes.data_as(C.POINTER(C.c_double)))
         return out[:p.num_observables]
+
+    def _arrays(self, p: PackedBatch):
+        return [np.ascontiguousarray(a) for a in (
+            p.num_qubits.astype(np.int32, copy=False), p.op_offsets.astype(np.int64, copy=False),
+            p.op_codes.astype(np.int32, copy=False), p.op_wires.astype(np.int32, copy=False),
+            p.op_params.astype(np.float64, copy=False), p.op_inverse.astype(np.uint8, copy=False),
+            p.obs_offsets.astype(np.int64, copy=False), p.term_offsets.astype(np.int64, copy=False),
+            p.term_coeffs.astype(np.float64, copy=False), p.term_x.astype(np.uint64, copy=False),
+            p.term_y.astype(np.uint64, copy=False), p.term_z.astype(np.uint64, copy=False))]
+
+    def parametric_gates(self, p: PackedBatch) -> np.ndarray:
+        """Number of parametric gates of each circuit (its Jacobian width)."""
+        global _NPAR
+        if _NPAR is None:
+            _NPAR = np.array([0 if name in _NO_PARAM else 1 for name in sorted(gate_codes(), key=gate_codes().get)])
+        per_op = _NPAR[p.op_codes] if p.op_codes.size else np.zeros(0, np.int64)
+        cs = np.concatenate([[0], np.cumsum(per_op)]).astype(np.int64)
+        return cs[p.op_offsets[1:]] - cs[p.op_offsets[:-1]]
+
+    def run_adjoint(self, packed: PackedBatch):
+        """<O> per observable and, per circuit, the Jacobian (observables x
+        parametric gates) by the in-place adjoint sweep."""
+        p = packed
+        arrays = self._arrays(p)
+        npar = self.parametric_gates(p)
+        nobs = np.diff(p.obs_offsets)
+        widths = npar * nobs
+        values = np.zeros(max(p.num_observables, 1), np.float64)
+        jac = np.zeros(max(int(widths.sum()), 1), np.float64)
+        call("plgb_batch_adjoint", self._h, p.num_circuits, *[_ptr(a) for a in arrays],
+             values.ctypes.data_as(C.POINTER(C.c_double)), jac.ctypes.data_as(C.POINTER(C.c_double)))
+        offs = np.concatenate([[0], np.cumsum(widths)])
+        jacs = [jac[offs[c]:offs[c + 1]].reshape(int(nobs[c]), int(npar[c])) for c in range(p.num_circuits)]
+        return values[:p.num_observables], jacs
 
     def stats(self) -> dict:
         n = 1 << 16

@@ -11,8 +11,10 @@ queues independently, so work of different lanes overlaps on the device:
   lane takes ALL queued requests the budget admits (requests that arrived
   while the previous batch was on the GPU join here) and runs them as one
   batch of the batch engine;
-* `adjoint_lanes` adjoint lanes: fused forward pass, <H>, then the in-place
-  adjoint sweep, one request at a time per lane.
+* `adjoint_lanes` adjoint lanes: every pass takes all queued adjoint
+  requests the budget admits; the engine runs them concurrently on host
+  threads with their own streams (fused forward pass, <H>, in-place adjoint
+  sweep).
 
 Results of a request do not depend on what else is in flight: a forward
 request's value is bit-identical to running it alone in a batch engine with
@@ -82,7 +84,7 @@ class ServeResult:
 
 class Server:
     def __init__(self, precision: int = 128, budget_bytes: float = 150e9, big_qubits: int = 20,
-                 adjoint_lanes: int = 4, max_batch: int = 4096, tile_bits: int = 11):
+                 adjoint_lanes: int = 1, max_batch: int = 4096, tile_bits: int = 11):
         self.precision = int(precision)
         self.S = 16 if self.precision == 128 else 8
         self.budget = MemoryBudget(int(budget_bytes))
@@ -93,6 +95,10 @@ class Server:
         # forward lanes keep their engines (device arenas, tuned tile sizes)
         self.engines = [BatchEngine(self.precision, wave_bytes=int(budget_bytes)),
                         BatchEngine(self.precision, wave_bytes=int(budget_bytes))]
+        # adjoint lanes: batches of requests, each circuit on its own host
+        # thread and stream inside the engine
+        self.adj_engines = [BatchEngine(self.precision, tile_bits=self.tile_bits, wave_bytes=int(budget_bytes))
+                            for _ in range(self.adjoint_lanes)]
         self._names = {v: k for k, v in gate_codes().items()}
 
     # ---------------------------------------------------------------- helpers
@@ -127,23 +133,11 @@ class Server:
             terms.append(TP(fac) if fac else NO("Identity", [0]))
         return HA([float(c) for c in p.term_coeffs[t0:t1]], terms)
 
-    def adjoint_one(self, r: int):
-        """<H> and its Jacobian for request r, exactly as run alone."""
-        n = int(self.packed.num_qubits[r])
-        SV = ops.StateVectorC128 if self.precision == 128 else ops.StateVectorC64
-        M = ops.MeasurementsC128 if self.precision == 128 else ops.MeasurementsC64
-        S = self._ops_struct(r)
-        H = self._hamiltonian(r)
-        sv = SV(n)
-        sv.applyOperations(S, min(self.tile_bits, n))
-        value = float(M(sv).expval(H))
-        npar = sum(1 for p in S.params if p)
-        jac = np.zeros(max(1, npar), np.float64)
-        tp = np.arange(npar, dtype=np.int64)
-        arr = (VP * 1)(H._h)
-        call("plgb_adjoint_jacobian_inplace", sv._h, arr, 1, S._h, tp.ctypes.data_as(C.POINTER(C.c_int64)), npar,
-             jac.ctypes.data_as(C.POINTER(C.c_double)))
-        return value, jac[:npar]
+    def adjoint_one(self, r: int, lane: int = 0):
+        """<H> and its Jacobian for request r run alone (a batch of one on
+        the lane's engine: the same computation as inside any batch)."""
+        vals, jacs = self.adj_engines[lane].run_adjoint(self.packed.select([r]))
+        return float(vals[0]), jacs[0][0]
 
     # ------------------------------------------------------------------- run
     def run(self, packed: PackedBatch, arrival: np.ndarray, adjoint: np.ndarray, speed: float = 1.0) -> ServeResult:
@@ -210,20 +204,22 @@ class Server:
                 closing.set()
 
         def adjoint_lane(li):
+            eng = self.adj_engines[li - 2]
             try:
                 while True:
-                    got = take(li, 1)
+                    got = take(li, self.max_batch)
                     if not got:
                         return
-                    r = got[0]
                     ts = now()
-                    v, j = self.adjoint_one(r)
+                    vals, js = eng.run_adjoint(packed.select(got))
                     te = now()
-                    self.budget.release(self._bytes(r))
+                    for r in got:
+                        self.budget.release(self._bytes(r))
                     with lock:
-                        values[r], jacs[r] = v, j
-                        start[r], done[r], lane_of[r] = ts, te, li
-                        batches.append((li, 1, te - ts))
+                        for k, r in enumerate(got):
+                            values[r], jacs[r] = vals[k], js[k][0]
+                            start[r], done[r], lane_of[r] = ts, te, li
+                        batches.append((li, len(got), te - ts))
             except Exception as e:
                 errors.append(e)
                 closing.set()

@@ -176,3 +176,33 @@ def test_batch_double_float_vs_fp64(ops_module):
     norms = np.array([max(1.0, np.abs(packed.term_coeffs[packed.term_offsets[k]:packed.term_offsets[k + 1]]).sum())
                       for k in range(packed.num_observables)])
     assert np.all(np.abs(va - vb) <= 50e-12 * norms)
+
+
+def test_batch_adjoint_matches_single_register_adjoint(ops_module):
+    # run_adjoint == <H> and AdjointJacobianC128 of each circuit alone
+    from lightning_gb300.workloads import config4_packed
+
+    packed, _, _ = config4_packed(rate=2000.0, duration=0.01, seed=9, n_max=11)
+    eng = BatchEngine(128)
+    vals, jacs = eng.run_adjoint(packed)
+    from lightning_gb300.serve import Server
+
+    srv = Server(128, adjoint_lanes=1)
+    srv.packed, srv.adjoint = packed, np.ones(packed.num_circuits, bool)
+    for c in range(0, packed.num_circuits, 3):
+        n = int(packed.num_qubits[c])
+        S = srv._ops_struct(c)
+        H = srv._hamiltonian(c)
+        sv = ops_module.StateVectorC128(n)
+        for name, w, prm in zip(S.names, S.wires, S.params):
+            sv.applyOperation(name, w, False, prm)
+        v = float(ops_module.MeasurementsC128(sv).expval(H))
+        npar = sum(1 for p in S.params if p)
+        j = ops_module.AdjointJacobianC128()(sv, [H], S, list(range(npar)))
+        scale = max(1.0, float(np.sum(np.abs(packed.term_coeffs[packed.term_offsets[c]:packed.term_offsets[c + 1]]))))
+        assert abs(vals[c] - v) <= 50e-12 * scale
+        assert jacs[c].shape == (1, npar)
+        assert np.max(np.abs(jacs[c][0] - j)) <= 50e-12 * scale
+        # alone (a batch of one) is bit-identical to the batch
+        va, ja = srv.adjoint_one(c)
+        assert va == vals[c] and np.array_equal(ja, jacs[c][0])

@@ -594,6 +594,10 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
         stats_.padded += cc.ne != cc.n ? 1 : 0;
     }
     stats_.device_ms = dev_ms_total;
+    stats_.done_ms.assign(static_cast<size_t>(nc), 0.0);
+    for (int c = 0; c < nc; c++) {
+        stats_.done_ms[static_cast<size_t>(c)] = stats_.wave_done_ms[static_cast<size_t>(stats_.wave_of[static_cast<size_t>(c)])];
+    }
     stats_.total_ms = ms_since(t_start);
 }
 
@@ -626,6 +630,7 @@ template <class T> void BatchEngine<T>::run_adjoint(const BatchInput &in, double
     int active = 0;
     std::atomic<int> next{0};
     std::vector<std::string> errors(static_cast<size_t>(nc));
+    stats_.done_ms.assign(static_cast<size_t>(nc), 0.0);
     int dev = 0;
     cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
     auto worker = [&]() {
@@ -705,6 +710,7 @@ template <class T> void BatchEngine<T>::run_adjoint(const BatchInput &in, double
                 }
                 const auto j = Adjoint<T>::jacobian(sv, obs, ops, tp, false, true);
                 std::copy(j.begin(), j.end(), jac + jac_off[static_cast<size_t>(c)]);
+                stats_.done_ms[static_cast<size_t>(c)] = ms_since(t_start);
             } catch (const std::exception &e) {
                 errors[static_cast<size_t>(c)] = e.what();
             }
@@ -764,6 +770,10 @@ template <class T> std::string BatchEngine<T>::stats_json() const {
     js += "], \"wave_of\": [";
     for (size_t i = 0; i < stats_.wave_of.size(); i++) {
         js += (i ? ", " : "") + std::to_string(stats_.wave_of[i]);
+    }
+    js += "], \"done_ms\": [";
+    for (size_t i = 0; i < stats_.done_ms.size(); i++) {
+        js += (i ? ", " : "") + std::to_string(stats_.done_ms[i]);
     }
     return js + "]}";
 }

@@ -87,6 +87,7 @@ struct BatchStats {
     std::map<int, int> tile_bits; // register size -> tile bits used
     std::vector<double> wave_done_ms; // completion time of each wave, from the start of run()
     std::vector<int> wave_of;         // wave index of each circuit
+    std::vector<double> done_ms;      // when each circuit's results were ready, from the start of the run
 };
 
 template <class T> class BatchEngine {

@@ -90,12 +90,18 @@ template <class T> struct DiagForm {
 template <class T>
 void launch_tile_pass(cudaStream_t s, cx<T> *sv, const TilePassDesc &d, const TileOp<T> *ops, const DiagForm<T> *forms,
                       const cx<T> *tables);
+struct df;
+
 // Adjoint sweep: the pass applied to two registers (lambda and H lambda),
 // with its TK_REDUCE ops accumulated into partials[slot * G + CTA].
 template <class T>
 void launch_tile_pass_adj(cudaStream_t s, cx<T> *lam, cx<T> *hlam, const TilePassDesc &d, const TileOp<T> *ops,
                           const DiagForm<T> *forms, const cx<T> *tables, double *partials, int G);
 int adj_grid_capacity(size_t tile_bytes_each);
+// the same in double-float arithmetic (io as for launch_tile_pass_reg_df)
+void launch_tile_pass_adj_df(cudaStream_t s, void *lam, void *hlam, int io, const TilePassDesc &d,
+                             const TileOp<df> *ops, const DiagForm<df> *forms, const cx<df> *tables, double *partials,
+                             int G);
 void launch_adj_sum(cudaStream_t s, const double *partials, int nslots, int G, double *out);
 
 // A merged-diagonal table of 2^t entries described by its factors instead
@@ -118,7 +124,6 @@ struct TableRecipe {
 bool tile_variant_occ(int precision);
 bool set_tile_variant_occ(int precision, bool occ);
 
-struct df;
 // Complex128 passes in double-float arithmetic (df.cuh).  io: 0 = doubles in
 // and out, 1 = doubles in / df out (first pass of a program), 2 = df in and
 // out, 3 = df in / doubles out (last pass).

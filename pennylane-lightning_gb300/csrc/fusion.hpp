@@ -25,7 +25,8 @@ template <class T> struct FusedProgram {
     StageDesc *d_stages{nullptr};
     // double-float copies of the op tables (complex128 programs whose every
     // pass runs on the register kernel; df_ok tells whether they exist)
-    bool df_ok{false};
+    bool df_ok{false};  // df tables exist (every segment is a tile pass)
+    bool df_reg{false}; // and every pass runs on the register kernel
     void *dev_df{nullptr};
     const void *d_ops_df{nullptr}, *d_forms_df{nullptr}, *d_tables_df{nullptr};
     // host copies (compile_fused without upload); indices in the segments'

@@ -1152,11 +1152,13 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
                    "H2D");
     }
     if constexpr (std::is_same_v<T, double>) {
-        bool all_reg = !prog->segs.empty();
+        bool all_reg = !prog->segs.empty(), all_tile = !prog->segs.empty();
         for (const auto &seg : prog->segs) {
             all_reg = all_reg && seg.tile && seg.reg;
+            all_tile = all_tile && seg.tile;
         }
-        if (all_reg) {
+        prog->df_reg = all_reg;
+        if (all_tile) {
             // the same tables re-encoded as double-float (same 16-byte layout)
             static_assert(sizeof(TileOp<double>) == sizeof(TileOp<df>) && sizeof(DiagForm<double>) == sizeof(DiagForm<df>),
                           "double-float op tables must share the double layout");
@@ -1211,7 +1213,7 @@ bool c128_fp64_passes() { return g_c128_fp64; }
 template <class T> void run_fused(StateVector<T> &sv, const FusedProgram<T> &prog) {
     PLGB_REQUIRE(prog.n == sv.num_qubits(), "fused program compiled for a different register size");
     if constexpr (std::is_same_v<T, double>) {
-        if (prog.df_ok && !c128_fp64_passes()) {
+        if (prog.df_reg && prog.df_ok && !c128_fp64_passes()) {
             // the register holds df values between the first and the last pass
             const size_t np = prog.segs.size();
             for (size_t k = 0; k < np; k++) {
@@ -1242,6 +1244,20 @@ void run_fused_adjoint(StateVector<T> &lam, StateVector<T> &hlam, const FusedPro
     PLGB_REQUIRE(prog.n == lam.num_qubits() && prog.n == hlam.num_qubits(),
                  "adjoint program compiled for a different register size");
     PLGB_REQUIRE(lam.stream() == hlam.stream(), "adjoint registers must share a stream");
+    if constexpr (std::is_same_v<T, double>) {
+        if (prog.df_ok && !c128_fp64_passes()) {
+            // both registers hold df values between the first and the last pass
+            const size_t np = prog.segs.size();
+            for (size_t k = 0; k < np; k++) {
+                const int io = np == 1 ? 0 : k == 0 ? 1 : k + 1 == np ? 3 : 2;
+                launch_tile_pass_adj_df(lam.stream(), lam.data(), hlam.data(), io, prog.segs[k].desc,
+                                        static_cast<const TileOp<df> *>(prog.d_ops_df),
+                                        static_cast<const DiagForm<df> *>(prog.d_forms_df),
+                                        static_cast<const cx<df> *>(prog.d_tables_df), partials, G);
+            }
+            return;
+        }
+    }
     for (const auto &seg : prog.segs) {
         if (seg.tile) {
             launch_tile_pass_adj<T>(lam.stream(), lam.data(), hlam.data(), seg.desc, prog.d_ops, prog.d_forms,

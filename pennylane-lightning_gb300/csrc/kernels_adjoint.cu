@@ -20,6 +20,8 @@
 // |tile factor|^2.
 #include "tile_smem.cuh"
 
+#include <type_traits>
+
 namespace plgb {
 
 namespace {
@@ -28,9 +30,9 @@ constexpr int kAdjThreads = kTileThreads;
 
 } // namespace
 
-template <class T>
+template <class T, class SI = T, class SO = T>
 __global__ void __launch_bounds__(kAdjThreads)
-    k_tile_adj(cx<T> *__restrict__ a, cx<T> *__restrict__ b, const TilePassDesc dp, const TileOp<T> *__restrict__ ops,
+    k_tile_adj(cx<SI> *a, cx<SI> *b, const TilePassDesc dp, const TileOp<T> *__restrict__ ops,
                const DiagForm<T> *__restrict__ forms, const cx<T> *__restrict__ tables, double *__restrict__ partials,
                int G) {
     extern __shared__ unsigned char smraw[];
@@ -56,8 +58,8 @@ __global__ void __launch_bounds__(kAdjThreads)
         }
         for (u32 j = threadIdx.x; j < T_; j += blockDim.x) {
             const u64 gj = gbase | local_offset(j, d);
-            ta[j] = a[gj];
-            tb[j] = b[gj];
+            ta[j] = ld_conv<T, SI>(a[gj]);
+            tb[j] = ld_conv<T, SI>(b[gj]);
         }
         if (threadIdx.x == 0) {
             sd.tile_factor = cx<T>{1, 0};
@@ -77,19 +79,39 @@ __global__ void __launch_bounds__(kAdjThreads)
                 const bool want_re = (op.mode & 1) != 0;
                 const double sgn = (op.mode & 2) ? -1.0 : 1.0;
                 double v = 0.0;
-                for (u32 j = threadIdx.x; j < T_; j += blockDim.x) {
-                    if ((j & op.rcmask) != op.lcval) {
-                        continue;
+                if constexpr (std::is_same_v<T, df>) {
+                    // double-float products and a double-float running sum,
+                    // one conversion per thread
+                    df acc{0.f, 0.f};
+                    for (u32 j = threadIdx.x; j < T_; j += blockDim.x) {
+                        if ((j & op.rcmask) != op.lcval) {
+                            continue;
+                        }
+                        const u32 k = j ^ op.lo1;
+                        const cx<df> p = tb[j];
+                        const cx<df> q = ta[k];
+                        df z = want_re ? p.x * q.x + p.y * q.y : p.x * q.y - p.y * q.x;
+                        if ((static_cast<unsigned>(__popc(k & op.lo0)) ^ gpar) & 1u) {
+                            z = -z;
+                        }
+                        acc = acc + z;
                     }
-                    const u32 k = j ^ op.lo1;
-                    const cx<T> p = tb[j];
-                    const cx<T> q = ta[k];
-                    double z = want_re ? static_cast<double>(p.x) * q.x + static_cast<double>(p.y) * q.y
-                                       : static_cast<double>(p.x) * q.y - static_cast<double>(p.y) * q.x;
-                    if ((static_cast<unsigned>(__popc(k & op.lo0)) ^ gpar) & 1u) {
-                        z = -z;
+                    v = df_to_double(acc);
+                } else {
+                    for (u32 j = threadIdx.x; j < T_; j += blockDim.x) {
+                        if ((j & op.rcmask) != op.lcval) {
+                            continue;
+                        }
+                        const u32 k = j ^ op.lo1;
+                        const cx<T> p = tb[j];
+                        const cx<T> q = ta[k];
+                        double z = want_re ? static_cast<double>(p.x) * q.x + static_cast<double>(p.y) * q.y
+                                           : static_cast<double>(p.x) * q.y - static_cast<double>(p.y) * q.x;
+                        if ((static_cast<unsigned>(__popc(k & op.lo0)) ^ gpar) & 1u) {
+                            z = -z;
+                        }
+                        v += z;
                     }
-                    v += z;
                 }
                 v *= sgn;
 #pragma unroll
@@ -106,7 +128,15 @@ __global__ void __launch_bounds__(kAdjThreads)
                         tot += s_red[w];
                     }
                     const cx<T> f = sd.tile_factor;
-                    const double f2 = static_cast<double>(f.x) * f.x + static_cast<double>(f.y) * f.y;
+                    double fx, fy;
+                    if constexpr (std::is_same_v<T, df>) {
+                        fx = static_cast<double>(f.x);
+                        fy = static_cast<double>(f.y);
+                    } else {
+                        fx = static_cast<double>(f.x);
+                        fy = static_cast<double>(f.y);
+                    }
+                    const double f2 = fx * fx + fy * fy;
                     s_acc[op.diag_slot] += tot * op.rmul * f2;
                 }
                 __syncthreads();
@@ -121,11 +151,14 @@ __global__ void __launch_bounds__(kAdjThreads)
             __syncthreads();
         }
         const cx<T> f = sd.tile_factor;
-        const cx<T> sf{f.x * d.pass_scale, f.y * d.pass_scale};
+        const T ps = from_double<T>(d.pass_scale);
+        const cx<T> sf{f.x * ps, f.y * ps};
+        cx<SO> *ao = reinterpret_cast<cx<SO> *>(a);
+        cx<SO> *bo = reinterpret_cast<cx<SO> *>(b);
         for (u32 j = threadIdx.x; j < T_; j += blockDim.x) {
             const u64 gj = gbase | local_offset(j, d);
-            a[gj] = sf * ta[j];
-            b[gj] = sf * tb[j];
+            ao[gj] = st_conv<SO, T>(sf * ta[j]);
+            bo[gj] = st_conv<SO, T>(sf * tb[j]);
         }
         __syncthreads();
     }
@@ -140,11 +173,11 @@ __global__ void __launch_bounds__(kAdjThreads)
 }
 
 namespace {
-template <class T> void adj_smem_attr() {
+template <class T, class SI = T, class SO = T> void adj_smem_attr() {
     static bool attr = false;
     if (!attr) {
-        cuda_check(cudaFuncSetAttribute(k_tile_adj<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
-                   "adjoint tile smem attribute");
+        cuda_check(cudaFuncSetAttribute(k_tile_adj<T, SI, SO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        200 * 1024), "adjoint tile smem attribute");
         attr = true;
     }
 }
@@ -154,6 +187,10 @@ int adj_grid_capacity(size_t tile_bytes_each) {
     // the launcher's grid never exceeds this many CTAs for 2 tiles of this size
     adj_smem_attr<double>();
     adj_smem_attr<float>();
+    adj_smem_attr<df, double, df>();
+    adj_smem_attr<df, df, df>();
+    adj_smem_attr<df, df, double>();
+    adj_smem_attr<df, double, double>();
     int per_sm = 1;
     const size_t smem = 2 * tile_bytes_each;
     cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_adj<double>, kAdjThreads, smem),
@@ -186,6 +223,42 @@ void launch_tile_pass_adj(cudaStream_t s, cx<T> *lam, cx<T> *hlam, const TilePas
     k_tile_adj<T><<<static_cast<unsigned>(grid), kAdjThreads, smem, s>>>(lam, hlam, d, ops, forms, tables, partials, G);
     cuda_check(cudaGetLastError(), "k_tile_adj launch");
     note_launch();
+}
+
+template <class SI, class SO>
+static void launch_adj_df_io(cudaStream_t s, void *lam, void *hlam, const TilePassDesc &d, const TileOp<df> *ops,
+                             const DiagForm<df> *forms, const cx<df> *tables, double *partials, int G) {
+    const size_t smem = 2 * (sizeof(cx<df>) << d.t);
+    adj_smem_attr<df, SI, SO>();
+    if (smem > 200 * 1024) {
+        throw std::runtime_error("adjoint tile pass: two tiles do not fit shared memory");
+    }
+    int per_sm = 1;
+    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_adj<df, SI, SO>, kAdjThreads, smem),
+               "adjoint occupancy");
+    if (per_sm < 1) {
+        throw std::runtime_error("adjoint tile pass: tile does not fit one SM");
+    }
+    const u64 cap = static_cast<u64>(LaunchGeom::sm_count()) * static_cast<u64>(per_sm);
+    u64 grid = d.ntiles < cap ? d.ntiles : cap;
+    if (grid > static_cast<u64>(G)) {
+        grid = static_cast<u64>(G);
+    }
+    k_tile_adj<df, SI, SO><<<static_cast<unsigned>(grid), kAdjThreads, smem, s>>>(
+        static_cast<cx<SI> *>(lam), static_cast<cx<SI> *>(hlam), d, ops, forms, tables, partials, G);
+    cuda_check(cudaGetLastError(), "k_tile_adj (df) launch");
+    note_launch();
+}
+
+void launch_tile_pass_adj_df(cudaStream_t s, void *lam, void *hlam, int io, const TilePassDesc &d,
+                             const TileOp<df> *ops, const DiagForm<df> *forms, const cx<df> *tables, double *partials,
+                             int G) {
+    switch (io) {
+    case 0: launch_adj_df_io<double, double>(s, lam, hlam, d, ops, forms, tables, partials, G); break;
+    case 1: launch_adj_df_io<double, df>(s, lam, hlam, d, ops, forms, tables, partials, G); break;
+    case 2: launch_adj_df_io<df, df>(s, lam, hlam, d, ops, forms, tables, partials, G); break;
+    default: launch_adj_df_io<df, double>(s, lam, hlam, d, ops, forms, tables, partials, G); break;
+    }
 }
 
 // out[slot] = sum over CTAs of partials[slot * G + c], one warp per slot in a

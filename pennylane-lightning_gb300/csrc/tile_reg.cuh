@@ -68,31 +68,6 @@ template <class T> __device__ __forceinline__ cx<T> shx(cx<T> v, int m) {
     return cx<T>{shfl_val(v.x, m), shfl_val(v.y, m)};
 }
 
-// Register <-> memory formats: complex64 / complex128 registers compute in
-// their own type; a df register reads doubles (first pass of a program) or
-// df, and writes df or doubles (last pass).
-template <class T, class S> __device__ __forceinline__ cx<T> ld_conv(const cx<S> &v) {
-    if constexpr (std::is_same_v<T, df> && std::is_same_v<S, double>) {
-        return cx<df>{df_from_bits(v.x), df_from_bits(v.y)};
-    } else {
-        return v;
-    }
-}
-template <class S, class T> __device__ __forceinline__ cx<S> st_conv(const cx<T> &v) {
-    if constexpr (std::is_same_v<T, df> && std::is_same_v<S, double>) {
-        return cx<double>{df_to_double(v.x), df_to_double(v.y)};
-    } else {
-        return v;
-    }
-}
-// a per-pass double constant in the register's type
-template <class T> __device__ __forceinline__ T from_double(double x) {
-    if constexpr (std::is_same_v<T, df>) {
-        return df(x);
-    } else {
-        return static_cast<T>(x);
-    }
-}
 
 // Layout of a register stage, held in registers: local index of register
 // slot i of this thread = jt | (bit k of i placed at local bit rb[k]).

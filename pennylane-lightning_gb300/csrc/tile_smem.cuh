@@ -4,6 +4,7 @@
 // every op of the pass runs on it with all threads of the CTA.
 #pragma once
 
+#include "df.cuh"
 #include "fused.hpp"
 
 namespace plgb {
@@ -36,11 +37,15 @@ __device__ __forceinline__ double flip_sign(double x, unsigned neg) {
 __device__ __forceinline__ float flip_sign(float x, unsigned neg) {
     return __int_as_float(__float_as_int(x) ^ static_cast<int>(neg << 31));
 }
+__device__ __forceinline__ df flip_sign(df x, unsigned neg) { return df{flip_sign(x.hi, neg), flip_sign(x.lo, neg)}; }
 template <class T> __device__ __forceinline__ cx<T> flip(cx<T> v, unsigned neg) {
     return cx<T>{flip_sign(v.x, neg), flip_sign(v.y, neg)};
 }
+__device__ __forceinline__ float shfl_one(float x, int m) { return __shfl_xor_sync(0xffffffffu, x, m); }
+__device__ __forceinline__ double shfl_one(double x, int m) { return __shfl_xor_sync(0xffffffffu, x, m); }
+__device__ __forceinline__ df shfl_one(df x, int m) { return df{shfl_one(x.hi, m), shfl_one(x.lo, m)}; }
 template <class T> __device__ __forceinline__ cx<T> shfl_xor(cx<T> v, int m) {
-    return cx<T>{__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m)};
+    return cx<T>{shfl_one(v.x, m), shfl_one(v.y, m)};
 }
 
 // Evaluate a small diagonal form on the global bits of a tile base.

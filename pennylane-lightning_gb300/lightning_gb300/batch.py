@@ -223,6 +223,11 @@ class BatchEngine:
         jacs = [jac[offs[c]:offs[c + 1]].reshape(int(nobs[c]), int(npar[c])) for c in range(p.num_circuits)]
         return values[:p.num_observables], jacs
 
+    def done_ms(self) -> list:
+        """When each circuit of the last run had its results, in ms from the
+        start of the run."""
+        return self.stats().get("done_ms", [])
+
     def stats(self) -> dict:
         n = 1 << 16
         while True:

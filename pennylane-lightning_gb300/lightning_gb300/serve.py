@@ -84,10 +84,13 @@ class ServeResult:
 
 class Server:
     def __init__(self, precision: int = 128, budget_bytes: float = 150e9, big_qubits: int = 20,
-                 adjoint_lanes: int = 1, max_batch: int = 4096, tile_bits: int = 11):
+                 adjoint_lanes: int = 1, max_batch: int = 4096, tile_bits: int = 11, adjoint_share: float = 0.4):
         self.precision = int(precision)
         self.S = 16 if self.precision == 128 else 8
-        self.budget = MemoryBudget(int(budget_bytes))
+        # forward and adjoint lanes draw on separate shares of the budget, so
+        # a backlog of one kind cannot starve the other
+        self.budget = MemoryBudget(int(budget_bytes * (1.0 - adjoint_share)))
+        self.adj_budget = MemoryBudget(int(budget_bytes * adjoint_share))
         self.big = int(big_qubits)
         self.max_batch = int(max_batch)
         self.tile_bits = int(tile_bits)
@@ -97,7 +100,8 @@ class Server:
                         BatchEngine(self.precision, wave_bytes=int(budget_bytes))]
         # adjoint lanes: batches of requests, each circuit on its own host
         # thread and stream inside the engine
-        self.adj_engines = [BatchEngine(self.precision, tile_bits=self.tile_bits, wave_bytes=int(budget_bytes))
+        self.adj_engines = [BatchEngine(self.precision, tile_bits=self.tile_bits,
+                                        wave_bytes=int(budget_bytes * adjoint_share))
                             for _ in range(self.adjoint_lanes)]
         self._names = {v: k for k, v in gate_codes().items()}
 
@@ -162,22 +166,26 @@ class Server:
         def now():
             return time.perf_counter() - t0
 
+        def budget_of(li):
+            return self.budget if li < 2 else self.adj_budget
+
         def take(li, limit):
             """Block for the first queued request of lane li, then take every
-            queued request the budget admits, up to `limit`."""
+            queued request the lane's budget admits, up to `limit`."""
+            bud = budget_of(li)
             with cvs[li]:
                 while not queues[li]:
                     if closing.is_set():
                         return []
                     cvs[li].wait(0.05)
                 first = queues[li][0]
-            self.budget.acquire(self._bytes(first))
+            bud.acquire(self._bytes(first))
             got = [first]
             with cvs[li]:
                 queues[li].popleft()
                 while queues[li] and len(got) < limit:
                     r = queues[li][0]
-                    if not self.budget.acquire(self._bytes(r), block=False):
+                    if not bud.acquire(self._bytes(r), block=False):
                         break
                     got.append(queues[li].popleft())
             return got
@@ -192,12 +200,14 @@ class Server:
                     ts = now()
                     vals = eng.run(packed.select(got))
                     te = now()
+                    fin = eng.done_ms()
                     for r in got:
                         self.budget.release(self._bytes(r))
                     with lock:
                         for k, r in enumerate(got):
                             values[r] = vals[k]
-                            start[r], done[r], lane_of[r] = ts, te, li
+                            start[r], lane_of[r] = ts, li
+                            done[r] = min(te, ts + fin[k] / 1e3) if k < len(fin) else te
                         batches.append((li, len(got), te - ts))
             except Exception as e:  # surfaced after the run
                 errors.append(e)
@@ -213,12 +223,14 @@ class Server:
                     ts = now()
                     vals, js = eng.run_adjoint(packed.select(got))
                     te = now()
+                    fin = eng.done_ms()
                     for r in got:
-                        self.budget.release(self._bytes(r))
+                        self.adj_budget.release(self._bytes(r))
                     with lock:
                         for k, r in enumerate(got):
                             values[r], jacs[r] = vals[k], js[k][0]
-                            start[r], done[r], lane_of[r] = ts, te, li
+                            start[r], lane_of[r] = ts, li
+                            done[r] = min(te, ts + fin[k] / 1e3) if k < len(fin) else te
                         batches.append((li, len(got), te - ts))
             except Exception as e:
                 errors.append(e)

@@ -91,3 +91,16 @@ def test_inplace_jacobian_matches_copying_entry():
     sv, S = circ.run(theta)
     b = jacobian(circ, theta, sv=sv, S=S, in_place=False)
     assert np.array_equal(a, b)
+
+
+def test_double_float_sweep_matches_fp64(ops_module):
+    # the fused adjoint sweep runs in double-float arithmetic by default
+    circ, theta = config3_circuit(n=12, layers=3, nterms=25)
+    a = jacobian(circ, theta, in_place=True)
+    prev = ops_module.set_c128_fp64_passes(True)
+    try:
+        b = jacobian(circ, theta, in_place=True)
+    finally:
+        ops_module.set_c128_fp64_passes(prev)
+    assert np.max(np.abs(a - b)) <= 50e-12 * max(1.0, np.max(np.abs(b)))
+    assert not np.array_equal(a, b)

@@ -90,16 +90,31 @@ __device__ __forceinline__ Layout stage_layout(const StageDesc *st, u32 tid, int
     return Layout{jt, st->rb[0], st->rb[1], st->rb[2], st->rb[3]};
 }
 
+// Shared-memory addresses of a thread's 16 slots.  The swizzle is linear
+// over XOR and the thread and register parts of a local index have disjoint
+// bits, so swz(jt | reg(i)) = swz(jt) ^ (XOR of swz(1 << rb_k) over the set
+// bits k of i): four swizzles per layout, then one XOR per slot.
+template <class T> struct SlotAddr {
+    u32 base, s0, s1, s2, s3;
+    __device__ __forceinline__ explicit SlotAddr(const Layout &l)
+        : base(swz<T>(l.jt)), s0(swz<T>(1u << l.rb0)), s1(swz<T>(1u << l.rb1)), s2(swz<T>(1u << l.rb2)),
+          s3(swz<T>(1u << l.rb3)) {}
+    __device__ __forceinline__ u32 operator()(int i) const {
+        return base ^ ((i & 1) ? s0 : 0u) ^ ((i & 2) ? s1 : 0u) ^ ((i & 4) ? s2 : 0u) ^ ((i & 8) ? s3 : 0u);
+    }
+};
 template <class T> __device__ __forceinline__ void to_smem(cx<T> *tile, const cx<T> (&v)[NR], const Layout &l) {
+    const SlotAddr<T> ad(l);
 #pragma unroll
     for (int i = 0; i < NR; i++) {
-        tile[swz<T>(l.at(i))] = v[i];
+        tile[ad(i)] = v[i];
     }
 }
 template <class T> __device__ __forceinline__ void from_smem(const cx<T> *tile, cx<T> (&v)[NR], const Layout &l) {
+    const SlotAddr<T> ad(l);
 #pragma unroll
     for (int i = 0; i < NR; i++) {
-        v[i] = tile[swz<T>(l.at(i))];
+        v[i] = tile[ad(i)];
     }
 }
 
@@ -307,7 +322,12 @@ __device__ __forceinline__ void tile_reg_run(const cx<SI> *ain, cx<SO> *aout, co
                     const u32 zl = sh.zl[s];
                     const int ngen = sh.ngen[s];
                     const cx<T> *tab = tables + op.table_off;
-                    if (op.has_table) {
+                    if (op.has_table && zl == 0) {
+#pragma unroll
+                        for (int i = 0; i < NR; i++) {
+                            v[i] = tab[cur.at(i)] * v[i];
+                        }
+                    } else if (op.has_table) {
 #pragma unroll
                         for (int i = 0; i < NR; i++) {
                             const u32 j = cur.at(i);

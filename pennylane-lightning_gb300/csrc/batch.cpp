@@ -412,6 +412,7 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
             size_t item0;
             int nitems;
             u64 tiles;
+            int max_ops;
         };
         std::vector<BatchTileItem<T>> titems;
         std::vector<Launch> launches;
@@ -432,7 +433,7 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
                 }
             }
             for (auto &kv : by_t) {
-                Launch L{kv.first, titems.size(), 0, 0};
+                Launch L{kv.first, titems.size(), 0, 0, 0};
                 for (int i : kv.second) {
                     const auto &cc = comp[static_cast<size_t>(c0 + i)];
                     const auto &o = po[static_cast<size_t>(i)];
@@ -445,6 +446,7 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
                     it.desc = cc.prog->segs[static_cast<size_t>(k)].desc;
                     it.tile_begin = L.tiles;
                     L.tiles += it.desc.ntiles;
+                    L.max_ops = std::max(L.max_ops, it.desc.nops);
                     titems.push_back(it);
                     L.nitems++;
                 }
@@ -535,9 +537,9 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
         for (const auto &L : launches) {
             if (use_df) {
                 launch_tile_reg_batch<df>(s_, L.t, reinterpret_cast<const BatchTileItem<df> *>(d_titems + L.item0),
-                                          L.nitems, L.tiles);
+                                          L.nitems, L.tiles, L.max_ops);
             } else {
-                launch_tile_reg_batch<T>(s_, L.t, d_titems + L.item0, L.nitems, L.tiles);
+                launch_tile_reg_batch<T>(s_, L.t, d_titems + L.item0, L.nitems, L.tiles, L.max_ops);
             }
             stats_.launches++;
         }

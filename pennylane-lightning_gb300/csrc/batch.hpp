@@ -53,7 +53,8 @@ struct DevRecipe {
 void launch_expand_tables(cudaStream_t s, const DevRecipe *recipes, int nrec, u64 total_entries, int enc);
 
 template <class T>
-void launch_tile_reg_batch(cudaStream_t s, int t, const BatchTileItem<T> *items, int nitems, u64 total_tiles);
+void launch_tile_reg_batch(cudaStream_t s, int t, const BatchTileItem<T> *items, int nitems, u64 total_tiles,
+                           int max_ops);
 template <class T> void launch_batch_set_one(cudaStream_t s, cx<T> *const *svs, int n);
 template <class T>
 void launch_pauli_batch(cudaStream_t s, const BatchRedItem<T> *items, int nitems, u64 total_blocks, double *partials,

@@ -64,6 +64,23 @@ __device__ __forceinline__ df operator*(df a, df b) {
     return df_quick_two_sum(p, e);
 }
 __device__ __forceinline__ bool operator==(df a, df b) { return a.hi == b.hi && a.lo == b.lo; }
+// a + b * c with one renormalisation: the product's error terms go straight
+// into the low sum (15 FP32 instructions instead of 18 for * then +).
+__device__ __forceinline__ df df_fma(df a, df b, df c) {
+    const float p = __fmul_rn(b.hi, c.hi);
+    float e = __fmaf_rn(b.hi, c.hi, -p);
+    e = __fmaf_rn(b.hi, c.lo, e);
+    e = __fmaf_rn(b.lo, c.hi, e);
+    const df s = df_two_sum(a.hi, p);
+    return df_quick_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, e)));
+}
+// complex products and acc + a * b as chains of df_fma
+__device__ __forceinline__ cx<df> operator*(cx<df> a, cx<df> b) {
+    return cx<df>{df_fma(a.x * b.x, -a.y, b.y), df_fma(a.x * b.y, a.y, b.x)};
+}
+__device__ __forceinline__ cx<df> cfma(cx<df> a, cx<df> b, cx<df> acc) {
+    return cx<df>{df_fma(df_fma(acc.x, a.x, b.x), -a.y, b.y), df_fma(df_fma(acc.y, a.x, b.y), a.y, b.x)};
+}
 
 // double -> df with integer operations only (no f64 instruction)
 __device__ __forceinline__ df df_from_bits(double x) {

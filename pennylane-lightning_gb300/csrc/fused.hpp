@@ -20,6 +20,7 @@ enum TileKind : int {
 constexpr int kMaxReducePerPass = 64; // reduction slots accumulated per CTA and pass
 
 constexpr int kRegBits = 4;              // amplitudes per thread in register stages: 2^4
+constexpr int kMaxOpsPerPass = 192;      // ops of a pass staged in shared memory per CTA
 constexpr int kMinRegTileBits = 9;       // register kernel needs >= 32 threads
 constexpr int kMaxDiagOpsPerPass = 48;   // merged diagonals evaluated per tile
 
@@ -75,6 +76,17 @@ template <class T> struct TileOp {
     int rslot{0};
     double rmul{1.0};
     cx<T> m[16]{};
+};
+
+// The fields of a TileOp that register stages and the tile prologue read,
+// staged once per CTA and pass in shared memory (k_tile_reg*).
+template <class T> struct RegOpS {
+    int kind, mode, rk, diag_slot;
+    u32 rcmask, rcval;
+    int has_table, table_off;
+    u64 gcmask, gcval;
+    int ngforms, gform_begin, nmforms, mform_begin;
+    cx<T> m[4];
 };
 
 // A diagonal factor on at most 4 bits: tab[k] with k = bits (first = MSB).

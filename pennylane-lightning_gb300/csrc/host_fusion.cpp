@@ -369,6 +369,9 @@ bool plan_stages(std::vector<TileOp<T>> &ops, const std::vector<DiagForm<T>> &fo
     if (d.t < kMinRegTileBits || d.t > 12) { // 2^(t-4) <= 256 threads
         return false;
     }
+    if (d.nops > kMaxOpsPerPass) {
+        return false; // the register kernel stages at most kMaxOpsPerPass op records
+    }
     for (int i = d.op_begin; i < d.op_begin + d.nops; i++) {
         if (ops[static_cast<size_t>(i)].kind == TK_REDUCE) {
             return false; // adjoint passes run on the two-register kernel
@@ -691,17 +694,20 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
             PassPlan cur;
             cur.fused = true;
             cur.local = pp.local;
-            int ndl = 0, last_dl = -1, nred = 0;
+            int ndl = 0, last_dl = -1, nred = 0, nprim = 0;
             for (size_t k = 0; k < ord.size(); k++) {
                 const bool dg = diag[ord[k]] != 0;
                 const bool rd = P[ord[k]].kind == Prim<T>::Reduce;
-                if ((dg && lv[k] != last_dl && ndl == kDiagLevelsPerPass) || (rd && nred == kMaxReducePerPass)) {
+                // (a primitive becomes at most one op, merged diagonals fewer)
+                if ((dg && lv[k] != last_dl && ndl == kDiagLevelsPerPass) || (rd && nred == kMaxReducePerPass) ||
+                    nprim == kMaxOpsPerPass - kMaxDiagOpsPerPass) {
                     split.push_back(std::move(cur));
                     cur = PassPlan{};
                     cur.fused = true;
                     cur.local = pp.local;
                     ndl = 0;
                     nred = 0;
+                    nprim = 0;
                     last_dl = -1;
                 }
                 if (dg && lv[k] != last_dl) {
@@ -709,6 +715,7 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
                     last_dl = lv[k];
                 }
                 nred += rd ? 1 : 0;
+                nprim += (dg && P[ord[k]].kind != Prim<T>::Parity) ? 0 : 1;
                 cur.prims.push_back(ord[k]);
             }
             if (!cur.prims.empty()) {

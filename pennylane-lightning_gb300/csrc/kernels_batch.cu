@@ -15,6 +15,7 @@ __global__ void __launch_bounds__(256, OCC ? 2 : 1)
     cx<T> *tile = reinterpret_cast<cx<T> *>(smraw);
     __shared__ TileShared<T> sh;
     __shared__ TilePassDesc sd;
+    const RegOpS<T> *recs = nullptr; // staged op records of the current item
     int cur = -1;
     for (u64 gt = blockIdx.x; gt < total_tiles; gt += gridDim.x) {
         // item owning global tile gt: the last one whose tile_begin <= gt
@@ -32,18 +33,20 @@ __global__ void __launch_bounds__(256, OCC ? 2 : 1)
             if (threadIdx.x == 0) {
                 sd = items[lo].desc;
             }
+            recs = op_records<T, true>(smraw + (sizeof(cx<T>) << items[lo].desc.t), items[lo].ops, items[lo].desc);
             __syncthreads();
             cur = lo;
         }
         const BatchTileItem<T> &it = items[lo];
-        tile_reg_run<T>(it.sv, it.sv, sd, it.ops, it.forms, it.tables, it.stages, gt - it.tile_begin, tile, sh);
+        tile_reg_run<T>(it.sv, it.sv, sd, it.ops, it.forms, it.tables, it.stages, gt - it.tile_begin, tile, sh, recs);
     }
 }
 
 template <class T, bool OCC>
-static void launch_batch_impl(cudaStream_t s, int t, const BatchTileItem<T> *items, int nitems, u64 total_tiles) {
+static void launch_batch_impl(cudaStream_t s, int t, const BatchTileItem<T> *items, int nitems, u64 total_tiles,
+                              int max_ops) {
     const int threads = 1 << (t - kRegBits);
-    const size_t smem = sizeof(cx<T>) << t;
+    const size_t smem = (sizeof(cx<T>) << t) + op_record_bytes<T, true>(max_ops);
     static bool attr = false;
     if (!attr) {
         cuda_check(cudaFuncSetAttribute(k_tile_reg_batch<T, OCC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -64,14 +67,15 @@ static void launch_batch_impl(cudaStream_t s, int t, const BatchTileItem<T> *ite
 }
 
 template <class T>
-void launch_tile_reg_batch(cudaStream_t s, int t, const BatchTileItem<T> *items, int nitems, u64 total_tiles) {
-    if (t < kMinRegTileBits || t > 12 || nitems < 1 || total_tiles < 1) {
+void launch_tile_reg_batch(cudaStream_t s, int t, const BatchTileItem<T> *items, int nitems, u64 total_tiles,
+                           int max_ops) {
+    if (t < kMinRegTileBits || t > 12 || nitems < 1 || total_tiles < 1 || max_ops > kMaxOpsPerPass) {
         throw std::runtime_error("batched tile pass: unsupported geometry");
     }
     if (tile_variant_occ(std::is_same_v<T, float> ? 64 : 128)) {
-        launch_batch_impl<T, true>(s, t, items, nitems, total_tiles);
+        launch_batch_impl<T, true>(s, t, items, nitems, total_tiles, max_ops);
     } else {
-        launch_batch_impl<T, false>(s, t, items, nitems, total_tiles);
+        launch_batch_impl<T, false>(s, t, items, nitems, total_tiles, max_ops);
     }
 }
 
@@ -274,12 +278,12 @@ void launch_pauli_batch(cudaStream_t s, const BatchRedItem<T> *items, int nitems
 }
 
 #define PLGB_BATCH_INST(T)                                                                                        \
-    template void launch_tile_reg_batch<T>(cudaStream_t, int, const BatchTileItem<T> *, int, u64);               \
+    template void launch_tile_reg_batch<T>(cudaStream_t, int, const BatchTileItem<T> *, int, u64, int);          \
     template void launch_batch_set_one<T>(cudaStream_t, cx<T> *const *, int);                                    \
     template void launch_pauli_batch<T>(cudaStream_t, const BatchRedItem<T> *, int, u64, double *, double *);
 PLGB_BATCH_INST(float)
 PLGB_BATCH_INST(double)
-template void launch_tile_reg_batch<df>(cudaStream_t, int, const BatchTileItem<df> *, int, u64);
+template void launch_tile_reg_batch<df>(cudaStream_t, int, const BatchTileItem<df> *, int, u64, int);
 template void launch_batch_set_one<df>(cudaStream_t, cx<df> *const *, int);
 
 } // namespace plgb

@@ -21,6 +21,10 @@ namespace plgb {
 // hiding; chosen per precision (tile_variant_occ).
 #define PLGB_TILE_BOUNDS(OCC) __launch_bounds__(256, (OCC) ? 2 : 1)
 
+// op records staged in shared memory for complex64 only (fewer spills at 128
+// registers for complex128 and double-float when read from global memory)
+template <class T> constexpr bool kStageRecs = std::is_same_v<T, float>;
+
 template <class T, bool OCC>
 __global__ void PLGB_TILE_BOUNDS(OCC) k_tile_reg(cx<T> *__restrict__ a, const TilePassDesc d,
                                                  const TileOp<T> *__restrict__ ops,
@@ -35,9 +39,10 @@ __global__ void PLGB_TILE_BOUNDS(OCC) k_tile_reg(cx<T> *__restrict__ a, const Ti
     if (threadIdx.x == 0) {
         sd = d;
     }
+    const auto *recs = op_records<T, kStageRecs<T>>(smraw + (sizeof(cx<T>) << d.t), ops, d);
     __syncthreads();
     for (u64 g = blockIdx.x; g < sd.ntiles; g += gridDim.x) {
-        tile_reg_run<T>(a, a, sd, ops, forms, tables, stages, g, tile, sh);
+        tile_reg_run<T>(a, a, sd, ops, forms, tables, stages, g, tile, sh, recs);
     }
 }
 
@@ -54,9 +59,10 @@ __global__ void PLGB_TILE_BOUNDS(OCC) k_tile_reg_df(const cx<SI> *ain, cx<SO> *a
     if (threadIdx.x == 0) {
         sd = d;
     }
+    const auto *recs = op_records<df, kStageRecs<df>>(smraw + (sizeof(cx<df>) << d.t), ops, d);
     __syncthreads();
     for (u64 g = blockIdx.x; g < sd.ntiles; g += gridDim.x) {
-        tile_reg_run<df, SI, SO>(ain, aout, sd, ops, forms, tables, stages, g, tile, sh);
+        tile_reg_run<df, SI, SO>(ain, aout, sd, ops, forms, tables, stages, g, tile, sh, recs);
     }
 }
 
@@ -88,7 +94,7 @@ template <class SI, class SO, bool OCC>
 static void launch_df(cudaStream_t s, void *sv, const TilePassDesc &d, const TileOp<df> *ops, const DiagForm<df> *forms,
                       const cx<df> *tables, const StageDesc *stages) {
     const int threads = 1 << (d.t - kRegBits);
-    const size_t smem = sizeof(cx<df>) << d.t;
+    const size_t smem = (sizeof(cx<df>) << d.t) + op_record_bytes<df, kStageRecs<df>>(d.nops);
     static bool attr = false;
     const unsigned grid = tile_grid(k_tile_reg_df<SI, SO, OCC>, threads, smem, d.ntiles, attr);
     k_tile_reg_df<SI, SO, OCC><<<grid, threads, smem, s>>>(static_cast<const cx<SI> *>(sv), static_cast<cx<SO> *>(sv),
@@ -110,7 +116,7 @@ static void launch_df_io(cudaStream_t s, void *sv, int io, const TilePassDesc &d
 
 void launch_tile_pass_reg_df(cudaStream_t s, void *sv, int io, const TilePassDesc &d, const TileOp<df> *ops,
                              const DiagForm<df> *forms, const cx<df> *tables, const StageDesc *stages) {
-    if (d.t < kMinRegTileBits || d.t > 12 || d.ndiag > kMaxDiagOpsPerPass) {
+    if (d.t < kMinRegTileBits || d.t > 12 || d.ndiag > kMaxDiagOpsPerPass || d.nops > kMaxOpsPerPass) {
         throw std::runtime_error("register tile pass (df): unsupported geometry");
     }
     if (tile_variant_occ(128)) {
@@ -124,7 +130,7 @@ template <class T, bool OCC>
 static void launch_reg(cudaStream_t s, cx<T> *sv, const TilePassDesc &d, const TileOp<T> *ops, const DiagForm<T> *forms,
                        const cx<T> *tables, const StageDesc *stages) {
     const int threads = 1 << (d.t - kRegBits);
-    const size_t smem = sizeof(cx<T>) << d.t;
+    const size_t smem = (sizeof(cx<T>) << d.t) + op_record_bytes<T, kStageRecs<T>>(d.nops);
     static bool attr = false;
     const unsigned grid = tile_grid(k_tile_reg<T, OCC>, threads, smem, d.ntiles, attr);
     k_tile_reg<T, OCC><<<grid, threads, smem, s>>>(sv, d, ops, forms, tables, stages);
@@ -135,7 +141,7 @@ static void launch_reg(cudaStream_t s, cx<T> *sv, const TilePassDesc &d, const T
 template <class T>
 void launch_tile_pass_reg(cudaStream_t s, cx<T> *sv, const TilePassDesc &d, const TileOp<T> *ops,
                           const DiagForm<T> *forms, const cx<T> *tables, const StageDesc *stages) {
-    if (d.t < kMinRegTileBits || d.t > 12 || d.ndiag > kMaxDiagOpsPerPass) {
+    if (d.t < kMinRegTileBits || d.t > 12 || d.ndiag > kMaxDiagOpsPerPass || d.nops > kMaxOpsPerPass) {
         throw std::runtime_error("register tile pass: unsupported geometry");
     }
     if (tile_variant_occ(sizeof(T) == 8 ? 128 : 64)) {

@@ -120,8 +120,8 @@ template <class T> __device__ __forceinline__ void from_smem(const cx<T> *tile, 
 
 // One-target op on register bit K for the eight pairs of a thread, one
 // specialisation per op shape so the unrolled body has no mode branches.
-template <int MODE, bool CTRL, class T, int K>
-__device__ __forceinline__ void reg_op_k(cx<T> (&v)[NR], const TileOp<T> &op, const Layout &l) {
+template <int MODE, bool CTRL, class T, int K, class OP>
+__device__ __forceinline__ void reg_op_k(cx<T> (&v)[NR], const OP &op, const Layout &l) {
     const u32 cm = op.rcmask, cv = op.rcval;
     const T ca = op.m[0].x, cb = op.m[0].y;
     const cx<T> m0 = op.m[0], m1 = op.m[1], m2 = op.m[2], m3 = op.m[3];
@@ -135,7 +135,14 @@ __device__ __forceinline__ void reg_op_k(cx<T> (&v)[NR], const TileOp<T> &op, co
             continue;
         }
         const cx<T> v0 = v[i], v1 = v[i1];
-        if constexpr (MODE == RM_SROT_A) { // [[1, -b], [b, 1]]
+        if constexpr (std::is_same_v<T, df> && MODE == RM_SROT_A) {
+            const df nb = -cb;
+            v[i] = cx<T>{df_fma(v0.x, nb, v1.x), df_fma(v0.y, nb, v1.y)};
+            v[i1] = cx<T>{df_fma(v1.x, cb, v0.x), df_fma(v1.y, cb, v0.y)};
+        } else if constexpr (std::is_same_v<T, df> && MODE == RM_SROT_B) {
+            v[i] = cx<T>{df_fma(-v1.x, ca, v0.x), df_fma(-v1.y, ca, v0.y)};
+            v[i1] = cx<T>{df_fma(v0.x, ca, v1.x), df_fma(v0.y, ca, v1.y)};
+        } else if constexpr (MODE == RM_SROT_A) { // [[1, -b], [b, 1]]
             v[i] = cx<T>{v0.x - cb * v1.x, v0.y - cb * v1.y};
             v[i1] = cx<T>{cb * v0.x + v1.x, cb * v0.y + v1.y};
         } else if constexpr (MODE == RM_SROT_B) { // [[a, -1], [1, a]]
@@ -150,8 +157,8 @@ __device__ __forceinline__ void reg_op_k(cx<T> (&v)[NR], const TileOp<T> &op, co
         }
     }
 }
-template <int MODE, bool CTRL, class T>
-__device__ __forceinline__ void reg_op_m(cx<T> (&v)[NR], const TileOp<T> &op, const Layout &l) {
+template <int MODE, bool CTRL, class T, class OP>
+__device__ __forceinline__ void reg_op_m(cx<T> (&v)[NR], const OP &op, const Layout &l) {
     switch (op.rk) {
     case 0: reg_op_k<MODE, CTRL, T, 0>(v, op, l); break;
     case 1: reg_op_k<MODE, CTRL, T, 1>(v, op, l); break;
@@ -159,7 +166,7 @@ __device__ __forceinline__ void reg_op_m(cx<T> (&v)[NR], const TileOp<T> &op, co
     default: reg_op_k<MODE, CTRL, T, 3>(v, op, l); break;
     }
 }
-template <class T> __device__ __forceinline__ void reg_op(cx<T> (&v)[NR], const TileOp<T> &op, const Layout &l) {
+template <class T, class OP> __device__ __forceinline__ void reg_op(cx<T> (&v)[NR], const OP &op, const Layout &l) {
     if (op.rcmask == 0) {
         switch (op.mode) {
         case RM_SROT_A: reg_op_m<RM_SROT_A, false>(v, op, l); break;
@@ -200,11 +207,65 @@ template <class T> struct TileShared {
 
 // Apply pass `d` to tile g of register `a` (all threads of the CTA; the CTA
 // has 2^(d.t - 4) threads and 2^d.t amplitudes of shared memory at `tile`).
-template <class T, class SI = T, class SO = T>
+// Op records of a pass, read by every register stage of every tile: either
+// the global TileOp array or the fields register stages read (RegOpS),
+// copied into shared memory once per CTA (STAGE).  Staging saves global
+// loads per tile but costs registers: measured faster for the complex64
+// kernels and the batched kernels; the single-register double-float kernel
+// reads the global records (the staged form raised its spills six-fold at
+// 128 registers).
+template <class T, bool STAGE> using PassOpRec = std::conditional_t<STAGE, RegOpS<T>, TileOp<T>>;
+template <class T, bool STAGE> constexpr size_t op_record_bytes(int nops) {
+    return STAGE ? static_cast<size_t>(nops) * sizeof(RegOpS<T>) : 0;
+}
+
+// Stage the pass's op records (the fields register stages read) in shared
+// memory; all threads of the CTA; the caller synchronises.
+template <class T>
+__device__ __forceinline__ void stage_ops(RegOpS<T> *sops, const TileOp<T> *__restrict__ ops, const TilePassDesc &d) {
+    for (int k = threadIdx.x; k < d.nops; k += blockDim.x) {
+        const TileOp<T> &o = ops[d.op_begin + k];
+        RegOpS<T> r;
+        r.kind = o.kind;
+        r.mode = o.mode;
+        r.rk = o.rk;
+        r.diag_slot = o.diag_slot;
+        r.rcmask = o.rcmask;
+        r.rcval = o.rcval;
+        r.has_table = o.has_table;
+        r.table_off = o.table_off;
+        r.gcmask = o.gcmask;
+        r.gcval = o.gcval;
+        r.ngforms = o.ngforms;
+        r.gform_begin = o.gform_begin;
+        r.nmforms = o.nmforms;
+        r.mform_begin = o.mform_begin;
+        for (int q = 0; q < 4; q++) {
+            r.m[q] = o.m[q];
+        }
+        sops[k] = r;
+    }
+}
+
+// The records of pass d for tile_reg_run, indexed from d.op_begin: staged at
+// smem_after_tile (all threads; the caller synchronises) or in place.
+template <class T, bool STAGE>
+__device__ __forceinline__ const PassOpRec<T, STAGE> *op_records(unsigned char *smem_after_tile, const TileOp<T> *ops,
+                                                             const TilePassDesc &d) {
+    if constexpr (STAGE) {
+        RegOpS<T> *sops = reinterpret_cast<RegOpS<T> *>(smem_after_tile);
+        stage_ops(sops, ops, d);
+        return sops;
+    } else {
+        return ops + d.op_begin;
+    }
+}
+
+template <class T, class SI = T, class SO = T, class REC>
 __device__ __forceinline__ void tile_reg_run(const cx<SI> *ain, cx<SO> *aout, const TilePassDesc &d,
                                              const TileOp<T> *__restrict__ ops, const DiagForm<T> *__restrict__ forms,
                                              const cx<T> *__restrict__ tables, const StageDesc *__restrict__ stages,
-                                             u64 g, cx<T> *tile, TileShared<T> &sh) {
+                                             u64 g, cx<T> *tile, TileShared<T> &sh, const REC *recs) {
     const int w = d.t - RB;
     const u32 tid = threadIdx.x;
     const int lane = static_cast<int>(tid & 31u);
@@ -235,7 +296,7 @@ __device__ __forceinline__ void tile_reg_run(const cx<SI> *ain, cx<SO> *aout, co
     // prologue: tile-uniform parts of every merged diagonal, one warp per op
     int slot = 0;
     for (int oi = 0; oi < d.nops; oi++) {
-        const TileOp<T> &op = ops[d.op_begin + oi];
+        const REC &op = recs[oi];
         if (op.kind != TK_DIAGTAB) {
             continue;
         }
@@ -313,7 +374,7 @@ __device__ __forceinline__ void tile_reg_run(const cx<SI> *ain, cx<SO> *aout, co
                 cur_stage = si;
             }
             for (int oi = st->op_begin; oi < st->op_begin + st->nops; oi++) {
-                const TileOp<T> &op = ops[oi];
+                const REC &op = recs[oi - d.op_begin];
                 if ((gbase & op.gcmask) != op.gcval) {
                     continue;
                 }
@@ -348,16 +409,17 @@ __device__ __forceinline__ void tile_reg_run(const cx<SI> *ain, cx<SO> *aout, co
                         }
                     }
                 } else if (op.kind == TK_PARITY) {
+                    const TileOp<T> &po = ops[oi];
 #pragma unroll
                     for (int i = 0; i < NR; i++) {
                         const u64 idx = gbase | local_offset_r(cur.at(i), d);
-                        if ((idx & op.cmask) != op.cval) {
-                            if (op.zero_outside) {
+                        if ((idx & po.cmask) != po.cval) {
+                            if (po.zero_outside) {
                                 v[i] = cx<T>{0, 0};
                             }
                             continue;
                         }
-                        v[i] = ((__popcll(idx & op.pmask) & 1) ? op.m[1] : op.m[0]) * v[i];
+                        v[i] = ((__popcll(idx & po.pmask) & 1) ? op.m[1] : op.m[0]) * v[i];
                     }
                 } else {
                     reg_op(v, op, cur);

@@ -282,7 +282,8 @@ def gpu_arm(args) -> dict | None:
         "data": "synthetic (seeded Haar SU(2) + CZ circuit, seed 1001)",
         "config": {"workload": f"config1: {n} qubits complex128, {cycles} cycles x ({n} Haar SU(2) + {n // 2} CZ)",
                    "qubits": n, "gates_per_step": len(circuit), "algorithmic_bytes_per_step": alg_bytes,
-                   "l2": "inputs larger than L2 (16 GiB state)", "parallelism": f"replicas x{ws}",
+                   "l2": (f"inputs larger than L2 ({(1 << n) * 16 / 2**30:g} GiB state)" if (1 << n) * 16 > 129e6
+                          else f"state of {(1 << n) * 16 / 2**20:g} MiB fits L2"), "parallelism": f"replicas x{ws}",
                    "path": f"fused tile passes, 2^{best_tb} amplitudes per tile" if best_tb else "unfused per-gate kernels",
                    "tile_bits": best_tb, "passes_per_step": passes,
                    "tuning_ms_per_step": {str(k): round(v, 1) for k, v in sorted(tune.items())}},

@@ -141,6 +141,12 @@ int plgb_meas_var_sparse(plgb_sv *sv, const int64_t *indptr, int64_t nptr, const
  * fastest */
 int plgb_meas_generate_samples(plgb_sv *sv, const int64_t *wires, int nw, int64_t shots, uint64_t seed,
                                int64_t *out);
+/* generate_mcmc_samples(num_wires, kernelname, num_burnin, num_shots) with
+ * set_random_seed(seed) (LQubitBindings.hpp:340-349 ->
+ * MeasurementsLQubit.hpp:551-594 generate_samples_metropolis,
+ * TransitionKernels.hpp:37-163); out holds num_shots * num_qubits int64 bits */
+int plgb_meas_generate_mcmc_samples(plgb_sv *sv, const char *kernelname, int64_t num_burnin, int64_t num_shots,
+                                    uint64_t seed, int64_t *out);
 
 /* ---- observables (Bindings.hpp:467-591, LQubitBindings.hpp:358-407) ---- */
 /* NamedObsC*(name, wires) */

@@ -307,6 +307,16 @@ int orc_samples(void *h, const int64_t *w, int nw, int64_t shots, uint64_t seed,
         }
     });
 }
+int orc_mcmc_samples(void *h, const char *kernel, int64_t burnin, int64_t shots,
+                     uint64_t seed, int64_t *out) {
+    return with_sv(h, [&](auto &sv) {
+        const auto s = orc::mcmc_samples(sv, std::string(kernel), static_cast<size_t>(burnin),
+                                         static_cast<size_t>(shots), static_cast<size_t>(seed));
+        for (size_t i = 0; i < s.size(); i++) {
+            out[i] = static_cast<int64_t>(s[i]);
+        }
+    });
+}
 int orc_adjoint(void *h, int nops, const char **names, const double *params,
                 const int *nparams, const int64_t *wires, const int *nwires,
                 const uint8_t *inverses, const double *mats,

@@ -1260,6 +1260,65 @@ std::vector<size_t> samples(const StateVec<T> &sv, const std::vector<size_t> &wi
     return out;
 }
 
+// MeasurementsLQubit.hpp:551-594 generate_samples_metropolis and :740-770
+// metropolis_step, with the transition kernels of TransitionKernels.hpp.
+// kernel_factory (TransitionKernels.hpp:150-162) builds the non-zero-random
+// kernel for the type Local (any name but "NonZeroRandom") and the local
+// bit-flip kernel for NonZeroRandom; restated as the reference behaves.
+template <class T>
+std::vector<size_t> mcmc_samples(const StateVec<T> &sv, const std::string &kernel, size_t burnin, size_t shots,
+                                 size_t seed) {
+    std::mt19937 rng;
+    rng.seed(seed);
+    std::uniform_real_distribution<T> distrib(0.0, 1.0);
+    const size_t n = sv.n;
+    const bool nonzero_kernel = kernel != "NonZeroRandom";
+    std::vector<size_t> nz;
+    std::uniform_int_distribution<size_t> d_nz, d_site(0, n - 1), d_bin(0, 1);
+    if (nonzero_kernel) {
+        for (size_t i = 0; i < sv.len(); i++) {
+            if (std::abs(sv.data[i]) > std::numeric_limits<T>::epsilon()) {
+                nz.push_back(i);
+            }
+        }
+        if (nz.empty()) {
+            throw std::runtime_error("MCMC sampling: the state has no non-zero amplitude");
+        }
+        d_nz = std::uniform_int_distribution<size_t>(0, nz.size() - 1);
+    }
+    auto plog = [&](size_t i) { return std::log((sv.data[i] * std::conj(sv.data[i])).real()); };
+    auto step = [&](size_t init) {
+        const T init_plog = plog(init);
+        size_t trans = init;
+        if (nonzero_kernel) {
+            trans = nz[d_nz(rng)];
+        } else {
+            const size_t site = d_site(rng);
+            const size_t value = d_bin(rng);
+            const size_t bit = (static_cast<unsigned>(init) >> static_cast<unsigned>(site)) & 1U;
+            if (value != bit) {
+                trans = bit == 0 ? init + (size_t{1} << site) : init - (size_t{1} << site);
+            }
+        }
+        const T trans_plog = plog(trans);
+        const T alph = std::min<T>(1., T(1) * std::exp(trans_plog - init_plog));
+        const T ran = distrib(rng);
+        return ran < alph ? trans : init;
+    };
+    std::vector<size_t> out(shots * n, 0);
+    size_t idx = 0;
+    for (size_t i = 0; i < burnin; i++) {
+        idx = step(idx);
+    }
+    for (size_t s = 0; s < shots; s++) {
+        idx = step(idx);
+        for (size_t j = 0; j < n; j++) {
+            out[s * n + (n - 1 - j)] = (idx >> j) & 1U;
+        }
+    }
+    return out;
+}
+
 // ---------------------------------------------------------------------------
 // Adjoint Jacobian (LQ/algorithms/AdjointJacobianLQubit.hpp:225-491,
 // core/algorithms/AdjointJacobianBase.hpp, JacobianData.hpp OpsData).

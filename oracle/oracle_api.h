@@ -89,6 +89,9 @@ int ORC_FN(var_obs)(void *sv, const char *spec, const double *cdata,
                     const int64_t *idata, double *out);
 int ORC_FN(samples)(void *sv, const int64_t *wires, int nw, int64_t shots,
                     uint64_t seed, int64_t *out);
+/* generate_mcmc_samples: shots x num_qubits bits (MeasurementsLQubit.hpp:551) */
+int ORC_FN(mcmc_samples)(void *sv, const char *kernel, int64_t burnin,
+                         int64_t shots, uint64_t seed, int64_t *out);
 int ORC_FN(adjoint)(void *sv, int nops, const char **names,
                     const double *params, const int *nparams,
                     const int64_t *wires, const int *nwires,

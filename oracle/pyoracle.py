@@ -68,6 +68,7 @@ def _load(kind: str) -> C.CDLL:
         "expval_obs": (C.c_int, [C.c_void_p, C.c_char_p, _DP, _I64P, _DP]),
         "var_obs": (C.c_int, [C.c_void_p, C.c_char_p, _DP, _I64P, _DP]),
         "samples": (C.c_int, [C.c_void_p, _I64P, C.c_int, C.c_int64, C.c_uint64, _I64P]),
+        "mcmc_samples": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64, C.c_int64, C.c_uint64, _I64P]),
         "adjoint": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_char_p), _DP, _IP, _I64P, _IP, _U8P, _DP, _I64P,
                               _I64P, _IP, _U8P, C.c_int, C.POINTER(C.c_char_p), _DP, _I64P, _I64P, C.c_int,
                               C.c_int, _DP]),
@@ -293,6 +294,11 @@ class OracleSV:
             w = _i64(wires)
             self.o._check(self.o._fn("samples")(self.h, _p(w, _I64P), len(w), shots, seed, _p(out, _I64P)))
         return out.reshape(shots, nw)
+
+    def mcmc_samples(self, kernel: str, burnin: int, shots: int, seed: int) -> np.ndarray:
+        out = np.empty(max(1, shots * self.n), dtype=np.int64)
+        self.o._check(self.o._fn("mcmc_samples")(self.h, kernel.encode(), burnin, shots, seed, _p(out, _I64P)))
+        return out[: shots * self.n].reshape(shots, self.n)
 
     def adjoint(self, ops, obs_specs, trainable, od: ObsData | None = None, apply_ops=False) -> np.ndarray:
         """ops: list of dicts {name, params, wires, inverse, matrix, cwires, cvals}."""

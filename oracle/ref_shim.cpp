@@ -330,6 +330,18 @@ int ref_samples(void *h, const int64_t *w, int nw, int64_t shots, uint64_t seed,
         }
     });
 }
+int ref_mcmc_samples(void *h, const char *kernel, int64_t burnin, int64_t shots,
+                     uint64_t seed, int64_t *out) {
+    return with_sv(h, [&](auto &sv) {
+        Measurements<std::decay_t<decltype(sv)>> m(sv);
+        m.setSeed(static_cast<std::size_t>(seed));
+        auto s = m.generate_samples_metropolis(std::string(kernel), static_cast<std::size_t>(burnin),
+                                               static_cast<std::size_t>(shots));
+        for (std::size_t i = 0; i < s.size(); i++) {
+            out[i] = static_cast<int64_t>(s[i]);
+        }
+    });
+}
 int ref_adjoint(void *h, int nops, const char **names, const double *params,
                 const int *nparams, const int64_t *wires, const int *nwires,
                 const uint8_t *inverses, const double *mats,

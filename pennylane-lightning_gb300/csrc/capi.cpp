@@ -581,6 +581,19 @@ int plgb_meas_generate_samples(plgb_sv *sv, const int64_t *wires, int nw, int64_
     });
 }
 
+int plgb_meas_generate_mcmc_samples(plgb_sv *sv, const char *kernelname, int64_t num_burnin, int64_t num_shots,
+                                    uint64_t seed, int64_t *out) {
+    return with_sv(sv, [&](auto &s) {
+        need(kernelname, "kernelname");
+        need(out, "out");
+        using T = decltype(s.data()->x);
+        const auto r = Measure<T>::mcmc_samples(s, std::string(kernelname), num_burnin, num_shots, seed);
+        if (!r.empty()) {
+            std::memcpy(out, r.data(), r.size() * sizeof(int64_t));
+        }
+    });
+}
+
 // ---- observables --------------------------------------------------------------
 int plgb_obs_named(const char *name, const int64_t *wires, int nw, plgb_obs **out) {
     return guard([&] {

@@ -242,6 +242,8 @@ template <class T> struct Measure {
     static double var_obs(StateVector<T> &sv, const ObsNode &obs);
     static std::vector<int64_t> samples(StateVector<T> &sv, const std::vector<int64_t> &wires, int64_t shots,
                                         uint64_t seed);
+    static std::vector<int64_t> mcmc_samples(StateVector<T> &sv, const std::string &kernel, int64_t burnin,
+                                             int64_t shots, uint64_t seed);
     static void apply_obs(StateVector<T> &sv, const ObsNode &obs);
     // dst = obs |src> (dst: same register size, any content); Pauli sums
     // need no temporary register

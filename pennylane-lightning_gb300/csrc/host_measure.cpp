@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <limits>
 #include <map>
 #include <sstream>
 #include <stack>
@@ -542,6 +543,107 @@ std::vector<int64_t> Measure<T>::samples(StateVector<T> &sv, const std::vector<i
             out[static_cast<size_t>(s) * nw + (nw - 1 - j)] = static_cast<int64_t>((idx >> j) & 1U);
         }
     }
+    return out;
+}
+
+// Metropolis-Hastings sampling (generate_mcmc_samples): MeasurementsLQubit.hpp
+// :551-594 generate_samples_metropolis, :740-770 metropolis_step, transition
+// kernels TransitionKernels.hpp:37-163.  The reference's kernel_factory
+// builds the non-zero-random kernel for the type Local (every name but
+// "NonZeroRandom") and the local bit-flip kernel for NonZeroRandom; this
+// keeps that mapping.  The random numbers do not depend on the state, so they
+// are drawn here from std::mt19937 in the reference's order (proposal draws,
+// then the acceptance draw, per step) and the device runs the chain
+// (kernels_mcmc.cu).
+template <class T>
+std::vector<int64_t> Measure<T>::mcmc_samples(StateVector<T> &sv, const std::string &kernel, int64_t burnin,
+                                              int64_t shots, uint64_t seed) {
+    PLGB_REQUIRE(burnin >= 0 && shots >= 0, "MCMC sampling: burn-in and shots must be non-negative");
+    const int n = sv.num_qubits();
+    const u64 N = sv.length();
+    const u64 steps = static_cast<u64>(burnin) + static_cast<u64>(shots);
+    std::vector<int64_t> out(static_cast<size_t>(shots) * static_cast<size_t>(n));
+    std::mt19937 rng;
+    rng.seed(static_cast<std::mt19937::result_type>(seed));
+    std::uniform_real_distribution<T> distrib(0.0, 1.0);
+    const bool nonzero_kernel = kernel != "NonZeroRandom";
+    std::vector<T> ran(steps);
+    cudaStream_t st = sv.stream();
+    const T eps = std::numeric_limits<T>::epsilon();
+    if (nonzero_kernel) {
+        const u64 nchunks = (N + kMcmcChunk - 1) / kMcmcChunk;
+        auto b0 = sv.scratch().carve({nchunks * sizeof(unsigned)});
+        launch_nz_count<T>(st, sv.data(), N, eps, nchunks, reinterpret_cast<unsigned *>(b0[0]));
+        std::vector<unsigned> counts(nchunks);
+        cuda_check(cudaMemcpyAsync(counts.data(), b0[0], nchunks * sizeof(unsigned), cudaMemcpyDeviceToHost, st),
+                   "D2H");
+        sv.synchronize();
+        std::vector<u64> prefix(nchunks + 1, 0);
+        for (u64 c = 0; c < nchunks; c++) {
+            prefix[c + 1] = prefix[c] + counts[c];
+        }
+        const u64 nnz = prefix[nchunks];
+        PLGB_REQUIRE(nnz > 0, "MCMC sampling: the state has no non-zero amplitude");
+        std::uniform_int_distribution<size_t> d_nz(0, static_cast<size_t>(nnz - 1));
+        std::vector<u64> rank(steps);
+        for (u64 s = 0; s < steps; s++) {
+            rank[s] = d_nz(rng);
+            ran[s] = distrib(rng);
+        }
+        const size_t nout = static_cast<size_t>(shots) * static_cast<size_t>(n);
+        auto b = sv.scratch().carve({(nchunks + 1) * sizeof(u64), steps * sizeof(u64), steps * sizeof(T),
+                                     steps * sizeof(u64), steps * sizeof(T), static_cast<size_t>(shots) * sizeof(u64),
+                                     nout * sizeof(long long)});
+        u64 *d_prefix = reinterpret_cast<u64 *>(b[0]);
+        u64 *d_rank = reinterpret_cast<u64 *>(b[1]);
+        T *d_ran = reinterpret_cast<T *>(b[2]);
+        u64 *d_tidx = reinterpret_cast<u64 *>(b[3]);
+        T *d_tplog = reinterpret_cast<T *>(b[4]);
+        u64 *d_idx = reinterpret_cast<u64 *>(b[5]);
+        long long *d_out = reinterpret_cast<long long *>(b[6]);
+        cuda_check(cudaMemcpyAsync(d_prefix, prefix.data(), prefix.size() * sizeof(u64), cudaMemcpyHostToDevice, st),
+                   "H2D");
+        if (steps > 0) {
+            cuda_check(cudaMemcpyAsync(d_rank, rank.data(), steps * sizeof(u64), cudaMemcpyHostToDevice, st), "H2D");
+            cuda_check(cudaMemcpyAsync(d_ran, ran.data(), steps * sizeof(T), cudaMemcpyHostToDevice, st), "H2D");
+            launch_nz_select<T>(st, sv.data(), N, eps, d_prefix, nchunks, d_rank, steps, d_tidx, d_tplog);
+            launch_mcmc_chain_nz<T>(st, sv.data(), d_tidx, d_tplog, d_ran, steps, static_cast<u64>(burnin), d_idx);
+        }
+        launch_index_bits(st, d_idx, static_cast<u64>(shots), n, d_out);
+        if (nout > 0) {
+            cuda_check(cudaMemcpyAsync(out.data(), d_out, nout * sizeof(long long), cudaMemcpyDeviceToHost, st), "D2H");
+        }
+        sv.synchronize();
+        return out;
+    }
+    // the reference tests bits of the index truncated to 32 bits
+    PLGB_REQUIRE(n <= 32, "MCMC sampling with the local kernel: at most 32 qubits");
+    std::uniform_int_distribution<size_t> dist_site(0, static_cast<size_t>(n - 1)), dist_bin(0, 1);
+    std::vector<unsigned char> site(steps), value(steps);
+    for (u64 s = 0; s < steps; s++) {
+        site[s] = static_cast<unsigned char>(dist_site(rng));
+        value[s] = static_cast<unsigned char>(dist_bin(rng));
+        ran[s] = distrib(rng);
+    }
+    const size_t nout = static_cast<size_t>(shots) * static_cast<size_t>(n);
+    auto b = sv.scratch().carve({steps, steps, steps * sizeof(T), static_cast<size_t>(shots) * sizeof(u64),
+                                 nout * sizeof(long long)});
+    auto *d_site = reinterpret_cast<unsigned char *>(b[0]);
+    auto *d_value = reinterpret_cast<unsigned char *>(b[1]);
+    T *d_ran = reinterpret_cast<T *>(b[2]);
+    u64 *d_idx = reinterpret_cast<u64 *>(b[3]);
+    long long *d_out = reinterpret_cast<long long *>(b[4]);
+    if (steps > 0) {
+        cuda_check(cudaMemcpyAsync(d_site, site.data(), steps, cudaMemcpyHostToDevice, st), "H2D");
+        cuda_check(cudaMemcpyAsync(d_value, value.data(), steps, cudaMemcpyHostToDevice, st), "H2D");
+        cuda_check(cudaMemcpyAsync(d_ran, ran.data(), steps * sizeof(T), cudaMemcpyHostToDevice, st), "H2D");
+        launch_mcmc_chain_local<T>(st, sv.data(), d_site, d_value, d_ran, steps, static_cast<u64>(burnin), d_idx);
+    }
+    launch_index_bits(st, d_idx, static_cast<u64>(shots), n, d_out);
+    if (nout > 0) {
+        cuda_check(cudaMemcpyAsync(out.data(), d_out, nout * sizeof(long long), cudaMemcpyDeviceToHost, st), "D2H");
+    }
+    sv.synchronize();
     return out;
 }
 

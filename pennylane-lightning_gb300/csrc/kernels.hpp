@@ -110,6 +110,21 @@ void launch_pauli_accumulate(cudaStream_t s, const cx<T> *psi, cx<T> *out, u64 N
 // Probabilities: all wires (elementwise), or marginal over `k` wires given by
 // their bit positions (wires[0] = MSB of the output index).
 template <class T> void launch_probs_all(cudaStream_t s, const cx<T> *sv, u64 N, T *out);
+
+// Metropolis-Hastings sampling (kernels_mcmc.cu)
+constexpr u64 kMcmcChunk = 4096; // amplitudes per non-zero counting chunk
+template <class T>
+void launch_nz_count(cudaStream_t s, const cx<T> *sv, u64 N, T eps, u64 nchunks, unsigned *counts);
+template <class T>
+void launch_nz_select(cudaStream_t s, const cx<T> *sv, u64 N, T eps, const u64 *prefix, u64 nchunks, const u64 *rank,
+                      u64 steps, u64 *tidx, T *tplog);
+template <class T>
+void launch_mcmc_chain_nz(cudaStream_t s, const cx<T> *sv, const u64 *tidx, const T *tplog, const T *ran, u64 steps,
+                          u64 burnin, u64 *out);
+template <class T>
+void launch_mcmc_chain_local(cudaStream_t s, const cx<T> *sv, const unsigned char *site, const unsigned char *value,
+                             const T *ran, u64 steps, u64 burnin, u64 *out);
+void launch_index_bits(cudaStream_t s, const u64 *idx, u64 shots, int n, long long *out);
 template <class T>
 void launch_probs_marginal(cudaStream_t s, const cx<T> *sv, u64 N, int k, const TBits &tb, double *out);
 

@@ -368,12 +368,6 @@ void launch_csr_apply(cudaStream_t s, const cx<T> *sv, cx<T> *out, u64 N, const 
 // ---------------------------------------------------------------------------
 // Probabilities.
 // ---------------------------------------------------------------------------
-// |psi_i|^2 rounded exactly as std::norm does without contraction (two
-// products, one sum), so the distribution a seeded sampler consumes is
-// bit-identical to the reference's.
-__device__ __forceinline__ double norm_rn(cx<double> x) { return __dadd_rn(__dmul_rn(x.x, x.x), __dmul_rn(x.y, x.y)); }
-__device__ __forceinline__ float norm_rn(cx<float> x) { return __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y)); }
-
 template <class T> __global__ void k_probs_all(const cx<T> *__restrict__ a, u64 N, T *__restrict__ out) {
     GRID_STRIDE(i, N) { out[i] = norm_rn(a[i]); }
 }

@@ -41,6 +41,14 @@ template <class T> __host__ __device__ inline cx<T> cfma(cx<T> a, cx<T> b, cx<T>
     return {acc.x + a.x * b.x - a.y * b.y, acc.y + a.x * b.y + a.y * b.x};
 }
 
+#if defined(__CUDACC__)
+// |psi_i|^2 rounded exactly as std::norm does without contraction (two
+// products, one sum), so the distribution a seeded sampler consumes is
+// bit-identical to the reference's.
+__device__ __forceinline__ double norm_rn(cx<double> x) { return __dadd_rn(__dmul_rn(x.x, x.x), __dmul_rn(x.y, x.y)); }
+__device__ __forceinline__ float norm_rn(cx<float> x) { return __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y)); }
+#endif
+
 // Insert a zero bit at each of the `nins` ascending positions `ins`.
 __host__ __device__ inline u64 insert_zeros(u64 k, const int *ins, int nins) {
     for (int i = 0; i < nins; i++) {

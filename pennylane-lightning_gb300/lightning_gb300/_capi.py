@@ -70,6 +70,7 @@ SIGNATURES = {
     "plgb_meas_var_matrix": (C.c_int, [VP, DP, I64P, C.c_int, DP]),
     "plgb_meas_var_sparse": (C.c_int, [VP, I64P, C.c_int64, I64P, DP, C.c_int64, DP]),
     "plgb_meas_generate_samples": (C.c_int, [VP, I64P, C.c_int, C.c_int64, C.c_uint64, I64P]),
+    "plgb_meas_generate_mcmc_samples": (C.c_int, [VP, C.c_char_p, C.c_int64, C.c_int64, C.c_uint64, I64P]),
     "plgb_obs_named": (C.c_int, [C.c_char_p, I64P, C.c_int, C.POINTER(VP)]),
     "plgb_obs_hermitian": (C.c_int, [DP, I64P, C.c_int, C.POINTER(VP)]),
     "plgb_obs_tensor_prod": (C.c_int, [C.POINTER(VP), C.c_int, C.POINTER(VP)]),

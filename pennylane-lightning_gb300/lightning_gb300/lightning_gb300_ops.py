@@ -532,7 +532,16 @@ class _MeasurementsBase:
         return out[: shots * nw].reshape(shots, nw).astype(np.uint64)
 
     def generate_mcmc_samples(self, num_wires, kernelname, num_burnin, num_shots):
-        raise LightningException("MCMC sampling is not provided by the GB300 backend")
+        """Metropolis-Hastings samples, shape (num_shots, num_wires), num_wires
+        = the register's qubits (LQubitBindings.hpp:340-349)."""
+        n = self._sv._n
+        if int(num_wires) != n:
+            raise LightningException(f"generate_mcmc_samples samples all {n} qubits (num_wires = {num_wires})")
+        shots = int(num_shots)
+        out = np.empty(max(1, shots * n), dtype=np.int64)
+        call("plgb_meas_generate_mcmc_samples", self._sv._h, str(kernelname).encode(), int(num_burnin), shots,
+             self._next_seed(), out.ctypes.data_as(I64P))
+        return out[: shots * n].reshape(shots, n).astype(np.uint64)
 
     def expval(self, *args):
         r = C.c_double()

@@ -116,6 +116,9 @@ def main() -> int:
         meta[f"ham_{tag}"] = {"terms": [[c, wd, ws] for c, wd, ws in terms]}
         arrays[f"samples_{tag}"] = s.samples(2000, 37)
         arrays[f"samples_w_{tag}"] = s.samples(2000, 37, [3, 0])
+        # Metropolis-Hastings samples for both transition-kernel names
+        for kname in ("Local", "NonZeroRandom"):
+            arrays[f"mcmc_{kname}_{tag}"] = s.mcmc_samples(kname, 50, 1500, 91)
 
     # config 0 (reduced n and full n = 20), c128
     for nq, layers, tag in ((8, 3, "small"), (20, 10, "full")):

@@ -1,6 +1,7 @@
 """GPU backend vs the golden fixtures produced by the reference's own C++
 (tests/golden/make_golden.py): per-gate states, probabilities (bit-exact for
-all wires), expectation values, seeded samples (exact), and config 0 at its
+all wires), expectation values, seeded and Metropolis-Hastings samples
+(exact), and config 0 at its
 full size (20 qubits, 10 layers: <sum Z> and the 600-parameter Jacobian).
 """
 import json
@@ -70,6 +71,10 @@ def test_measurements_vs_reference(ops_module, golden, tag):
     m.set_random_seed(37)
     assert np.array_equal(m.generate_samples(5, 2000).astype(np.int64), g[f"samples_{tag}"])
     assert np.array_equal(m.generate_samples([3, 0], 2000).astype(np.int64), g[f"samples_w_{tag}"])
+    m.set_random_seed(91)
+    for kname in ("Local", "NonZeroRandom"):
+        s = m.generate_mcmc_samples(5, kname, 50, 1500).astype(np.int64)
+        assert np.array_equal(s, g[f"mcmc_{kname}_{tag}"]), kname
 
 
 @pytest.mark.parametrize("size", ["small", "full"])

@@ -4,7 +4,9 @@ named, Hermitian, Pauli-sum, mixed and sparse observables, seeded samples.
 Mirrors pennylane_lightning/core/simulators/lightning_qubit/measurements/tests/
 Test_MeasurementsLQubit.cpp (:205-430 expval by name/matrix, :534-968 probs
 index ordering with permuted targets) and core/measurements/tests/
-Test_MeasurementsBase.cpp (:1319-1323 seeded samples).
+Test_MeasurementsBase.cpp (:1319-1323 seeded samples); Metropolis-Hastings
+samples (MeasurementsLQubit.hpp:551-594, TransitionKernels.hpp) exactly as
+the oracle draws them.
 """
 import numpy as np
 import pytest
@@ -133,3 +135,49 @@ def test_samples_exact(ops_module, oracle, dt):
     for wires in ([3], [7, 0, 2]):
         s = m.generate_samples(wires, 3000)
         assert np.array_equal(s.astype(np.int64), o.samples(3000, 37, wires))
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+def test_mcmc_samples_exact(ops_module, oracle, dt):
+    # generate_mcmc_samples: both transition-kernel names, with and without
+    # burn-in, on a dense state and on one with zero amplitudes (which the
+    # non-zero-random kernel never proposes).  Integer outputs must equal the
+    # oracle's for the same seed.
+    rng, sv, m, o = _setup(ops_module, oracle, 9, dt, seed_of("mcmc", dt.__name__))
+    for zeros in (False, True):
+        if zeros:
+            st = rand_state(rng, 9, dt)
+            st[rng.random(st.size) < 0.5] = 0
+            st = (st / np.linalg.norm(st)).astype(dt)
+            sv.updateData(st)
+            o.set_state(st)
+        for kname in ("Local", "NonZeroRandom"):
+            for burnin, shots, seed in ((0, 4000, 3), (250, 3000, 77)):
+                m.set_random_seed(seed)
+                s = m.generate_mcmc_samples(9, kname, burnin, shots)
+                assert s.shape == (shots, 9)
+                assert np.array_equal(s.astype(np.int64), o.mcmc_samples(kname, burnin, shots, seed)), (zeros, kname)
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+def test_mcmc_samples_large_register(ops_module, oracle, dt):
+    # 2^20 amplitudes: 256 counting chunks, so the rank -> index search spans
+    # chunk boundaries.
+    rng, sv, m, o = _setup(ops_module, oracle, 20, dt, seed_of("mcmc20", dt.__name__))
+    m.set_random_seed(2024)
+    s = m.generate_mcmc_samples(20, "Local", 100, 2000)
+    assert np.array_equal(s.astype(np.int64), o.mcmc_samples("Local", 100, 2000, 2024))
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+def test_mcmc_samples_edges(ops_module, oracle, dt):
+    from lightning_gb300.lightning_gb300_ops import LightningException
+
+    rng, sv, m, o = _setup(ops_module, oracle, 4, dt, seed_of("mcmc-edge", dt.__name__))
+    m.set_random_seed(1)
+    assert m.generate_mcmc_samples(4, "Local", 10, 0).shape == (0, 4)
+    with pytest.raises(LightningException):
+        m.generate_mcmc_samples(3, "Local", 0, 10)  # every qubit is sampled
+    sv.updateData(np.zeros(16, dtype=dt))
+    with pytest.raises(LightningException):
+        m.generate_mcmc_samples(4, "Local", 0, 10)  # no non-zero amplitude to propose

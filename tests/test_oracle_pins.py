@@ -79,6 +79,9 @@ def test_golden_measurements(oracle, golden, tag):
     # seeded samples: exact integers
     assert np.array_equal(o.samples(2000, 37), g[f"samples_{tag}"])
     assert np.array_equal(o.samples(2000, 37, [3, 0]), g[f"samples_w_{tag}"])
+    # Metropolis-Hastings (MeasurementsLQubit.hpp:551-594): exact integers
+    for kname in ("Local", "NonZeroRandom"):
+        assert np.array_equal(o.mcmc_samples(kname, 50, 1500, 91), g[f"mcmc_{kname}_{tag}"]), kname
 
 
 def test_golden_config0_small(oracle, golden):
@@ -213,6 +216,15 @@ def test_restatement_vs_reference_measurements(oracle, dt):
     spec2 = f"ham 2 0.5 prod 2 named PauliX 0 herm 1 3 {off} -1.25 named Hadamard 2"
     assert_close(a.var_obs(spec2, od), b.var_obs(spec2, od), dt, scale=100)
     assert np.array_equal(a.samples(3000, 11), b.samples(3000, 11))
+    # MCMC on a state with zeros (the non-zero-random kernel skips them)
+    st0 = st.copy()
+    st0[rng.random(st0.size) < 0.4] = 0
+    st0 = (st0 / np.linalg.norm(st0)).astype(dt)
+    a.set_state(st0)
+    b.set_state(st0)
+    for kname in ("Local", "NonZeroRandom", "other"):
+        for burnin, shots in ((0, 700), (33, 500)):
+            assert np.array_equal(a.mcmc_samples(kname, burnin, shots, 5), b.mcmc_samples(kname, burnin, shots, 5))
 
 
 def test_restatement_vs_reference_adjoint(oracle):

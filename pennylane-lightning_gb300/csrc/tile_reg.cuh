@@ -69,6 +69,31 @@ template <class T> __device__ __forceinline__ cx<T> shx(cx<T> v, int m) {
 }
 
 
+// State amplitudes stream through a pass once: load and store them with the
+// evict-first cache policy so that they do not push the pass's diagonal
+// tables and op records (read by every tile) out of L1.
+__device__ __forceinline__ cx<float> ld_stream(const cx<float> *p) {
+    const float2 t = __ldcs(reinterpret_cast<const float2 *>(p));
+    return cx<float>{t.x, t.y};
+}
+__device__ __forceinline__ cx<double> ld_stream(const cx<double> *p) {
+    const double2 t = __ldcs(reinterpret_cast<const double2 *>(p));
+    return cx<double>{t.x, t.y};
+}
+__device__ __forceinline__ cx<df> ld_stream(const cx<df> *p) {
+    const float4 t = __ldcs(reinterpret_cast<const float4 *>(p));
+    return cx<df>{df{t.x, t.y}, df{t.z, t.w}};
+}
+__device__ __forceinline__ void st_stream(cx<float> *p, cx<float> v) {
+    __stcs(reinterpret_cast<float2 *>(p), make_float2(v.x, v.y));
+}
+__device__ __forceinline__ void st_stream(cx<double> *p, cx<double> v) {
+    __stcs(reinterpret_cast<double2 *>(p), make_double2(v.x, v.y));
+}
+__device__ __forceinline__ void st_stream(cx<df> *p, cx<df> v) {
+    __stcs(reinterpret_cast<float4 *>(p), make_float4(v.x.hi, v.x.lo, v.y.hi, v.y.lo));
+}
+
 // Layout of a register stage, held in registers: local index of register
 // slot i of this thread = jt | (bit k of i placed at local bit rb[k]).
 // The canonical layout (load / store) has rb = {w, w+1, w+2, w+3}, jt = tid.
@@ -291,7 +316,7 @@ __device__ __forceinline__ void tile_reg_run(const cx<SI> *ain, cx<SO> *aout, co
     const u64 tbase = gbase | off_t;
 #pragma unroll
     for (int i = 0; i < NR; i++) {
-        v[i] = ld_conv<T, SI>(ain[tbase | off_r(i)]);
+        v[i] = ld_conv<T, SI>(ld_stream(&ain[tbase | off_r(i)]));
     }
     // prologue: tile-uniform parts of every merged diagonal, one warp per op
     int slot = 0;
@@ -488,7 +513,7 @@ __device__ __forceinline__ void tile_reg_run(const cx<SI> *ain, cx<SO> *aout, co
     const cx<T> f = sh.factor;
 #pragma unroll
     for (int i = 0; i < NR; i++) {
-        aout[tbase | off_r(i)] = st_conv<SO, T>(f * v[i]);
+        st_stream(&aout[tbase | off_r(i)], st_conv<SO, T>(f * v[i]));
     }
     __syncthreads();
 }

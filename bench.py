@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-circuits leg (config 2)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the autograd adjoint leg (config 3)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg (config 4)")
+    ap.add_argument("--adjoint-qubits", type=int, default=28, help="config-3 register size (32: the 64 GiB variant)")
+    ap.add_argument("--adjoint-layers", type=int, default=12, help="config-3 layers (6 for the 32-qubit variant)")
+    ap.add_argument("--adjoint-fd", type=int, default=0,
+                    help="also check this many sampled gradient entries by central finite differences")
     ap.add_argument("--serve-seconds", type=float, default=2.0,
                     help="length of the config-4 arrival window replayed by the serving leg")
     return ap.parse_args()
@@ -318,7 +322,7 @@ def gpu_arm(args) -> dict | None:
         if not args.no_batch:
             res["batched"] = {"c128": batched_leg(ops, 128), "c64": batched_leg(ops, 64)}
         if not args.no_adjoint:
-            res["adjoint"] = adjoint_leg()
+            res["adjoint"] = adjoint_leg(args.adjoint_qubits, args.adjoint_layers, args.adjoint_fd)
         if not args.no_serve:
             res["serving"] = serve_leg(args.serve_seconds)
     return res
@@ -362,7 +366,7 @@ def batched_leg(ops, prec: int, plain_every: int = 32) -> dict:
     packed = config2_packed(4096, seed=1002)
     names = {v: k for k, v in gate_codes().items()}
     eng = BatchEngine(prec)
-    eng.run(packed.select(range(64)))  # warm-up: tile-size autotuning and device arenas
+    eng.run(packed)  # warm-up: tile-size autotuning, device arenas and pinned staging at full size
     t = time.perf_counter()
     eng.run(packed)
     dt = time.perf_counter() - t
@@ -388,9 +392,12 @@ def batched_leg(ops, prec: int, plain_every: int = 32) -> dict:
             "speedup_vs_plain": packed.num_circuits / dt / plain}
 
 
-def adjoint_leg(n: int = 28, layers: int = 12) -> dict:
+def adjoint_leg(n: int = 28, layers: int = 12, fd: int = 0) -> dict:
     """Config 3: <H> of the 200-term Hamiltonian and its gradient in all
-    1008 rotation angles through torch.autograd (checkpointed adjoint)."""
+    rotation angles (1008 at 28 qubits x 12 layers, 576 at 32 x 6) through
+    torch.autograd (checkpointed adjoint: two registers alive in the
+    backward).  fd > 0: central finite differences (h = 1e-4) on that many
+    sampled angles, as a check of the gradient at this size."""
     import torch
 
     from lightning_gb300.torch_adjoint import config3_circuit, expval
@@ -402,9 +409,22 @@ def adjoint_leg(n: int = 28, layers: int = 12) -> dict:
     t1 = time.perf_counter()
     e.backward()
     t2 = time.perf_counter()
-    return {"metric": "config3 gradient s", "qubits": n, "params": int(theta.size), "forward_s": t1 - t0,
-            "backward_s": t2 - t1, "params_per_s": theta.size / (t2 - t0), "registers_in_backward": 2,
-            "value": float(e.item())}
+    out = {"metric": "config3 gradient s", "qubits": n, "layers": layers, "params": int(theta.size),
+           "forward_s": t1 - t0, "backward_s": t2 - t1, "params_per_s": theta.size / (t2 - t0),
+           "registers_in_backward": 2, "state_gib": (1 << n) * 16 / 2**30, "value": float(e.item())}
+    if fd > 0:
+        grad = t.grad.numpy()
+        idx = np.random.default_rng(1003).choice(theta.size, size=min(fd, theta.size), replace=False)
+        h, errs = 1e-4, []
+        for j in idx:
+            tp, tm = theta.copy(), theta.copy()
+            tp[j] += h
+            tm[j] -= h
+            with torch.no_grad():
+                d = (float(expval(torch.tensor(tp), circ)) - float(expval(torch.tensor(tm), circ))) / (2 * h)
+            errs.append(abs(d - grad[j]))
+        out["fd_check"] = {"params": [int(j) for j in idx], "h": h, "max_abs_err": float(max(errs))}
+    return out
 
 
 def serve_leg(seconds: float) -> dict:

@@ -71,6 +71,11 @@ template <class T> BatchEngine<T>::BatchEngine() {
     cuda_check(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking), "cudaStreamCreate");
     cuda_check(cudaEventCreate(&ev0_), "cudaEventCreate");
     cuda_check(cudaEventCreate(&ev1_), "cudaEventCreate");
+    cuda_check(cudaEventCreate(&ev_run0_), "cudaEventCreate");
+    for (int i = 0; i < 2; i++) {
+        cuda_check(cudaEventCreate(&wev0_[i]), "cudaEventCreate");
+        cuda_check(cudaEventCreate(&wev1_[i]), "cudaEventCreate");
+    }
 }
 
 template <class T> BatchEngine<T>::~BatchEngine() {
@@ -82,10 +87,21 @@ template <class T> BatchEngine<T>::~BatchEngine() {
             cudaFree(p);
         }
     }
-    for (void *p : {h_prog_, h_items_, h_out_}) {
-        if (p) {
-            cudaFreeHost(p);
+    for (int i = 0; i < 2; i++) {
+        for (void *p : {h_prog_[i], h_items_[i], h_out_[i]}) {
+            if (p) {
+                cudaFreeHost(p);
+            }
         }
+        if (wev0_[i]) {
+            cudaEventDestroy(wev0_[i]);
+        }
+        if (wev1_[i]) {
+            cudaEventDestroy(wev1_[i]);
+        }
+    }
+    if (ev_run0_) {
+        cudaEventDestroy(ev_run0_);
     }
     if (ev0_) {
         cudaEventDestroy(ev0_);
@@ -198,12 +214,12 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
     }
     stats_.tile_bits = tsel;
 
-    // ---- lower + compile on a pool of host threads
-    const auto t_comp = std::chrono::steady_clock::now();
+    // ---- lower + compile on a pool of host threads, one wave at a time
     std::vector<Compiled<T>> comp(static_cast<size_t>(nc));
     std::atomic<int> next{0};
+    int comp_hi = 0;
     auto worker = [&]() {
-        for (int c = next++; c < nc; c = next++) {
+        for (int c = next++; c < comp_hi; c = next++) {
             Compiled<T> &cc = comp[static_cast<size_t>(c)];
             try {
                 cc.n = in.num_qubits[c];
@@ -268,9 +284,12 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
             }
         }
     };
-    {
+    auto compile_range = [&](int lo, int hi) {
+        const auto t_comp = std::chrono::steady_clock::now();
+        next = lo;
+        comp_hi = hi;
         int nt = threads_ > 0 ? threads_ : static_cast<int>(std::thread::hardware_concurrency());
-        nt = std::max(1, std::min({nt, 64, nc}));
+        nt = std::max(1, std::min({nt, 64, hi - lo}));
         std::vector<std::thread> pool;
         for (int i = 1; i < nt; i++) {
             pool.emplace_back(worker);
@@ -279,36 +298,61 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
         for (auto &th : pool) {
             th.join();
         }
-    }
-    for (auto &cc : comp) {
-        if (!cc.error.empty()) {
-            throw PLError(cc.error);
+        for (int c = lo; c < hi; c++) {
+            if (!comp[static_cast<size_t>(c)].error.empty()) {
+                throw PLError(comp[static_cast<size_t>(c)].error);
+            }
         }
-    }
-    stats_.compile_ms = ms_since(t_comp);
+        stats_.compile_ms += ms_since(t_comp);
+    };
 
-    // ---- waves
+    // ---- waves of registers that fit the memory budget, planned from the
+    // register sizes.  The host compiles and packs wave k+1 while the device
+    // runs wave k: pinned staging buffers alternate between two sets, the
+    // device arenas are reused in stream order.
+    std::vector<std::pair<int, int>> wave_rng;
     stats_.wave_of.assign(static_cast<size_t>(nc), 0);
-    float dev_ms_total = 0;
-    int c0 = 0;
-    while (c0 < nc) {
-        // registers of this wave
+    for (int c0 = 0; c0 < nc;) {
         int c1 = c0;
         size_t sv_bytes = 0;
-        std::vector<size_t> sv_off;
         while (c1 < nc) {
-            const size_t b = align_up(sizeof(cx<T>) << comp[static_cast<size_t>(c1)].ne);
+            const size_t b = align_up(sizeof(cx<T>) << std::max(in.num_qubits[c1], kBatchMinQubits));
             if (c1 > c0 && sv_bytes + b > wave_bytes_) {
                 break;
             }
-            sv_off.push_back(sv_bytes);
             sv_bytes += b;
+            stats_.wave_of[static_cast<size_t>(c1)] = static_cast<int>(wave_rng.size());
             c1++;
         }
-        const int wn = c1 - c0;
+        wave_rng.emplace_back(c0, c1);
+        c0 = c1;
+    }
+    const int nwaves = static_cast<int>(wave_rng.size());
+    stats_.wave_done_ms.assign(static_cast<size_t>(nwaves), 0.0);
+    float dev_ms_total = 0;
+
+    struct WaveRun {
+        int k{0}, set{0}, c0{0}, c1{0};
+        std::vector<std::pair<int64_t, size_t>> obs_item; // (observable index, item index)
+        size_t nred_items{0};
+        double enqueue_ms{0};
+    };
+    auto prepare_and_enqueue = [&](int k) -> WaveRun {
+        WaveRun W;
+        W.k = k;
+        W.set = k & 1;
+        W.c0 = wave_rng[static_cast<size_t>(k)].first;
+        W.c1 = wave_rng[static_cast<size_t>(k)].second;
+        const int c0 = W.c0, c1 = W.c1, set = W.set;
+        compile_range(c0, c1);
+        // registers of this wave
+        size_t sv_bytes = 0;
+        std::vector<size_t> sv_off;
         for (int c = c0; c < c1; c++) {
-            stats_.wave_of[static_cast<size_t>(c)] = stats_.waves;
+            sv_off.push_back(sv_bytes);
+            sv_bytes += align_up(sizeof(cx<T>) << comp[static_cast<size_t>(c)].ne);
         }
+        const int wn = c1 - c0;
         grow(d_states_, c_states_, sv_bytes, false);
         char *states = static_cast<char *>(d_states_);
 
@@ -336,9 +380,9 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
         pbytes = std::max<size_t>(pbytes, 256);
         const auto t_pack = std::chrono::steady_clock::now();
         stats_.program_bytes += static_cast<double>(pbytes);
-        grow(h_prog_, ch_prog_, pbytes, true);
+        grow(h_prog_[set], ch_prog_[set], pbytes, true);
         grow(d_prog_, c_prog_, pbytes, false);
-        char *hp = static_cast<char *>(h_prog_);
+        char *hp = static_cast<char *>(h_prog_[set]);
         for (int i = 0; i < wn; i++) {
             const auto &pr = *comp[static_cast<size_t>(c0 + i)].prog;
             if (!comp[static_cast<size_t>(c0 + i)].fast) {
@@ -457,7 +501,7 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
         // reductions: one item per (register, observable, flip-mask group)
         std::vector<PauliGroup> groups;
         std::vector<BatchRedItem<T>> ritems;
-        std::vector<std::pair<int64_t, size_t>> obs_item; // (observable index, item index)
+        auto &obs_item = W.obs_item;
         u64 rblocks = 0;
         for (int i = 0; i < wn; i++) {
             const auto &cc = comp[static_cast<size_t>(c0 + i)];
@@ -487,9 +531,9 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
         const size_t b_recs = align_up(std::max<size_t>(1, recs.size()) * sizeof(DevRecipe));
         const size_t b_facs = align_up(std::max<size_t>(1, facs.size()) * sizeof(TableFactor));
         const size_t ibytes = b_titems + b_ptrs + b_ritems + b_groups + b_recs + b_facs;
-        grow(h_items_, ch_items_, ibytes, true);
+        grow(h_items_[set], ch_items_[set], ibytes, true);
         grow(d_items_, c_items_, ibytes, false);
-        char *hi = static_cast<char *>(h_items_);
+        char *hi = static_cast<char *>(h_items_[set]);
         char *di = static_cast<char *>(d_items_);
         auto *d_titems = reinterpret_cast<BatchTileItem<T> *>(di);
         auto *d_ptrs = reinterpret_cast<cx<T> **>(di + b_titems);
@@ -516,12 +560,17 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
 
         const size_t nred = std::max<size_t>(1, ritems.size());
         grow(d_red_, c_red_, (rblocks + nred) * sizeof(double), false);
-        grow(h_out_, ch_out_, nred * sizeof(double), true);
+        grow(h_out_[set], ch_out_[set], nred * sizeof(double), true);
+        W.nred_items = ritems.size();
         double *partials = static_cast<double *>(d_red_);
         double *item_sums = partials + rblocks;
 
         // ---- device work of the wave
-        cuda_check(cudaEventRecord(ev0_, s_), "event");
+        cuda_check(cudaEventRecord(wev0_[set], s_), "event");
+        if (k == 0) {
+            cuda_check(cudaEventRecord(ev_run0_, s_), "event");
+            W.enqueue_ms = ms_since(t_start);
+        }
         cuda_check(cudaMemcpyAsync(dp, hp, pbytes, cudaMemcpyHostToDevice, s_), "H2D programs");
         cuda_check(cudaMemcpyAsync(di, hi, ibytes, cudaMemcpyHostToDevice, s_), "H2D items");
         cuda_check(cudaMemsetAsync(states, 0, sv_bytes, s_), "memset registers");
@@ -561,18 +610,27 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
         if (!ritems.empty()) {
             launch_pauli_batch<T>(s_, d_ritems, static_cast<int>(ritems.size()), rblocks, partials, item_sums);
             stats_.launches += 2;
-            cuda_check(cudaMemcpyAsync(h_out_, item_sums, ritems.size() * sizeof(double), cudaMemcpyDeviceToHost, s_),
+            cuda_check(cudaMemcpyAsync(h_out_[set], item_sums, ritems.size() * sizeof(double),
+                                       cudaMemcpyDeviceToHost, s_),
                        "D2H sums");
         }
-        cuda_check(cudaEventRecord(ev1_, s_), "event");
-        cuda_check(cudaEventSynchronize(ev1_), "wave sync");
+        cuda_check(cudaEventRecord(wev1_[set], s_), "event");
+        return W;
+    };
+    double run0_ms = 0; // host time at which the device work of wave 0 was enqueued
+    auto finish = [&](const WaveRun &W) {
+        const int set = W.set, c0 = W.c0, c1 = W.c1, wn = c1 - c0;
+        cuda_check(cudaEventSynchronize(wev1_[set]), "wave sync");
         float wms = 0;
-        cuda_check(cudaEventElapsedTime(&wms, ev0_, ev1_), "event time");
+        cuda_check(cudaEventElapsedTime(&wms, wev0_[set], wev1_[set]), "event time");
         dev_ms_total += wms;
-        stats_.wave_done_ms.push_back(ms_since(t_start));
+        float done = 0;
+        cuda_check(cudaEventElapsedTime(&done, ev_run0_, wev1_[set]), "event time");
+        stats_.wave_done_ms[static_cast<size_t>(W.k)] = run0_ms + static_cast<double>(done);
 
         // observable sums in a fixed order
-        const double *sums = static_cast<const double *>(h_out_);
+        const double *sums = static_cast<const double *>(h_out_[set]);
+        const auto &obs_item = W.obs_item;
         int64_t ob_last = -1;
         for (const auto &oi : obs_item) {
             if (oi.first != ob_last) {
@@ -590,8 +648,15 @@ template <class T> void BatchEngine<T>::run(const BatchInput &in, double *out) {
             }
         }
         stats_.waves++;
-        c0 = c1;
+    };
+    WaveRun cur = prepare_and_enqueue(0);
+    run0_ms = cur.enqueue_ms;
+    for (int k = 1; k < nwaves; k++) {
+        WaveRun nxt = prepare_and_enqueue(k);
+        finish(cur);
+        cur = std::move(nxt);
     }
+    finish(cur);
     for (const auto &cc : comp) {
         stats_.padded += cc.ne != cc.n ? 1 : 0;
     }

@@ -125,6 +125,7 @@ template <class T> class BatchEngine {
 
     cudaStream_t s_{nullptr};
     cudaEvent_t ev0_{nullptr}, ev1_{nullptr};
+    cudaEvent_t wev0_[2]{}, wev1_[2]{}, ev_run0_{nullptr}; // per staging set; start of a run's device work
     int fixed_tile_bits_{0};
     size_t wave_bytes_{size_t{8} << 30};
     int threads_{0};
@@ -133,8 +134,9 @@ template <class T> class BatchEngine {
     // grow-only device / pinned host arenas
     void *d_states_{nullptr}, *d_prog_{nullptr}, *d_items_{nullptr}, *d_red_{nullptr};
     size_t c_states_{0}, c_prog_{0}, c_items_{0}, c_red_{0};
-    void *h_prog_{nullptr}, *h_items_{nullptr}, *h_out_{nullptr};
-    size_t ch_prog_{0}, ch_items_{0}, ch_out_{0};
+    // pinned staging, two sets: wave k packs into set k % 2
+    void *h_prog_[2]{}, *h_items_[2]{}, *h_out_[2]{};
+    size_t ch_prog_[2]{}, ch_items_[2]{}, ch_out_[2]{};
     BatchStats stats_;
 };
 

@@ -516,7 +516,10 @@ def reference_arm(args) -> None:
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_total * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64 arithmetic)", "data": "synthetic",
-        "config": {"workload": f"config1 cycle sample at {n_cpu} qubits (CPU)", "qubits": n_cpu},
+        "config": {"workload": f"config1: {args.qubits} qubits complex128, {args.cycles} cycles x ({args.qubits} "
+                               f"Haar SU(2) + {args.qubits // 2} CZ)", "qubits": args.qubits,
+                   "sample": f"first cycle at {n_cpu} qubits per step (the unfused-equivalent bytes of the "
+                             f"sampled gates over their time: the same metric)"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))

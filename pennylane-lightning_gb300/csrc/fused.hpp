@@ -20,6 +20,7 @@ enum TileKind : int {
 constexpr int kMaxReducePerPass = 64; // reduction slots accumulated per CTA and pass
 
 constexpr int kRegBits = 4;              // amplitudes per thread in register stages: 2^4
+constexpr int kAdjRegBits = 3;           // two-register adjoint passes: 2^3 of each register
 constexpr int kMaxOpsPerPass = 192;      // ops of a pass staged in shared memory per CTA
 constexpr int kMinRegTileBits = 9;       // register kernel needs >= 32 threads
 constexpr int kMaxDiagOpsPerPass = 48;   // merged diagonals evaluated per tile
@@ -67,6 +68,8 @@ template <class T> struct TileOp {
     int zero_outside{0};
     // register stages: target register bit, control predicates over the
     // register index and the thread index, slot of a merged diagonal
+    // (TK_REDUCE in a register stage: tcmask = the flip as a register-slot
+    // mask, tcval = merged diagonals before it in the pass)
     int rk{0};
     u32 rcmask{0}, rcval{0}, tcmask{0}, tcval{0};
     int diag_slot{0};
@@ -115,6 +118,15 @@ void launch_tile_pass_adj_df(cudaStream_t s, void *lam, void *hlam, int io, cons
                              const TileOp<df> *ops, const DiagForm<df> *forms, const cx<df> *tables, double *partials,
                              int G);
 void launch_adj_sum(cudaStream_t s, const double *partials, int nslots, int G, double *out);
+// the same on the register-blocked kernel, for passes with register stages
+// (kernels_adjoint_reg.cu)
+template <class T>
+void launch_tile_pass_reg_adj(cudaStream_t s, cx<T> *lam, cx<T> *hlam, const TilePassDesc &d, const TileOp<T> *ops,
+                              const DiagForm<T> *forms, const cx<T> *tables, const StageDesc *stages,
+                              double *partials, int G);
+void launch_tile_pass_reg_adj_df(cudaStream_t s, void *lam, void *hlam, int io, const TilePassDesc &d,
+                                 const TileOp<df> *ops, const DiagForm<df> *forms, const cx<df> *tables,
+                                 const StageDesc *stages, double *partials, int G);
 
 // A merged-diagonal table of 2^t entries described by its factors instead
 // of its values (batch engine: expanded on the device).  Entry j is the

@@ -365,27 +365,39 @@ std::vector<size_t> order_by_levels(const std::vector<size_t> &prims, const std:
 // when the pass needs the plain tile kernel.
 template <class T>
 bool plan_stages(std::vector<TileOp<T>> &ops, const std::vector<DiagForm<T>> &forms, TilePassDesc &d,
-                 std::vector<StageDesc> &stages) {
+                 std::vector<StageDesc> &stages, int rbits) {
     if (d.t < kMinRegTileBits || d.t > 12) { // 2^(t-4) <= 256 threads
         return false;
     }
     if (d.nops > kMaxOpsPerPass) {
         return false; // the register kernel stages at most kMaxOpsPerPass op records
     }
+    // Adjoint passes (with reductions) run on the two-register kernel
+    // (k_tile_reg_adj): a reduction sits in a register stage whose register
+    // bits hold its flip bit, so both amplitudes of every pair it sums are in
+    // the same thread; flips of two or more bits keep the pass on the
+    // shared-memory two-register kernel.
     for (int i = d.op_begin; i < d.op_begin + d.nops; i++) {
-        if (ops[static_cast<size_t>(i)].kind == TK_REDUCE) {
-            return false; // adjoint passes run on the two-register kernel
+        const auto &op = ops[static_cast<size_t>(i)];
+        if (op.kind == TK_REDUCE && __builtin_popcount(op.lo1) > 1) {
+            return false;
         }
     }
     const int begin = d.op_begin, end = d.op_begin + d.nops;
     auto single_target = [&](const TileOp<T> &op, int &q) {
+        if (op.kind == TK_REDUCE && op.lo1 != 0) {
+            q = __builtin_ctz(op.lo1);
+            return true;
+        }
         if ((op.kind != TK_PAIR && op.kind != TK_SROT) || op.lo0 != 0 || __builtin_popcount(op.lo1) != 1) {
             return false;
         }
         q = __builtin_ctz(op.lo1);
         return true;
     };
-    auto is_diag = [](const TileOp<T> &op) { return op.kind == TK_DIAGTAB || op.kind == TK_PARITY; };
+    auto is_diag = [](const TileOp<T> &op) {
+        return op.kind == TK_DIAGTAB || op.kind == TK_PARITY || (op.kind == TK_REDUCE && op.lo1 == 0);
+    };
     // limits of the register kernel's per-tile prologue
     int ndiag = 0;
     for (int i = begin; i < end; i++) {
@@ -414,7 +426,7 @@ bool plan_stages(std::vector<TileOp<T>> &ops, const std::vector<DiagForm<T>> &fo
     if (ndiag > kMaxDiagOpsPerPass) {
         return false;
     }
-    const int w = d.t - kRegBits;
+    const int w = d.t - rbits;
     auto layout_from = [&](int i0, int first_q) {
         StageDesc st{};
         st.kind = 0;
@@ -422,7 +434,7 @@ bool plan_stages(std::vector<TileOp<T>> &ops, const std::vector<DiagForm<T>> &fo
         if (first_q >= 0) {
             rb.push_back(first_q);
         }
-        for (int i = i0; i < end && static_cast<int>(rb.size()) < kRegBits; i++) {
+        for (int i = i0; i < end && static_cast<int>(rb.size()) < rbits; i++) {
             const auto &op = ops[static_cast<size_t>(i)];
             int q;
             if (single_target(op, q)) {
@@ -433,13 +445,13 @@ bool plan_stages(std::vector<TileOp<T>> &ops, const std::vector<DiagForm<T>> &fo
                 break;
             }
         }
-        for (int b = d.t - 1; b >= 0 && static_cast<int>(rb.size()) < kRegBits; b--) {
+        for (int b = d.t - 1; b >= 0 && static_cast<int>(rb.size()) < rbits; b--) {
             if (std::find(rb.begin(), rb.end(), b) == rb.end()) {
                 rb.push_back(b);
             }
         }
         for (int k = 0; k < kRegBits; k++) {
-            st.rb[k] = rb[static_cast<size_t>(k)];
+            st.rb[k] = k < rbits ? rb[static_cast<size_t>(k)] : d.t; // unused slots: never selected
         }
         int m = 0;
         for (int b = 0; b < d.t; b++) {
@@ -465,10 +477,14 @@ bool plan_stages(std::vector<TileOp<T>> &ops, const std::vector<DiagForm<T>> &fo
             if (op.kind == TK_DIAGTAB) {
                 op.diag_slot = slot++;
             }
+            if (op.kind == TK_REDUCE) {
+                op.tcmask = 0;     // no flip
+                op.tcval = slot;   // merged diagonals before it in the pass
+            }
         } else if (single_target(op, q)) {
             bool in = false;
             if (cur >= 0 && local[static_cast<size_t>(cur)].kind == 0) {
-                for (int k = 0; k < kRegBits; k++) {
+                for (int k = 0; k < rbits; k++) {
                     in = in || local[static_cast<size_t>(cur)].rb[k] == q;
                 }
             }
@@ -478,10 +494,18 @@ bool plan_stages(std::vector<TileOp<T>> &ops, const std::vector<DiagForm<T>> &fo
                 cur = static_cast<int>(local.size()) - 1;
             }
             const auto &st = local[static_cast<size_t>(cur)];
-            for (int k = 0; k < kRegBits; k++) {
+            for (int k = 0; k < rbits; k++) {
                 if (st.rb[k] == q) {
                     op.rk = k;
                 }
+            }
+            if (op.kind == TK_REDUCE) {
+                // the flip as a register-slot mask; rcmask / lcval stay the
+                // local projector
+                op.tcmask = 1u << op.rk;
+                op.tcval = slot;
+                local[static_cast<size_t>(cur)].nops = i - local[static_cast<size_t>(cur)].op_begin + 1;
+                continue;
             }
             // controls: every local insert bit except the target
             op.rcmask = 0;
@@ -1088,7 +1112,13 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
         }
         flush();
         d.nops = static_cast<int>(ops.size()) - d.op_begin;
-        seg.reg = plan_stages<T>(ops, forms, d, stages);
+        // passes with reductions (adjoint sweeps) run two registers per
+        // thread: 8 amplitudes of each (3 register bits) instead of 16
+        bool has_reduce = false;
+        for (int i = d.op_begin; i < d.op_begin + d.nops; i++) {
+            has_reduce = has_reduce || ops[static_cast<size_t>(i)].kind == TK_REDUCE;
+        }
+        seg.reg = plan_stages<T>(ops, forms, d, stages, has_reduce ? kAdjRegBits : kRegBits);
         prog->segs.push_back(std::move(seg));
         prog->passes++;
     }
@@ -1257,16 +1287,27 @@ void run_fused_adjoint(StateVector<T> &lam, StateVector<T> &hlam, const FusedPro
             const size_t np = prog.segs.size();
             for (size_t k = 0; k < np; k++) {
                 const int io = np == 1 ? 0 : k == 0 ? 1 : k + 1 == np ? 3 : 2;
-                launch_tile_pass_adj_df(lam.stream(), lam.data(), hlam.data(), io, prog.segs[k].desc,
-                                        static_cast<const TileOp<df> *>(prog.d_ops_df),
-                                        static_cast<const DiagForm<df> *>(prog.d_forms_df),
-                                        static_cast<const cx<df> *>(prog.d_tables_df), partials, G);
+                if (prog.segs[k].reg) {
+                    launch_tile_pass_reg_adj_df(lam.stream(), lam.data(), hlam.data(), io, prog.segs[k].desc,
+                                                static_cast<const TileOp<df> *>(prog.d_ops_df),
+                                                static_cast<const DiagForm<df> *>(prog.d_forms_df),
+                                                static_cast<const cx<df> *>(prog.d_tables_df), prog.d_stages,
+                                                partials, G);
+                } else {
+                    launch_tile_pass_adj_df(lam.stream(), lam.data(), hlam.data(), io, prog.segs[k].desc,
+                                            static_cast<const TileOp<df> *>(prog.d_ops_df),
+                                            static_cast<const DiagForm<df> *>(prog.d_forms_df),
+                                            static_cast<const cx<df> *>(prog.d_tables_df), partials, G);
+                }
             }
             return;
         }
     }
     for (const auto &seg : prog.segs) {
-        if (seg.tile) {
+        if (seg.tile && seg.reg) {
+            launch_tile_pass_reg_adj<T>(lam.stream(), lam.data(), hlam.data(), seg.desc, prog.d_ops, prog.d_forms,
+                                        prog.d_tables, prog.d_stages, partials, G);
+        } else if (seg.tile) {
             launch_tile_pass_adj<T>(lam.stream(), lam.data(), hlam.data(), seg.desc, prog.d_ops, prog.d_forms,
                                     prog.d_tables, partials, G);
         } else {

@@ -23,8 +23,6 @@ namespace plgb {
 
 namespace {
 
-constexpr int RB = kRegBits;
-constexpr int NR = 1 << RB;
 
 template <class T> __device__ __forceinline__ u32 swz(u32 j) {
     if constexpr (sizeof(T) == 8) { // 16-byte amplitudes: 8 per 128-byte row
@@ -128,30 +126,58 @@ template <class T> struct SlotAddr {
         return base ^ ((i & 1) ? s0 : 0u) ^ ((i & 2) ? s1 : 0u) ^ ((i & 4) ? s2 : 0u) ^ ((i & 8) ? s3 : 0u);
     }
 };
-template <class T> __device__ __forceinline__ void to_smem(cx<T> *tile, const cx<T> (&v)[NR], const Layout &l) {
+template <class T, int N> __device__ __forceinline__ void to_smem(cx<T> *tile, const cx<T> (&v)[N], const Layout &l) {
     const SlotAddr<T> ad(l);
 #pragma unroll
-    for (int i = 0; i < NR; i++) {
+    for (int i = 0; i < N; i++) {
         tile[ad(i)] = v[i];
     }
 }
-template <class T> __device__ __forceinline__ void from_smem(const cx<T> *tile, cx<T> (&v)[NR], const Layout &l) {
+template <class T, int N> __device__ __forceinline__ void from_smem(const cx<T> *tile, cx<T> (&v)[N], const Layout &l) {
     const SlotAddr<T> ad(l);
 #pragma unroll
-    for (int i = 0; i < NR; i++) {
+    for (int i = 0; i < N; i++) {
         v[i] = tile[ad(i)];
     }
 }
 
-// One-target op on register bit K for the eight pairs of a thread, one
+// One-target op on register bit K for the pairs of a thread, one
 // specialisation per op shape so the unrolled body has no mode branches.
-template <int MODE, bool CTRL, class T, int K, class OP>
-__device__ __forceinline__ void reg_op_k(cx<T> (&v)[NR], const OP &op, const Layout &l) {
+// TWO: the same op on a second register array v2 (adjoint sweeps), sharing
+// the coefficients and the control tests.
+template <int MODE, bool CTRL, class T, int K, bool TWO, class OP, int N>
+__device__ __forceinline__ void reg_op_k(cx<T> (&v)[N], cx<T> (&v2)[N], const OP &op, const Layout &l) {
+    if constexpr ((1 << K) >= N) {
+        return; // no such register bit at this register count
+    }
     const u32 cm = op.rcmask, cv = op.rcval;
     const T ca = op.m[0].x, cb = op.m[0].y;
     const cx<T> m0 = op.m[0], m1 = op.m[1], m2 = op.m[2], m3 = op.m[3];
+    auto pair = [&](cx<T> &x0, cx<T> &x1) {
+        const cx<T> v0 = x0, v1 = x1;
+        if constexpr (std::is_same_v<T, df> && MODE == RM_SROT_A) {
+            const df nb = -cb;
+            x0 = cx<T>{df_fma(v0.x, nb, v1.x), df_fma(v0.y, nb, v1.y)};
+            x1 = cx<T>{df_fma(v1.x, cb, v0.x), df_fma(v1.y, cb, v0.y)};
+        } else if constexpr (std::is_same_v<T, df> && MODE == RM_SROT_B) {
+            x0 = cx<T>{df_fma(-v1.x, ca, v0.x), df_fma(-v1.y, ca, v0.y)};
+            x1 = cx<T>{df_fma(v0.x, ca, v1.x), df_fma(v0.y, ca, v1.y)};
+        } else if constexpr (MODE == RM_SROT_A) { // [[1, -b], [b, 1]]
+            x0 = cx<T>{v0.x - cb * v1.x, v0.y - cb * v1.y};
+            x1 = cx<T>{cb * v0.x + v1.x, cb * v0.y + v1.y};
+        } else if constexpr (MODE == RM_SROT_B) { // [[a, -1], [1, a]]
+            x0 = cx<T>{ca * v0.x - v1.x, ca * v0.y - v1.y};
+            x1 = cx<T>{v0.x + ca * v1.x, v0.y + ca * v1.y};
+        } else if constexpr (MODE == RM_SWAP) {
+            x0 = v1;
+            x1 = v0;
+        } else { // general complex 2x2
+            x0 = cfma(m1, v1, m0 * v0);
+            x1 = cfma(m3, v1, m2 * v0);
+        }
+    };
 #pragma unroll
-    for (int i = 0; i < NR; i++) {
+    for (int i = 0; i < N; i++) {
         if (i & (1 << K)) {
             continue;
         }
@@ -159,52 +185,36 @@ __device__ __forceinline__ void reg_op_k(cx<T> (&v)[NR], const OP &op, const Lay
         if (CTRL && ((l.at(i) & cm) != cv)) {
             continue;
         }
-        const cx<T> v0 = v[i], v1 = v[i1];
-        if constexpr (std::is_same_v<T, df> && MODE == RM_SROT_A) {
-            const df nb = -cb;
-            v[i] = cx<T>{df_fma(v0.x, nb, v1.x), df_fma(v0.y, nb, v1.y)};
-            v[i1] = cx<T>{df_fma(v1.x, cb, v0.x), df_fma(v1.y, cb, v0.y)};
-        } else if constexpr (std::is_same_v<T, df> && MODE == RM_SROT_B) {
-            v[i] = cx<T>{df_fma(-v1.x, ca, v0.x), df_fma(-v1.y, ca, v0.y)};
-            v[i1] = cx<T>{df_fma(v0.x, ca, v1.x), df_fma(v0.y, ca, v1.y)};
-        } else if constexpr (MODE == RM_SROT_A) { // [[1, -b], [b, 1]]
-            v[i] = cx<T>{v0.x - cb * v1.x, v0.y - cb * v1.y};
-            v[i1] = cx<T>{cb * v0.x + v1.x, cb * v0.y + v1.y};
-        } else if constexpr (MODE == RM_SROT_B) { // [[a, -1], [1, a]]
-            v[i] = cx<T>{ca * v0.x - v1.x, ca * v0.y - v1.y};
-            v[i1] = cx<T>{v0.x + ca * v1.x, v0.y + ca * v1.y};
-        } else if constexpr (MODE == RM_SWAP) {
-            v[i] = v1;
-            v[i1] = v0;
-        } else { // general complex 2x2
-            v[i] = cfma(m1, v1, m0 * v0);
-            v[i1] = cfma(m3, v1, m2 * v0);
+        pair(v[i], v[i1]);
+        if constexpr (TWO) {
+            pair(v2[i], v2[i1]);
         }
     }
 }
-template <int MODE, bool CTRL, class T, class OP>
-__device__ __forceinline__ void reg_op_m(cx<T> (&v)[NR], const OP &op, const Layout &l) {
+template <int MODE, bool CTRL, bool TWO, class T, class OP, int N>
+__device__ __forceinline__ void reg_op_m(cx<T> (&v)[N], cx<T> (&v2)[N], const OP &op, const Layout &l) {
     switch (op.rk) {
-    case 0: reg_op_k<MODE, CTRL, T, 0>(v, op, l); break;
-    case 1: reg_op_k<MODE, CTRL, T, 1>(v, op, l); break;
-    case 2: reg_op_k<MODE, CTRL, T, 2>(v, op, l); break;
-    default: reg_op_k<MODE, CTRL, T, 3>(v, op, l); break;
+    case 0: reg_op_k<MODE, CTRL, T, 0, TWO>(v, v2, op, l); break;
+    case 1: reg_op_k<MODE, CTRL, T, 1, TWO>(v, v2, op, l); break;
+    case 2: reg_op_k<MODE, CTRL, T, 2, TWO>(v, v2, op, l); break;
+    default: reg_op_k<MODE, CTRL, T, 3, TWO>(v, v2, op, l); break;
     }
 }
-template <class T, class OP> __device__ __forceinline__ void reg_op(cx<T> (&v)[NR], const OP &op, const Layout &l) {
+template <bool TWO, class T, class OP, int N>
+__device__ __forceinline__ void reg_op(cx<T> (&v)[N], cx<T> (&v2)[N], const OP &op, const Layout &l) {
     if (op.rcmask == 0) {
         switch (op.mode) {
-        case RM_SROT_A: reg_op_m<RM_SROT_A, false>(v, op, l); break;
-        case RM_SROT_B: reg_op_m<RM_SROT_B, false>(v, op, l); break;
-        case RM_SWAP: reg_op_m<RM_SWAP, false>(v, op, l); break;
-        default: reg_op_m<RM_DENSE, false>(v, op, l); break;
+        case RM_SROT_A: reg_op_m<RM_SROT_A, false, TWO>(v, v2, op, l); break;
+        case RM_SROT_B: reg_op_m<RM_SROT_B, false, TWO>(v, v2, op, l); break;
+        case RM_SWAP: reg_op_m<RM_SWAP, false, TWO>(v, v2, op, l); break;
+        default: reg_op_m<RM_DENSE, false, TWO>(v, v2, op, l); break;
         }
     } else {
         switch (op.mode) {
-        case RM_SROT_A: reg_op_m<RM_SROT_A, true>(v, op, l); break;
-        case RM_SROT_B: reg_op_m<RM_SROT_B, true>(v, op, l); break;
-        case RM_SWAP: reg_op_m<RM_SWAP, true>(v, op, l); break;
-        default: reg_op_m<RM_DENSE, true>(v, op, l); break;
+        case RM_SROT_A: reg_op_m<RM_SROT_A, true, TWO>(v, v2, op, l); break;
+        case RM_SROT_B: reg_op_m<RM_SROT_B, true, TWO>(v, v2, op, l); break;
+        case RM_SWAP: reg_op_m<RM_SWAP, true, TWO>(v, v2, op, l); break;
+        default: reg_op_m<RM_DENSE, true, TWO>(v, v2, op, l); break;
         }
     }
 }
@@ -286,22 +296,83 @@ __device__ __forceinline__ const PassOpRec<T, STAGE> *op_records(unsigned char *
     }
 }
 
-template <class T, class SI = T, class SO = T, class REC>
+// Adjoint reduction in a register stage (two-register kernel): this
+// thread's share of  sum_j [(j & P) == pv] Re or Im( conj(b_j) a_k ) with
+// k = j ^ flip, signed by the parity of (k & yz) and of the tile's global
+// Y|Z bits.  XR = the flip as a register-slot mask (compile time, so both
+// slots stay in registers).  Products and the running sum in double-float
+// (complex64 / double-float registers) or FP64 (complex128 in FP64).
+template <class T, int XR, int N>
+__device__ __forceinline__ double reduce_slots(const cx<T> (&a)[N], const cx<T> (&b)[N], const Layout &l,
+                                               u32 pm, u32 pv, u32 yz, unsigned gpar, bool want_re) {
+    if constexpr (XR >= N) {
+        return 0.0; // no such register bit at this register count
+    }
+    if constexpr (std::is_same_v<T, double>) {
+        double acc = 0.0;
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            if ((l.at(i) & pm) != pv) {
+                continue;
+            }
+            const cx<double> p = b[i], q = a[i ^ XR];
+            double z = want_re ? fma(p.y, q.y, p.x * q.x) : fma(-p.y, q.x, p.x * q.y);
+            if ((static_cast<unsigned>(__popc(l.at(i ^ XR) & yz)) ^ gpar) & 1u) {
+                z = -z;
+            }
+            acc += z;
+        }
+        return acc;
+    } else {
+        df acc{0.f, 0.f};
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            if ((l.at(i) & pm) != pv) {
+                continue;
+            }
+            df px, py, qx, qy;
+            if constexpr (std::is_same_v<T, df>) {
+                px = b[i].x, py = b[i].y, qx = a[i ^ XR].x, qy = a[i ^ XR].y;
+            } else {
+                px = df(b[i].x), py = df(b[i].y), qx = df(a[i ^ XR].x), qy = df(a[i ^ XR].y);
+            }
+            df z = want_re ? df_fma(px * qx, py, qy) : df_fma(px * qy, -py, qx);
+            if ((static_cast<unsigned>(__popc(l.at(i ^ XR) & yz)) ^ gpar) & 1u) {
+                z = -z;
+            }
+            acc = acc + z;
+        }
+        return df_to_double(acc);
+    }
+}
+
+// Apply pass d to tile g.  DUAL (adjoint sweep): the same ops to a second
+// register b (its tile at tileb), and the pass's reductions (TK_REDUCE, in
+// register stages) accumulated per warp into s_part[slot * nwarps + warp];
+// s_f2[k] = |product of the first k merged diagonals' tile scalars|^2, the
+// deferred factor a reduction after k of them must include.
+template <class T, class SI = T, class SO = T, bool DUAL = false, int RBT = kRegBits, class REC>
 __device__ __forceinline__ void tile_reg_run(const cx<SI> *ain, cx<SO> *aout, const TilePassDesc &d,
                                              const TileOp<T> *__restrict__ ops, const DiagForm<T> *__restrict__ forms,
                                              const cx<T> *__restrict__ tables, const StageDesc *__restrict__ stages,
-                                             u64 g, cx<T> *tile, TileShared<T> &sh, const REC *recs) {
-    const int w = d.t - RB;
+                                             u64 g, cx<T> *tile, TileShared<T> &sh, const REC *recs,
+                                             const cx<SI> *bin = nullptr, cx<SO> *bout = nullptr,
+                                             cx<T> *tileb = nullptr, double *s_part = nullptr,
+                                             double *s_f2 = nullptr) {
+    constexpr int NRT = 1 << RBT; // amplitudes per thread and register
+    const int w = d.t - RBT;
     const u32 tid = threadIdx.x;
     const int lane = static_cast<int>(tid & 31u);
     const int warp = static_cast<int>(tid >> 5);
     const int nwarps = static_cast<int>(blockDim.x >> 5);
-    cx<T> v[NR];
+    cx<T> v[NRT];
+    cx<T> vb[DUAL ? NRT : 1];
     // global offset of canonical slot i of this thread: the local->global map
     // is a bit deposit, so it splits into a thread part and a slot part
     const u64 off_t = local_offset_r(tid, d);
     // canonical slot bits are local bits w..w+3 = global bits hb[w-L .. w-L+3]
-    const int g0 = d.hb[w - d.L], g1 = d.hb[w - d.L + 1], g2 = d.hb[w - d.L + 2], g3 = d.hb[w - d.L + 3];
+    const int g0 = d.hb[w - d.L], g1 = d.hb[w - d.L + 1], g2 = d.hb[w - d.L + 2];
+    const int g3 = RBT > 3 ? d.hb[w - d.L + 3] : 0;
     auto off_r = [&](int i) -> u64 {
         return ((i & 1) ? (u64{1} << g0) : 0) | ((i & 2) ? (u64{1} << g1) : 0) | ((i & 4) ? (u64{1} << g2) : 0) |
                ((i & 8) ? (u64{1} << g3) : 0);
@@ -315,8 +386,14 @@ __device__ __forceinline__ void tile_reg_run(const cx<SI> *ain, cx<SO> *aout, co
     }
     const u64 tbase = gbase | off_t;
 #pragma unroll
-    for (int i = 0; i < NR; i++) {
+    for (int i = 0; i < NRT; i++) {
         v[i] = ld_conv<T, SI>(ld_stream(&ain[tbase | off_r(i)]));
+    }
+    if constexpr (DUAL) {
+#pragma unroll
+        for (int i = 0; i < NRT; i++) {
+            vb[i] = ld_conv<T, SI>(ld_stream(&bin[tbase | off_r(i)]));
+        }
     }
     // prologue: tile-uniform parts of every merged diagonal, one warp per op
     int slot = 0;
@@ -380,6 +457,15 @@ __device__ __forceinline__ void tile_reg_run(const cx<SI> *ain, cx<SO> *aout, co
             f = f * sh.scal[s];
         }
         sh.factor = f;
+        if constexpr (DUAL) {
+            double f2 = 1.0;
+            s_f2[0] = f2;
+            for (int s = 0; s < d.ndiag; s++) {
+                const double x = static_cast<double>(sh.scal[s].x), y = static_cast<double>(sh.scal[s].y);
+                f2 *= x * x + y * y;
+                s_f2[s + 1] = f2;
+            }
+        }
     }
 
     Layout cur = canon;
@@ -391,8 +477,14 @@ __device__ __forceinline__ void tile_reg_run(const cx<SI> *ain, cx<SO> *aout, co
             if (cur_stage != si) {
                 const Layout nl = stage_layout(st, tid, w);
                 to_smem(tile, v, cur);
+                if constexpr (DUAL) {
+                    to_smem(tileb, vb, cur);
+                }
                 __syncthreads();
                 from_smem(tile, v, nl);
+                if constexpr (DUAL) {
+                    from_smem(tileb, vb, nl);
+                }
                 __syncthreads();
                 cur = nl;
                 cur_canon = false;
@@ -410,94 +502,156 @@ __device__ __forceinline__ void tile_reg_run(const cx<SI> *ain, cx<SO> *aout, co
                     const cx<T> *tab = tables + op.table_off;
                     if (op.has_table && zl == 0) {
 #pragma unroll
-                        for (int i = 0; i < NR; i++) {
-                            v[i] = tab[cur.at(i)] * v[i];
+                        for (int i = 0; i < NRT; i++) {
+                            const cx<T> tv = tab[cur.at(i)];
+                            v[i] = tv * v[i];
+                            if constexpr (DUAL) {
+                                vb[i] = tv * vb[i];
+                            }
                         }
                     } else if (op.has_table) {
 #pragma unroll
-                        for (int i = 0; i < NR; i++) {
+                        for (int i = 0; i < NRT; i++) {
                             const u32 j = cur.at(i);
-                            v[i] = cflip(tab[j] * v[i], static_cast<unsigned>(__popc(j & zl) & 1));
+                            const cx<T> tv = tab[j];
+                            const unsigned fl = static_cast<unsigned>(__popc(j & zl) & 1);
+                            v[i] = cflip(tv * v[i], fl);
+                            if constexpr (DUAL) {
+                                vb[i] = cflip(tv * vb[i], fl);
+                            }
                         }
                     } else if (zl) {
 #pragma unroll
-                        for (int i = 0; i < NR; i++) {
-                            v[i] = cflip(v[i], static_cast<unsigned>(__popc(cur.at(i) & zl) & 1));
+                        for (int i = 0; i < NRT; i++) {
+                            const unsigned fl = static_cast<unsigned>(__popc(cur.at(i) & zl) & 1);
+                            v[i] = cflip(v[i], fl);
+                            if constexpr (DUAL) {
+                                vb[i] = cflip(vb[i], fl);
+                            }
                         }
                     }
                     for (int f = 0; f < ngen; f++) {
                         const int gb = sh.gbit[s][f];
                         const cx<T> g0 = sh.gd0[s][f], g1 = sh.gd1[s][f];
 #pragma unroll
-                        for (int i = 0; i < NR; i++) {
-                            v[i] = (((cur.at(i) >> gb) & 1u) ? g1 : g0) * v[i];
+                        for (int i = 0; i < NRT; i++) {
+                            const cx<T> gv = ((cur.at(i) >> gb) & 1u) ? g1 : g0;
+                            v[i] = gv * v[i];
+                            if constexpr (DUAL) {
+                                vb[i] = gv * vb[i];
+                            }
                         }
                     }
                 } else if (op.kind == TK_PARITY) {
                     const TileOp<T> &po = ops[oi];
 #pragma unroll
-                    for (int i = 0; i < NR; i++) {
+                    for (int i = 0; i < NRT; i++) {
                         const u64 idx = gbase | local_offset_r(cur.at(i), d);
                         if ((idx & po.cmask) != po.cval) {
                             if (po.zero_outside) {
                                 v[i] = cx<T>{0, 0};
+                                if constexpr (DUAL) {
+                                    vb[i] = cx<T>{0, 0};
+                                }
                             }
                             continue;
                         }
-                        v[i] = ((__popcll(idx & po.pmask) & 1) ? op.m[1] : op.m[0]) * v[i];
+                        const cx<T> pv = (__popcll(idx & po.pmask) & 1) ? op.m[1] : op.m[0];
+                        v[i] = pv * v[i];
+                        if constexpr (DUAL) {
+                            vb[i] = pv * vb[i];
+                        }
                     }
+                } else if (DUAL && op.kind == TK_REDUCE) {
+                    if constexpr (DUAL) {
+                        const TileOp<T> &ro = ops[oi];
+                        const unsigned gpar = static_cast<unsigned>(__popcll(gbase & ro.pmask) & 1);
+                        const bool want_re = (ro.mode & 1) != 0;
+                        double z;
+                        switch (ro.tcmask) {
+                        case 0: z = reduce_slots<T, 0>(v, vb, cur, ro.rcmask, ro.lcval, ro.lo0, gpar, want_re); break;
+                        case 1: z = reduce_slots<T, 1>(v, vb, cur, ro.rcmask, ro.lcval, ro.lo0, gpar, want_re); break;
+                        case 2: z = reduce_slots<T, 2>(v, vb, cur, ro.rcmask, ro.lcval, ro.lo0, gpar, want_re); break;
+                        case 4: z = reduce_slots<T, 4>(v, vb, cur, ro.rcmask, ro.lcval, ro.lo0, gpar, want_re); break;
+                        default: z = reduce_slots<T, 8>(v, vb, cur, ro.rcmask, ro.lcval, ro.lo0, gpar, want_re); break;
+                        }
+                        if (ro.mode & 2) {
+                            z = -z;
+                        }
+#pragma unroll
+                        for (int m = 16; m > 0; m >>= 1) {
+                            z += __shfl_xor_sync(0xffffffffu, z, m);
+                        }
+                        if (lane == 0) {
+                            s_part[ro.diag_slot * nwarps + warp] += z * ro.rmul * s_f2[ro.tcval];
+                        }
+                    }
+                } else if constexpr (DUAL) {
+                    reg_op<true>(v, vb, op, cur);
                 } else {
-                    reg_op(v, op, cur);
+                    reg_op<false>(v, v, op, cur);
                 }
             }
         } else {
-            // shared-memory stage: two-target ops on the staged tile
+            // shared-memory stage: two-target ops on the staged tile(s)
             to_smem(tile, v, cur);
+            if constexpr (DUAL) {
+                to_smem(tileb, vb, cur);
+            }
             __syncthreads();
             const u32 T_ = 1u << d.t;
+            auto smem_op = [&](cx<T> *tl, const TileOp<T> &op) {
+                if (op.kind == TK_DENSE2) {
+                    const u32 nq = T_ >> op.nlins;
+                    for (u32 p = tid; p < nq; p += blockDim.x) {
+                        const u32 j0 = insert_zeros_r(p, op.lins, op.nlins) | op.lcval;
+                        const u32 ix[4] = {swz<T>(j0), swz<T>(j0 | op.lo1), swz<T>(j0 | op.lo0),
+                                           swz<T>(j0 | op.lo0 | op.lo1)};
+                        cx<T> x[4];
+#pragma unroll
+                        for (int r = 0; r < 4; r++) {
+                            x[r] = tl[ix[r]];
+                        }
+#pragma unroll
+                        for (int r = 0; r < 4; r++) {
+                            cx<T> acc = op.m[4 * r] * x[0];
+                            acc = cfma(op.m[4 * r + 1], x[1], acc);
+                            acc = cfma(op.m[4 * r + 2], x[2], acc);
+                            acc = cfma(op.m[4 * r + 3], x[3], acc);
+                            tl[ix[r]] = acc;
+                        }
+                    }
+                } else { // two-amplitude op with general offsets
+                    const u32 np = T_ >> op.nlins;
+                    for (u32 p = tid; p < np; p += blockDim.x) {
+                        const u32 j0 = insert_zeros_r(p, op.lins, op.nlins) | op.lcval;
+                        cx<T> &x0 = tl[swz<T>(j0 | op.lo0)];
+                        cx<T> &x1 = tl[swz<T>(j0 | op.lo1)];
+                        const cx<T> v0 = x0, v1 = x1;
+                        if (op.mode == RM_SWAP) {
+                            x0 = v1;
+                            x1 = v0;
+                        } else {
+                            x0 = cfma(op.m[1], v1, op.m[0] * v0);
+                            x1 = cfma(op.m[3], v1, op.m[2] * v0);
+                        }
+                    }
+                }
+            };
             for (int oi = st->op_begin; oi < st->op_begin + st->nops; oi++) {
                 const TileOp<T> &op = ops[oi];
                 if ((gbase & op.gcmask) == op.gcval) {
-                    if (op.kind == TK_DENSE2) {
-                        const u32 nq = T_ >> op.nlins;
-                        for (u32 p = tid; p < nq; p += blockDim.x) {
-                            const u32 j0 = insert_zeros_r(p, op.lins, op.nlins) | op.lcval;
-                            const u32 ix[4] = {swz<T>(j0), swz<T>(j0 | op.lo1), swz<T>(j0 | op.lo0),
-                                               swz<T>(j0 | op.lo0 | op.lo1)};
-                            cx<T> x[4];
-#pragma unroll
-                            for (int r = 0; r < 4; r++) {
-                                x[r] = tile[ix[r]];
-                            }
-#pragma unroll
-                            for (int r = 0; r < 4; r++) {
-                                cx<T> acc = op.m[4 * r] * x[0];
-                                acc = cfma(op.m[4 * r + 1], x[1], acc);
-                                acc = cfma(op.m[4 * r + 2], x[2], acc);
-                                acc = cfma(op.m[4 * r + 3], x[3], acc);
-                                tile[ix[r]] = acc;
-                            }
-                        }
-                    } else { // two-amplitude op with general offsets
-                        const u32 np = T_ >> op.nlins;
-                        for (u32 p = tid; p < np; p += blockDim.x) {
-                            const u32 j0 = insert_zeros_r(p, op.lins, op.nlins) | op.lcval;
-                            cx<T> &x0 = tile[swz<T>(j0 | op.lo0)];
-                            cx<T> &x1 = tile[swz<T>(j0 | op.lo1)];
-                            const cx<T> v0 = x0, v1 = x1;
-                            if (op.mode == RM_SWAP) {
-                                x0 = v1;
-                                x1 = v0;
-                            } else {
-                                x0 = cfma(op.m[1], v1, op.m[0] * v0);
-                                x1 = cfma(op.m[3], v1, op.m[2] * v0);
-                            }
-                        }
+                    smem_op(tile, op);
+                    if constexpr (DUAL) {
+                        smem_op(tileb, op);
                     }
                 }
                 __syncthreads();
             }
             from_smem(tile, v, canon);
+            if constexpr (DUAL) {
+                from_smem(tileb, vb, canon);
+            }
             __syncthreads();
             cur = canon;
             cur_canon = true;
@@ -506,14 +660,26 @@ __device__ __forceinline__ void tile_reg_run(const cx<SI> *ain, cx<SO> *aout, co
     }
     if (!cur_canon) {
         to_smem(tile, v, cur);
+        if constexpr (DUAL) {
+            to_smem(tileb, vb, cur);
+        }
         __syncthreads();
         from_smem(tile, v, canon);
+        if constexpr (DUAL) {
+            from_smem(tileb, vb, canon);
+        }
     }
     __syncthreads();
     const cx<T> f = sh.factor;
 #pragma unroll
-    for (int i = 0; i < NR; i++) {
+    for (int i = 0; i < NRT; i++) {
         st_stream(&aout[tbase | off_r(i)], st_conv<SO, T>(f * v[i]));
+    }
+    if constexpr (DUAL) {
+#pragma unroll
+        for (int i = 0; i < NRT; i++) {
+            st_stream(&bout[tbase | off_r(i)], st_conv<SO, T>(f * vb[i]));
+        }
     }
     __syncthreads();
 }

@@ -182,6 +182,20 @@ __device__ __forceinline__ void reg_op_k(cx<T> (&v)[N], cx<T> (&v2)[N], const OP
             continue;
         }
         const int i1 = i | (1 << K);
+        if constexpr (CTRL && MODE == RM_SWAP) {
+            // controlled swap (CNOT, CSWAP): selects instead of a branch per pair
+            const bool on = (l.at(i) & cm) == cv;
+            auto cswap = [&](cx<T> &x0, cx<T> &x1) {
+                const cx<T> v0 = x0, v1 = x1;
+                x0 = on ? v1 : v0;
+                x1 = on ? v0 : v1;
+            };
+            cswap(v[i], v[i1]);
+            if constexpr (TWO) {
+                cswap(v2[i], v2[i1]);
+            }
+            continue;
+        }
         if (CTRL && ((l.at(i) & cm) != cv)) {
             continue;
         }
@@ -312,24 +326,16 @@ __device__ __forceinline__ double reduce_slots(const cx<T> (&a)[N], const cx<T> 
         double acc = 0.0;
 #pragma unroll
         for (int i = 0; i < N; i++) {
-            if ((l.at(i) & pm) != pv) {
-                continue;
-            }
             const cx<double> p = b[i], q = a[i ^ XR];
             double z = want_re ? fma(p.y, q.y, p.x * q.x) : fma(-p.y, q.x, p.x * q.y);
-            if ((static_cast<unsigned>(__popc(l.at(i ^ XR) & yz)) ^ gpar) & 1u) {
-                z = -z;
-            }
-            acc += z;
+            z = sflip(z, (static_cast<unsigned>(__popc(l.at(i ^ XR) & yz)) ^ gpar) & 1u);
+            acc += ((l.at(i) & pm) == pv) ? z : 0.0;
         }
         return acc;
     } else {
         df acc{0.f, 0.f};
 #pragma unroll
         for (int i = 0; i < N; i++) {
-            if ((l.at(i) & pm) != pv) {
-                continue;
-            }
             df px, py, qx, qy;
             if constexpr (std::is_same_v<T, df>) {
                 px = b[i].x, py = b[i].y, qx = a[i ^ XR].x, qy = a[i ^ XR].y;
@@ -337,8 +343,9 @@ __device__ __forceinline__ double reduce_slots(const cx<T> (&a)[N], const cx<T> 
                 px = df(b[i].x), py = df(b[i].y), qx = df(a[i ^ XR].x), qy = df(a[i ^ XR].y);
             }
             df z = want_re ? df_fma(px * qx, py, qy) : df_fma(px * qy, -py, qx);
-            if ((static_cast<unsigned>(__popc(l.at(i ^ XR) & yz)) ^ gpar) & 1u) {
-                z = -z;
+            z = sflip(z, (static_cast<unsigned>(__popc(l.at(i ^ XR) & yz)) ^ gpar) & 1u);
+            if ((l.at(i) & pm) != pv) { // outside the projector: adds zero
+                z = df{0.f, 0.f};
             }
             acc = acc + z;
         }

@@ -176,6 +176,62 @@ std::vector<PauliGroup> group_pauli(const PauliSum &ps) {
     return groups;
 }
 
+// Every flip-mask group of a Pauli sum applied in one sweep per chunk of at
+// most kApplyMaxGroups groups / kApplyMaxTerms terms (launch_pauli_apply):
+// dst = sum_t c_t P_t psi.  Coefficients are split into double-float pairs
+// here.
+template <class T>
+void pauli_sum_into(const cx<T> *psi, StateVector<T> &dst, const std::vector<PauliGroup> &groups) {
+    struct Chunk {
+        size_t g0, g1, t0, t1;
+    };
+    std::vector<PauliGroupHdr> hdr;
+    std::vector<PauliTermDF> terms;
+    std::vector<Chunk> chunks;
+    Chunk cur{0, 0, 0, 0};
+    for (size_t g = 0; g < groups.size(); g++) {
+        const auto &G = groups[g];
+        const size_t nt = static_cast<size_t>(G.nterms);
+        if (cur.g1 > cur.g0 && (cur.g1 - cur.g0 == static_cast<size_t>(kApplyMaxGroups) ||
+                                terms.size() + nt - cur.t0 > static_cast<size_t>(kApplyMaxTerms))) {
+            chunks.push_back(cur);
+            cur = Chunk{g, g, terms.size(), terms.size()};
+        }
+        PauliGroupHdr h{};
+        h.x = G.x;
+        h.tbegin = static_cast<int>(terms.size() - cur.t0);
+        for (size_t t = 0; t < nt; t++) {
+            PauliTermDF tm{};
+            tm.yz = G.t[t].yz;
+            tm.chi = static_cast<float>(G.t[t].coeff);
+            tm.clo = static_cast<float>(G.t[t].coeff - static_cast<double>(tm.chi));
+            tm.ny4 = G.t[t].ny4;
+            terms.push_back(tm);
+        }
+        h.tend = static_cast<int>(terms.size() - cur.t0);
+        hdr.push_back(h);
+        cur.g1 = g + 1;
+        cur.t1 = terms.size();
+    }
+    if (cur.g1 > cur.g0) {
+        chunks.push_back(cur);
+    }
+    PLGB_REQUIRE(!chunks.empty(), "Pauli sum without terms");
+    auto bufs = dst.scratch().carve({hdr.size() * sizeof(PauliGroupHdr), terms.size() * sizeof(PauliTermDF)});
+    auto *d_hdr = reinterpret_cast<PauliGroupHdr *>(bufs[0]);
+    auto *d_terms = reinterpret_cast<PauliTermDF *>(bufs[1]);
+    cuda_check(cudaMemcpyAsync(d_hdr, hdr.data(), hdr.size() * sizeof(PauliGroupHdr), cudaMemcpyHostToDevice,
+                               dst.stream()), "H2D");
+    cuda_check(cudaMemcpyAsync(d_terms, terms.data(), terms.size() * sizeof(PauliTermDF), cudaMemcpyHostToDevice,
+                               dst.stream()), "H2D");
+    for (size_t c = 0; c < chunks.size(); c++) {
+        const auto &ch = chunks[c];
+        launch_pauli_apply<T>(dst.stream(), psi, dst.data(), dst.length(), d_hdr + ch.g0,
+                              static_cast<int>(ch.g1 - ch.g0), d_terms + ch.t0, static_cast<int>(ch.t1 - ch.t0),
+                              c == 0);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Observable application (Observable::applyInPlace)
 // ---------------------------------------------------------------------------
@@ -196,10 +252,7 @@ template <class T> void Measure<T>::apply_obs(StateVector<T> &sv, const ObsNode 
         PauliSum ps;
         StateVector<T> src(sv);
         if (compile_pauli(o, sv.num_qubits(), ps) && !ps.terms.empty()) {
-            const auto groups = group_pauli(ps);
-            for (size_t i = 0; i < groups.size(); i++) {
-                launch_pauli_accumulate<T>(sv.stream(), src.data(), sv.data(), sv.length(), groups[i], i == 0);
-            }
+            pauli_sum_into<T>(src.data(), sv, group_pauli(ps));
             sv.synchronize();
             return;
         }
@@ -249,10 +302,7 @@ void Measure<T>::apply_obs_into(const StateVector<T> &src, StateVector<T> &dst, 
     if (o.kind != ObsNode::Sparse && o.kind != ObsNode::Herm && compile_pauli(o, src.num_qubits(), ps) &&
         !ps.terms.empty()) {
         src.synchronize();
-        const auto groups = group_pauli(ps);
-        for (size_t i = 0; i < groups.size(); i++) {
-            launch_pauli_accumulate<T>(dst.stream(), src.data(), dst.data(), dst.length(), groups[i], i == 0);
-        }
+        pauli_sum_into<T>(src.data(), dst, group_pauli(ps));
         dst.synchronize();
         return;
     }

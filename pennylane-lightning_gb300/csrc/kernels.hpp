@@ -106,6 +106,22 @@ void launch_csr_apply(cudaStream_t s, const cx<T> *sv, cx<T> *out, u64 N, const 
 // Hamiltonian apply, one flip-mask group: out (+)= sum_t c_t P_t psi
 template <class T>
 void launch_pauli_accumulate(cudaStream_t s, const cx<T> *psi, cx<T> *out, u64 N, const PauliGroup &g, bool first);
+// All flip-mask groups of a Pauli sum in one sweep (kernels_measure.cu):
+// out[j] (+)= sum_g sum_{t in g} c_t i^ny_t (-1)^{|k & yz_t|} psi[k], k = j ^ x_g,
+// in double-float arithmetic (coefficients split on the host).
+struct PauliTermDF {
+    u64 yz;
+    float chi, clo; // coefficient as a double-float pair
+    int ny4, pad;
+};
+struct PauliGroupHdr {
+    u64 x;
+    int tbegin, tend; // terms [tbegin, tend) of the term array
+};
+constexpr int kApplyMaxGroups = 256, kApplyMaxTerms = 1024; // per launch (staged in shared memory)
+template <class T>
+void launch_pauli_apply(cudaStream_t s, const cx<T> *psi, cx<T> *out, u64 N, const PauliGroupHdr *groups, int ngroups,
+                        const PauliTermDF *terms, int nterms, bool first);
 
 // Probabilities: all wires (elementwise), or marginal over `k` wires given by
 // their bit positions (wires[0] = MSB of the output index).

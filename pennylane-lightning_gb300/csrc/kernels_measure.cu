@@ -7,6 +7,7 @@
 // measurements/MeasurementsLQubit.hpp (probs :90-163, expval :213-394),
 // ExpValFunc.hpp (:69-335), utils/LinearAlgebra.hpp innerProdC (:122-145),
 // observables/ObservablesLQubit.hpp HamiltonianApplyInPlace (:156-251).
+#include "df.cuh"
 #include "kernels.hpp"
 
 namespace plgb {
@@ -169,19 +170,42 @@ __device__ __forceinline__ double term_pair(const PauliTerm &t, u64 j, u64 jp, d
     }
 }
 
+template <class T> __device__ __forceinline__ df to_df(T x) {
+    if constexpr (std::is_same_v<T, double>) {
+        return df_from_bits(x);
+    } else {
+        return df{x, 0.f};
+    }
+}
+template <class T> __device__ __forceinline__ T from_df(df x) {
+    if constexpr (std::is_same_v<T, double>) {
+        return df_to_double(x);
+    } else {
+        return __fadd_rn(x.hi, x.lo);
+    }
+}
+// <psi| sum_t c_t P_t |psi> for one flip-mask group.  Products and sums in
+// double-float arithmetic (FP32 pipe; complex128 amplitudes split with
+// integer operations), one conversion per thread before the block reduction.
 template <class T>
 __global__ void __launch_bounds__(kReduceThreads) k_pauli_group(const cx<T> *__restrict__ a, u64 N, const __grid_constant__ PauliGroup g,
                                                                double *partials) {
-    double v[1] = {0.0};
+    __shared__ df sc[kMaxTermsPerGroup];
+    for (int t = static_cast<int>(threadIdx.x); t < g.nterms; t += static_cast<int>(blockDim.x)) {
+        sc[t] = df(g.t[t].coeff);
+    }
+    __syncthreads();
+    df acc{0.f, 0.f};
     if (g.x == 0) {
         GRID_STRIDE(j, N) {
             const cx<T> p = a[j];
-            const double w = static_cast<double>(p.x) * p.x + static_cast<double>(p.y) * p.y;
-            double f = 0.0;
+            const df pr = to_df<T>(p.x), pi = to_df<T>(p.y);
+            const df w = df_fma(pr * pr, pi, pi);
+            df f{0.f, 0.f};
             for (int t = 0; t < g.nterms; t++) {
-                f += (__popcll(j & g.t[t].yz) & 1) ? -g.t[t].coeff : g.t[t].coeff;
+                f = (__popcll(j & g.t[t].yz) & 1) ? f - sc[t] : f + sc[t];
             }
-            v[0] += w * f;
+            acc = df_fma(acc, w, f);
         }
     } else {
         const u64 half = N >> 1;
@@ -190,16 +214,27 @@ __global__ void __launch_bounds__(kReduceThreads) k_pauli_group(const cx<T> *__r
             const u64 jp = j ^ g.x;
             const cx<T> p = a[j];
             const cx<T> q = a[jp];
-            // A = conj(p) q
-            const double ar = static_cast<double>(p.x) * q.x + static_cast<double>(p.y) * q.y;
-            const double ai = static_cast<double>(p.x) * q.y - static_cast<double>(p.y) * q.x;
-            double f = 0.0;
+            const df pr = to_df<T>(p.x), pi = to_df<T>(p.y), qr = to_df<T>(q.x), qi = to_df<T>(q.y);
+            // conj(p) q = ar + i ai
+            const df ar = df_fma(pr * qr, pi, qi);
+            const df ai = df_fma(pr * qi, -pi, qr);
+            // per term (term_pair): i^ny ((s' + s) ar + i (s' - s) ai), real part;
+            // s' + s and s' - s are 0 or +-2
+            df A{0.f, 0.f}, B{0.f, 0.f};
             for (int t = 0; t < g.nterms; t++) {
-                f += g.t[t].coeff * term_pair(g.t[t], j, jp, ar, ai);
+                const bool s = (__popcll(j & g.t[t].yz) & 1) != 0, sp = (__popcll(jp & g.t[t].yz) & 1) != 0;
+                const df c2 = sc[t] + sc[t];
+                switch (g.t[t].ny4) {
+                case 0: if (s == sp) { A = s ? A - c2 : A + c2; } break;
+                case 1: if (s != sp) { B = sp ? B + c2 : B - c2; } break;
+                case 2: if (s == sp) { A = s ? A + c2 : A - c2; } break;
+                default: if (s != sp) { B = sp ? B - c2 : B + c2; } break;
+                }
             }
-            v[0] += f;
+            acc = df_fma(df_fma(acc, A, ar), B, ai);
         }
     }
+    double v[1] = {df_to_double(acc)};
     block_reduce_store<1>(v, partials);
 }
 template <class T>
@@ -280,6 +315,81 @@ template <class T>
 void launch_pauli_accumulate(cudaStream_t s, const cx<T> *psi, cx<T> *out, u64 N, const PauliGroup &g, bool first) {
     k_pauli_accumulate<T><<<grid_for(N, 256, 8), 256, 0, s>>>(psi, out, N, g, first ? 1 : 0);
     cuda_check(cudaGetLastError(), "k_pauli_accumulate launch");
+    note_launch();
+}
+
+// One sweep for every flip-mask group of a Pauli sum: each output amplitude
+// reads its partners psi[j ^ x_g] once per group and is written once.  The
+// products and sums run in double-float arithmetic on the FP32 pipe (FP64
+// runs at 1/64 of it on GB300); complex128 inputs are split with integer
+// operations and the result is converted once.
+template <class T>
+__global__ void __launch_bounds__(256) k_pauli_apply(const cx<T> *__restrict__ psi, cx<T> *__restrict__ out, u64 N,
+                                                     const PauliGroupHdr *__restrict__ groups, int ngroups,
+                                                     const PauliTermDF *__restrict__ terms, int nterms, int first) {
+    __shared__ PauliGroupHdr sg[kApplyMaxGroups];
+    __shared__ PauliTermDF st[kApplyMaxTerms];
+    for (int i = static_cast<int>(threadIdx.x); i < ngroups; i += static_cast<int>(blockDim.x)) {
+        sg[i] = groups[i];
+    }
+    for (int i = static_cast<int>(threadIdx.x); i < nterms; i += static_cast<int>(blockDim.x)) {
+        st[i] = terms[i];
+    }
+    __syncthreads();
+    GRID_STRIDE(j, N) {
+        df re{0.f, 0.f}, im{0.f, 0.f};
+        if (!first) {
+            const cx<T> o = out[j];
+            re = to_df<T>(o.x);
+            im = to_df<T>(o.y);
+        }
+        for (int g = 0; g < ngroups; g++) {
+            const u64 k = j ^ sg[g].x;
+            const cx<T> q = psi[k];
+            const df qr = to_df<T>(q.x), qi = to_df<T>(q.y);
+            const int t0 = sg[g].tbegin, t1 = sg[g].tend;
+            if (t1 - t0 == 1) { // one term: a signed real or imaginary coefficient
+                const PauliTermDF &tm = st[t0];
+                df c{tm.chi, tm.clo};
+                if ((__popcll(k & tm.yz) & 1) != 0) {
+                    c = -c;
+                }
+                switch (tm.ny4) {
+                case 0: re = df_fma(re, c, qr); im = df_fma(im, c, qi); break;
+                case 1: re = df_fma(re, -c, qi); im = df_fma(im, c, qr); break;
+                case 2: re = df_fma(re, -c, qr); im = df_fma(im, -c, qi); break;
+                default: re = df_fma(re, c, qi); im = df_fma(im, -c, qr); break;
+                }
+                continue;
+            }
+            df wr{0.f, 0.f}, wi{0.f, 0.f};
+            for (int t = t0; t < t1; t++) {
+                const PauliTermDF &tm = st[t];
+                df c{tm.chi, tm.clo};
+                if ((__popcll(k & tm.yz) & 1) != 0) {
+                    c = -c;
+                }
+                switch (tm.ny4) {
+                case 0: wr = wr + c; break;
+                case 1: wi = wi + c; break;
+                case 2: wr = wr - c; break;
+                default: wi = wi - c; break;
+                }
+            }
+            re = df_fma(df_fma(re, wr, qr), -wi, qi);
+            im = df_fma(df_fma(im, wr, qi), wi, qr);
+        }
+        out[j] = cx<T>{from_df<T>(re), from_df<T>(im)};
+    }
+}
+template <class T>
+void launch_pauli_apply(cudaStream_t s, const cx<T> *psi, cx<T> *out, u64 N, const PauliGroupHdr *groups, int ngroups,
+                        const PauliTermDF *terms, int nterms, bool first) {
+    if (ngroups < 1 || ngroups > kApplyMaxGroups || nterms < 1 || nterms > kApplyMaxTerms) {
+        throw std::runtime_error("Pauli-sum apply: group or term count out of range");
+    }
+    k_pauli_apply<T><<<grid_for(N, 256, 8), 256, 0, s>>>(psi, out, N, groups, ngroups, terms, nterms, first ? 1 : 0);
+    cuda_check(cudaGetLastError(), "k_pauli_apply launch");
     note_launch();
 }
 
@@ -440,6 +550,8 @@ void launch_probs_marginal(cudaStream_t s, const cx<T> *sv, u64 N, int k, const 
     template void launch_csr_apply<T>(cudaStream_t, const cx<T> *, cx<T> *, u64, const long long *,              \
                                       const long long *, const cx<T> *);                                          \
     template void launch_pauli_accumulate<T>(cudaStream_t, const cx<T> *, cx<T> *, u64, const PauliGroup &, bool); \
+    template void launch_pauli_apply<T>(cudaStream_t, const cx<T> *, cx<T> *, u64, const PauliGroupHdr *, int,    \
+                                        const PauliTermDF *, int, bool);                                          \
     template void launch_probs_all<T>(cudaStream_t, const cx<T> *, u64, T *);                                    \
     template void launch_probs_marginal<T>(cudaStream_t, const cx<T> *, u64, int, const TBits &, double *);
 

@@ -103,9 +103,6 @@ template <class T>
 void launch_csr_apply(cudaStream_t s, const cx<T> *sv, cx<T> *out, u64 N, const long long *indptr,
                       const long long *indices, const cx<T> *vals);
 
-// Hamiltonian apply, one flip-mask group: out (+)= sum_t c_t P_t psi
-template <class T>
-void launch_pauli_accumulate(cudaStream_t s, const cx<T> *psi, cx<T> *out, u64 N, const PauliGroup &g, bool first);
 // All flip-mask groups of a Pauli sum in one sweep (kernels_measure.cu):
 // out[j] (+)= sum_g sum_{t in g} c_t i^ny_t (-1)^{|k & yz_t|} psi[k], k = j ^ x_g,
 // in double-float arithmetic (coefficients split on the host).

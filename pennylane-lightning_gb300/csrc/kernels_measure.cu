@@ -1,7 +1,9 @@
 // Measurement and linear-algebra kernels (sm_103a).  All reductions are
 // warp-shuffle + shared-memory tree reductions into per-block partials,
 // followed by a fixed-order final sum, so a result does not depend on
-// scheduling.  Accumulation is in double for both precisions.
+// scheduling.  Accumulation is in double for both precisions, except the
+// Pauli-sum kernels, which multiply and add in double-float arithmetic (the
+// FP32 pipe; FP64 runs at 1/64 of its rate on GB300) and convert once.
 //
 // Reference semantics: pennylane_lightning/core/simulators/lightning_qubit/
 // measurements/MeasurementsLQubit.hpp (probs :90-163, expval :213-394),
@@ -285,38 +287,6 @@ void reduce_pauli_transition(cudaStream_t s, const cx<T> *a, const cx<T> *b, u64
     finalize<2>(s, partials, g, out);
 }
 
-// Hamiltonian apply for one flip-mask group:
-// out_j (+)= psi_{j^x} * sum_t c_t i^ny (-1)^{|(j^x) & yz|}.
-template <class T>
-__global__ void __launch_bounds__(256) k_pauli_accumulate(const cx<T> *__restrict__ psi, cx<T> *__restrict__ out, u64 N,
-                                                         const __grid_constant__ PauliGroup g, int first) {
-    GRID_STRIDE(j, N) {
-        const u64 k = j ^ g.x;
-        double wr = 0.0, wi = 0.0;
-        for (int t = 0; t < g.nterms; t++) {
-            const double c = (__popcll(k & g.t[t].yz) & 1) ? -g.t[t].coeff : g.t[t].coeff;
-            switch (g.t[t].ny4) {
-            case 0: wr += c; break;
-            case 1: wi += c; break;
-            case 2: wr -= c; break;
-            default: wi -= c; break;
-            }
-        }
-        const cx<T> q = psi[k];
-        const cx<T> w{static_cast<T>(wr), static_cast<T>(wi)};
-        if (first) {
-            out[j] = w * q;
-        } else {
-            out[j] = cfma(w, q, out[j]);
-        }
-    }
-}
-template <class T>
-void launch_pauli_accumulate(cudaStream_t s, const cx<T> *psi, cx<T> *out, u64 N, const PauliGroup &g, bool first) {
-    k_pauli_accumulate<T><<<grid_for(N, 256, 8), 256, 0, s>>>(psi, out, N, g, first ? 1 : 0);
-    cuda_check(cudaGetLastError(), "k_pauli_accumulate launch");
-    note_launch();
-}
 
 // One sweep for every flip-mask group of a Pauli sum: each output amplitude
 // reads its partners psi[j ^ x_g] once per group and is written once.  The
@@ -549,7 +519,6 @@ void launch_probs_marginal(cudaStream_t s, const cx<T> *sv, u64 N, int k, const 
                                        const cx<T> *, double *, double *);                                        \
     template void launch_csr_apply<T>(cudaStream_t, const cx<T> *, cx<T> *, u64, const long long *,              \
                                       const long long *, const cx<T> *);                                          \
-    template void launch_pauli_accumulate<T>(cudaStream_t, const cx<T> *, cx<T> *, u64, const PauliGroup &, bool); \
     template void launch_pauli_apply<T>(cudaStream_t, const cx<T> *, cx<T> *, u64, const PauliGroupHdr *, int,    \
                                         const PauliTermDF *, int, bool);                                          \
     template void launch_probs_all<T>(cudaStream_t, const cx<T> *, u64, T *);                                    \

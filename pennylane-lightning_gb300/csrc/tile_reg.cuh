@@ -327,7 +327,8 @@ __device__ __forceinline__ double reduce_slots(const cx<T> (&a)[N], const cx<T> 
 #pragma unroll
         for (int i = 0; i < N; i++) {
             const cx<double> p = b[i], q = a[i ^ XR];
-            double z = want_re ? fma(p.y, q.y, p.x * q.x) : fma(-p.y, q.x, p.x * q.y);
+            const double qa = want_re ? q.x : q.y, qb = want_re ? q.y : q.x, pb = want_re ? p.y : -p.y;
+            double z = fma(pb, qb, p.x * qa);
             z = sflip(z, (static_cast<unsigned>(__popc(l.at(i ^ XR) & yz)) ^ gpar) & 1u);
             acc += ((l.at(i) & pm) == pv) ? z : 0.0;
         }
@@ -342,7 +343,9 @@ __device__ __forceinline__ double reduce_slots(const cx<T> (&a)[N], const cx<T> 
             } else {
                 px = df(b[i].x), py = df(b[i].y), qx = df(a[i ^ XR].x), qy = df(a[i ^ XR].y);
             }
-            df z = want_re ? df_fma(px * qx, py, qy) : df_fma(px * qy, -py, qx);
+            // Re: px qx + py qy;  Im: px qy - py qx  (operands selected, one chain)
+            const df qa = want_re ? qx : qy, qb = want_re ? qy : qx, pb = want_re ? py : -py;
+            df z = df_fma(px * qa, pb, qb);
             z = sflip(z, (static_cast<unsigned>(__popc(l.at(i ^ XR) & yz)) ^ gpar) & 1u);
             if ((l.at(i) & pm) != pv) { // outside the projector: adds zero
                 z = df{0.f, 0.f};

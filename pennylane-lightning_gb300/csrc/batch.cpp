@@ -702,6 +702,9 @@ template <class T> void BatchEngine<T>::run_adjoint(const BatchInput &in, double
     cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
     auto worker = [&]() {
         cudaSetDevice(dev);
+        // the request's registers, scratch and programs come from this
+        // thread's pool: no device-wide wait in cudaFree between requests
+        ReusePool pool;
         for (int c = next++; c < nc; c = next++) {
             const int n = in.num_qubits[c];
             const size_t need = size_t{3} * (sizeof(cx<T>) << n);
@@ -712,6 +715,7 @@ template <class T> void BatchEngine<T>::run_adjoint(const BatchInput &in, double
                 active++;
             }
             try {
+                ReuseScope scope(pool);
                 OpsList ops;
                 for (int64_t o = in.op_offsets[c]; o < in.op_offsets[c + 1]; o++) {
                     OpRec r;
@@ -781,6 +785,10 @@ template <class T> void BatchEngine<T>::run_adjoint(const BatchInput &in, double
             } catch (const std::exception &e) {
                 errors[static_cast<size_t>(c)] = e.what();
             }
+            // every register of the request synchronised its stream when it
+            // was destroyed, and the results were copied back: its buffers
+            // are idle
+            pool.recycle();
             {
                 std::lock_guard<std::mutex> g(bmu);
                 in_use -= need;

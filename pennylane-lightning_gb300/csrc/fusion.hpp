@@ -49,12 +49,8 @@ template <class T> struct FusedProgram {
     FusedProgram(const FusedProgram &) = delete;
     FusedProgram &operator=(const FusedProgram &) = delete;
     ~FusedProgram() {
-        if (dev) {
-            cudaFree(dev);
-        }
-        if (dev_df) {
-            cudaFree(dev_df);
-        }
+        dev_free(dev);
+        dev_free(dev_df);
     }
 };
 

@@ -14,6 +14,8 @@
 #include <random>
 #include <string>
 #include <vector>
+#include <map>
+#include <unordered_map>
 
 namespace plgb {
 
@@ -62,6 +64,49 @@ struct OpsList {
 };
 
 bool is_named_gate(const std::string &name);
+
+// ---------------------------------------------------------------------------
+// Device and pinned buffers of the host layer.  Outside a ReuseScope these
+// are cudaMalloc / cudaFree (cudaFree waits for the whole device).  Inside
+// one, the thread's ReusePool hands out buffers it already holds and takes
+// freed ones back without waiting; they become reusable after
+// ReusePool::recycle(), which the owner calls once the work that used them
+// has completed (the batch engine's adjoint workers: after each request).
+// ---------------------------------------------------------------------------
+class ReusePool {
+  public:
+    ReusePool() = default;
+    ReusePool(const ReusePool &) = delete;
+    ReusePool &operator=(const ReusePool &) = delete;
+    ~ReusePool();
+    void *take(size_t bytes, bool pinned);
+    bool give(void *p); // false: not handed out by this pool
+    void recycle();     // pending buffers become reusable (their work is done)
+    size_t cap_bytes{size_t{4} << 30}; // held beyond this are released
+  private:
+    struct Buf {
+        size_t cap;
+        bool pinned;
+    };
+    std::unordered_map<void *, Buf> out_;
+    std::multimap<size_t, void *> free_[2]; // [pinned]
+    std::vector<std::pair<void *, Buf>> pending_;
+    size_t held_{0};
+};
+class ReuseScope {
+  public:
+    explicit ReuseScope(ReusePool &pool);
+    ~ReuseScope();
+    ReuseScope(const ReuseScope &) = delete;
+    ReuseScope &operator=(const ReuseScope &) = delete;
+
+  private:
+    ReusePool *prev_;
+};
+void *dev_alloc(size_t bytes);
+void dev_free(void *p);
+void *pinned_alloc(size_t bytes);
+void pinned_free(void *p);
 
 // ---------------------------------------------------------------------------
 // Device scratch owned by a state vector.

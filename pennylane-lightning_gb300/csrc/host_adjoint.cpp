@@ -183,12 +183,10 @@ std::vector<double> Adjoint<T>::jacobian(StateVector<T> &sv, const std::vector<O
             const int t = std::max(1, std::min({fused_tile_bits, n, tmax}));
             auto prog = compile_fused<T>(n, prims, t, true);
             const int G = adj_grid_capacity(sizeof(cx<T>) << t);
-            double *d_part = nullptr;
-            cuda_check(cudaMalloc(&d_part, (static_cast<size_t>(G) + 1) * ntp * sizeof(double)),
-                       "cudaMalloc(adjoint partials)");
+            double *d_part = static_cast<double *>(dev_alloc((static_cast<size_t>(G) + 1) * ntp * sizeof(double)));
             struct Guard {
                 double *p;
-                ~Guard() { cudaFree(p); }
+                ~Guard() { dev_free(p); }
             } guard{d_part};
             double *d_out = d_part + static_cast<size_t>(G) * ntp;
             cuda_check(cudaMemsetAsync(d_part, 0, static_cast<size_t>(G) * ntp * sizeof(double), lambda.stream()),
@@ -213,10 +211,10 @@ std::vector<double> Adjoint<T>::jacobian(StateVector<T> &sv, const std::vector<O
     // Pauli-generator results stay on the device (two doubles per
     // [param][obs]); one copy at the end instead of a sync per parameter
     double *d_res = nullptr;
-    cuda_check(cudaMalloc(&d_res, 2 * nobs * ntp * sizeof(double)), "cudaMalloc(adjoint results)");
+    d_res = static_cast<double *>(dev_alloc(2 * nobs * ntp * sizeof(double)));
     struct ResGuard {
         double *p;
-        ~ResGuard() { cudaFree(p); }
+        ~ResGuard() { dev_free(p); }
     } res_guard{d_res};
     std::vector<char> on_device(nobs * ntp, 0);
     std::vector<double> dev_scale(nobs * ntp, 0.0);
@@ -313,10 +311,10 @@ std::vector<cd> Adjoint<T>::vjp(StateVector<T> &sv, const OpsList &opsl, const s
     std::unique_ptr<StateVector<T>> mu_d;
     double *red = lambda.scratch_red();
     double *d_res = nullptr;
-    cuda_check(cudaMalloc(&d_res, 2 * ntp * sizeof(double)), "cudaMalloc(vjp results)");
+    d_res = static_cast<double *>(dev_alloc(2 * ntp * sizeof(double)));
     struct Guard {
         double *p;
-        ~Guard() { cudaFree(p); }
+        ~Guard() { dev_free(p); }
     } guard{d_res};
     std::vector<double> scale(ntp, 0.0);
     std::vector<char> on_device(ntp, 0);

@@ -1167,7 +1167,7 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
     const size_t b_forms = align_up(std::max<size_t>(1, forms.size()) * sizeof(DiagForm<T>));
     const size_t b_tab = align_up(std::max<size_t>(1, tables.size()) * sizeof(cx<T>));
     const size_t b_st = align_up(std::max<size_t>(1, stages.size()) * sizeof(StageDesc));
-    cuda_check(cudaMalloc(&prog->dev, b_ops + b_forms + b_tab + b_st), "cudaMalloc(fused program)");
+    prog->dev = dev_alloc(b_ops + b_forms + b_tab + b_st);
     char *base = static_cast<char *>(prog->dev);
     prog->d_ops = reinterpret_cast<TileOp<T> *>(base);
     prog->d_forms = reinterpret_cast<DiagForm<T> *>(base + b_ops);
@@ -1218,7 +1218,7 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
             for (size_t i = 0; i < tables.size(); i++) {
                 tables_df[i] = cdf(tables[i]);
             }
-            cuda_check(cudaMalloc(&prog->dev_df, b_ops + b_forms + b_tab), "cudaMalloc(fused program, df)");
+            prog->dev_df = dev_alloc(b_ops + b_forms + b_tab);
             char *bd = static_cast<char *>(prog->dev_df);
             prog->d_ops_df = bd;
             prog->d_forms_df = bd + b_ops;

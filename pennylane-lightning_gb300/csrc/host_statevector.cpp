@@ -35,15 +35,104 @@ static thread_local std::string g_last_error;
 void set_last_error(const std::string &msg) { g_last_error = msg; }
 const char *last_error() { return g_last_error.c_str(); }
 
+// ---- device / pinned buffers: cudaMalloc, or the thread's reuse pool
+namespace {
+thread_local ReusePool *tl_pool = nullptr;
+size_t pool_bucket(size_t bytes) {
+    size_t c = 256;
+    while (c < bytes) {
+        c <<= 1;
+    }
+    return c;
+}
+} // namespace
+
+ReusePool::~ReusePool() {
+    recycle();
+    for (int k = 0; k < 2; k++) {
+        for (auto &kv : free_[k]) {
+            k ? cudaFreeHost(kv.second) : cudaFree(kv.second);
+        }
+    }
+}
+void *ReusePool::take(size_t bytes, bool pinned) {
+    const size_t cap = pool_bucket(bytes);
+    auto &fl = free_[pinned ? 1 : 0];
+    void *p = nullptr;
+    auto it = fl.find(cap);
+    if (it != fl.end()) {
+        p = it->second;
+        fl.erase(it);
+        held_ -= cap;
+    } else if (pinned) {
+        cuda_check(cudaMallocHost(&p, cap), "cudaMallocHost(pool)");
+    } else {
+        cuda_check(cudaMalloc(&p, cap), "cudaMalloc(pool)");
+    }
+    out_[p] = Buf{cap, pinned};
+    return p;
+}
+bool ReusePool::give(void *p) {
+    auto it = out_.find(p);
+    if (it == out_.end()) {
+        return false;
+    }
+    pending_.emplace_back(p, it->second);
+    out_.erase(it);
+    return true;
+}
+void ReusePool::recycle() {
+    for (auto &pb : pending_) {
+        if (held_ + pb.second.cap > cap_bytes) {
+            pb.second.pinned ? cudaFreeHost(pb.first) : cudaFree(pb.first);
+        } else {
+            free_[pb.second.pinned ? 1 : 0].emplace(pb.second.cap, pb.first);
+            held_ += pb.second.cap;
+        }
+    }
+    pending_.clear();
+}
+ReuseScope::ReuseScope(ReusePool &pool) : prev_(tl_pool) { tl_pool = &pool; }
+ReuseScope::~ReuseScope() { tl_pool = prev_; }
+
+void *dev_alloc(size_t bytes) {
+    if (tl_pool) {
+        return tl_pool->take(bytes, false);
+    }
+    void *p = nullptr;
+    cuda_check(cudaMalloc(&p, bytes), "cudaMalloc");
+    return p;
+}
+void dev_free(void *p) {
+    if (!p || (tl_pool && tl_pool->give(p))) {
+        return;
+    }
+    cudaFree(p);
+}
+void *pinned_alloc(size_t bytes) {
+    if (tl_pool) {
+        return tl_pool->take(bytes, true);
+    }
+    void *p = nullptr;
+    cuda_check(cudaMallocHost(&p, bytes), "cudaMallocHost");
+    return p;
+}
+void pinned_free(void *p) {
+    if (!p || (tl_pool && tl_pool->give(p))) {
+        return;
+    }
+    cudaFreeHost(p);
+}
+
 void DeviceScratch::ensure_mat(size_t bytes) {
     if (bytes <= mat_bytes) {
         return;
     }
     if (mat) {
-        cudaFree(mat);
+        dev_free(mat);
         mat = nullptr;
     }
-    cuda_check(cudaMalloc(&mat, bytes), "cudaMalloc(scratch)");
+    mat = dev_alloc(bytes);
     mat_bytes = bytes;
 }
 std::vector<char *> DeviceScratch::carve(std::initializer_list<size_t> sizes) {
@@ -62,15 +151,9 @@ std::vector<char *> DeviceScratch::carve(std::initializer_list<size_t> sizes) {
 }
 
 DeviceScratch::~DeviceScratch() {
-    if (red) {
-        cudaFree(red);
-    }
-    if (host_out) {
-        cudaFreeHost(host_out);
-    }
-    if (mat) {
-        cudaFree(mat);
-    }
+    dev_free(red);
+    pinned_free(host_out);
+    dev_free(mat);
 }
 
 static const char *kGateNames[] = {
@@ -125,13 +208,13 @@ template <class T> void StateVector<T>::alloc_(bool zero) {
     PLGB_REQUIRE(n_ >= 0 && n_ <= 40, "number of qubits out of range");
     N_ = u64{1} << n_;
     if (owns_) {
-        cuda_check(cudaMalloc(&d_, N_ * sizeof(CT)), "cudaMalloc(state vector)");
+        d_ = static_cast<CT *>(dev_alloc(N_ * sizeof(CT)));
         if (zero) {
             cuda_check(cudaMemsetAsync(d_, 0, N_ * sizeof(CT), s_), "memset");
         }
     }
-    cuda_check(cudaMalloc(&scratch_.red, sizeof(double) * (kReduceBlocks * 2 + 8)), "cudaMalloc(reduction)");
-    cuda_check(cudaMallocHost(&scratch_.host_out, sizeof(double) * 8), "cudaMallocHost");
+    scratch_.red = static_cast<double *>(dev_alloc(sizeof(double) * (kReduceBlocks * 2 + 8)));
+    scratch_.host_out = static_cast<double *>(pinned_alloc(sizeof(double) * 8));
 }
 
 template <class T> StateVector<T>::StateVector(int num_qubits, cudaStream_t stream) : n_(num_qubits) {
@@ -171,7 +254,7 @@ template <class T> StateVector<T>::StateVector(const StateVector &o) : n_(o.n_),
 template <class T> StateVector<T>::~StateVector() {
     if (owns_ && d_) {
         cudaStreamSynchronize(s_);
-        cudaFree(d_);
+        dev_free(d_);
     }
     if (owns_stream_) {
         cudaStreamDestroy(s_);

@@ -101,6 +101,46 @@ def test_all_generators_multi_obs(ops_module, oracle, dt):
     assert_jac(jg, jo, dt, "generators")
 
 
+@pytest.mark.parametrize("dt", DTYPES)
+@pytest.mark.parametrize("with_two_bit_flips", [False, True])
+def test_fused_register_sweep_generators(ops_module, oracle, dt, with_two_bit_flips):
+    # One observable and Pauli-word generators only, on 11 qubits: the whole
+    # reverse sweep runs as fused two-register tile passes with reductions in
+    # register stages (flip on a register bit, Z-type without flip, controlled
+    # generators with a projector).  IsingXX / IsingYY flip two bits: their
+    # passes take the shared-memory two-register kernel, mixed with the
+    # register passes in one sweep.
+    from oracle.pyoracle import pauli_sum_spec
+
+    rng = np.random.default_rng(seed_of("adjreg", dt.__name__, with_two_bit_flips))
+    n = 11
+    gates = [("RX", 1), ("RY", 1), ("RZ", 1), ("CRX", 2), ("CRY", 2), ("CRZ", 2), ("IsingZZ", 2), ("MultiRZ", 3)]
+    if with_two_bit_flips:
+        gates += [("IsingXX", 2), ("IsingYY", 2)]
+    ops = [dict(name="Hadamard", wires=[q]) for q in range(n)]
+    for _ in range(4):
+        for name, k in gates:
+            w = [int(x) for x in rng.choice(n, size=k, replace=False)]
+            ops.append(dict(name=name, params=[float(rng.uniform(0, 6.28))], wires=w,
+                            inverse=bool(rng.integers(0, 2))))
+            ops.append(dict(name="CNOT", wires=[int(w[0]), int((w[0] + 3) % n)]))
+        ops.append(dict(name="RY", params=[float(rng.uniform(0, 6.28))], wires=[int(rng.integers(0, n))],
+                        cwires=[int(rng.integers(0, n))], cvals=[True]))
+    # controlled-RY entries whose control equals the target are invalid: redraw
+    for o in ops:
+        if o.get("cwires") and o["cwires"][0] == o["wires"][0]:
+            o["cwires"] = [(o["wires"][0] + 5) % n]
+    npar = sum(1 for o in ops if o.get("params"))
+    tp = list(range(npar))
+    terms = [(float(rng.normal()), "".join(rng.choice(list("XYZ"), size=m)),
+              [int(x) for x in rng.choice(n, size=m, replace=False)]) for m in (1, 2, 2, 3, 4)]
+    Named, _, Prod, Ham, _ = obs_ns(ops_module, dt)
+    H = Ham([t[0] for t in terms], [Prod([Named("Pauli" + c, [w]) for c, w in zip(t[1], t[2])]) for t in terms])
+    jg = gpu_jacobian(ops_module, dt, n, ops, [H], tp)
+    jo = oracle.sv(n, dt).adjoint(ops, [pauli_sum_spec(terms)], tp, apply_ops=True)
+    assert_jac(jg, jo, dt, "fused register sweep")
+
+
 def test_known_answers_rx_zzz(ops_module):
     # Test_AdjointJacobian.cpp:336-373 (values computed with parameter shift)
     Named, _, Prod, _, _ = obs_ns(ops_module, np.complex128)

@@ -181,3 +181,29 @@ def test_mcmc_samples_edges(ops_module, oracle, dt):
     sv.updateData(np.zeros(16, dtype=dt))
     with pytest.raises(LightningException):
         m.generate_mcmc_samples(4, "Local", 0, 10)  # no non-zero amplitude to propose
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+def test_large_pauli_sum_apply_chunks(ops_module, oracle, dt):
+    # var of a Pauli sum with more flip-mask groups than one launch of the
+    # one-sweep application takes (256): the application runs in chunks, the
+    # later ones adding to the first's output.
+    from oracle.pyoracle import pauli_sum_spec
+
+    rng, sv, m, o = _setup(ops_module, oracle, 10, dt, seed_of("bigham", dt.__name__))
+    terms = []
+    seen = set()
+    while len(terms) < 400:
+        k = int(rng.integers(1, 5))
+        wires = [int(x) for x in rng.choice(10, size=k, replace=False)]
+        word = "".join(rng.choice(list("XYZ"), size=k))
+        key = (word, tuple(wires))
+        if key in seen:
+            continue
+        seen.add(key)
+        terms.append((float(rng.normal()), word, wires))
+    Named, _, Prod, Ham, _ = obs_ns(ops_module, dt)
+    H = Ham([t[0] for t in terms], [Prod([Named("Pauli" + c, [w]) for c, w in zip(t[1], t[2])]) for t in terms])
+    spec = pauli_sum_spec(terms)
+    assert_close(m.expval(H), o.expval_obs(spec), dt, scale=400, what="E big H")
+    assert_close(m.var(H), o.var_obs(spec), dt, scale=4000, what="var big H")

@@ -148,18 +148,23 @@ def workload(n, cycles):
     return circuit, ham, unfused_bytes
 
 
-def traffic_from_profiles(kernel_tag: str):
-    """Per-launch DRAM bytes (read + write) recorded in profiles/<tag>.md."""
+def profile_value(kernel_tag: str, key: str):
+    """A `key: value` line recorded in profiles/<tag>.md (ncu figures)."""
     p = REPO / "profiles" / f"{kernel_tag}.md"
     if not p.exists():
         return None
     for ln in p.read_text().splitlines():
-        if ln.strip().startswith("traffic_bytes_per_launch:"):
+        if ln.strip().startswith(key + ":"):
             try:
                 return float(ln.split(":", 1)[1].strip().split()[0])
             except ValueError:
                 return None
     return None
+
+
+def traffic_from_profiles(kernel_tag: str):
+    """Per-launch DRAM bytes (read + write) recorded in profiles/<tag>.md."""
+    return profile_value(kernel_tag, "traffic_bytes_per_launch")
 
 
 def gpu_arm(args) -> dict | None:
@@ -298,7 +303,10 @@ def gpu_arm(args) -> dict | None:
                      "algorithmic_bytes_per_launch": pass_bytes, "avg_launch_ms": avg_launch_s * 1e3,
                      "note": "fused-actual bytes (2 N S per pass): the pass is instruction-bound on the FP32 "
                              "pipe (double-float arithmetic; GB300 runs FP64 at 1/64 of FP32), not HBM-bound; the "
-                             "unfused-equivalent rate is `value`"},
+                             "unfused-equivalent rate is `value`",
+                     "issue": {"metric": "smsp__issue_active (ncu, fraction of peak instruction issue)",
+                               "frac": profile_value(tag, "issue_active_frac"),
+                               "source": f"profiles/{tag}.md"}},
         "unfused": {"ms_per_step": tune.get(0), "value": alg_bytes / (tune[0] / 1e3) / 1e9 if tune.get(0) else None},
         "gpu_launches": launches,
         "clocks": clk.summary(),

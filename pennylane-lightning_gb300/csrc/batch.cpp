@@ -700,11 +700,12 @@ template <class T> void BatchEngine<T>::run_adjoint(const BatchInput &in, double
     stats_.done_ms.assign(static_cast<size_t>(nc), 0.0);
     int dev = 0;
     cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    std::atomic<int> next_worker{0};
     auto worker = [&]() {
         cudaSetDevice(dev);
         // the request's registers, scratch and programs come from this
-        // thread's pool: no device-wide wait in cudaFree between requests
-        ReusePool pool;
+        // worker's pool: no device-wide wait in cudaFree between requests
+        ReusePool &pool = *adj_pools_[static_cast<size_t>(next_worker++)];
         for (int c = next++; c < nc; c = next++) {
             const int n = in.num_qubits[c];
             const size_t need = size_t{3} * (sizeof(cx<T>) << n);
@@ -805,6 +806,9 @@ template <class T> void BatchEngine<T>::run_adjoint(const BatchInput &in, double
     }
     int nt = threads_ > 0 ? threads_ : static_cast<int>(std::thread::hardware_concurrency());
     nt = std::max(1, std::min({nt, 8, nc}));
+    while (static_cast<int>(adj_pools_.size()) < nt) {
+        adj_pools_.push_back(std::make_unique<ReusePool>());
+    }
     std::vector<std::thread> pool;
     for (int i = 1; i < nt; i++) {
         pool.emplace_back(worker);

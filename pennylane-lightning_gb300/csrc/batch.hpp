@@ -138,6 +138,9 @@ template <class T> class BatchEngine {
     void *h_prog_[2]{}, *h_items_[2]{}, *h_out_[2]{};
     size_t ch_prog_[2]{}, ch_items_[2]{}, ch_out_[2]{};
     BatchStats stats_;
+    // run_adjoint workers' buffer pools, kept between calls (a serving lane
+    // calls it once per request); worker k uses adj_pools_[k]
+    std::vector<std::unique_ptr<ReusePool>> adj_pools_;
 };
 
 } // namespace plgb

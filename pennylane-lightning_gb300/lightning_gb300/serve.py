@@ -11,9 +11,11 @@ queues independently, so work of different lanes overlaps on the device:
   lane takes ALL queued requests the budget admits (requests that arrived
   while the previous batch was on the GPU join here) and runs them as one
   batch of the batch engine;
-* `adjoint_lanes` adjoint lanes: every pass takes all queued adjoint
-  requests the budget admits; the engine runs them concurrently on host
-  threads with their own streams (fused forward pass, <H>, in-place adjoint
+* `adjoint_lanes` adjoint lanes sharing one queue: a lane that finishes
+  a request takes the next queued adjoint request the budget admits (up to
+  `adjoint_take` at a time), so adjoint work is admitted per request while
+  other requests are on the GPU; each lane runs on its own host thread,
+  streams and buffer pool (fused forward pass, <H>, in-place adjoint
   sweep).
 
 Results of a request do not depend on what else is in flight: a forward
@@ -84,7 +86,8 @@ class ServeResult:
 
 class Server:
     def __init__(self, precision: int = 128, budget_bytes: float = 150e9, big_qubits: int = 20,
-                 adjoint_lanes: int = 1, max_batch: int = 4096, tile_bits: int = 11, adjoint_share: float = 0.4):
+                 adjoint_lanes: int = 8, max_batch: int = 4096, tile_bits: int = 11, adjoint_share: float = 0.4,
+                 adjoint_take: int = 1):
         self.precision = int(precision)
         self.S = 16 if self.precision == 128 else 8
         # forward and adjoint lanes draw on separate shares of the budget, so
@@ -95,11 +98,12 @@ class Server:
         self.max_batch = int(max_batch)
         self.tile_bits = int(tile_bits)
         self.adjoint_lanes = int(adjoint_lanes)
+        self.adjoint_take = int(adjoint_take)
         # forward lanes keep their engines (device arenas, tuned tile sizes)
         self.engines = [BatchEngine(self.precision, wave_bytes=int(budget_bytes)),
                         BatchEngine(self.precision, wave_bytes=int(budget_bytes))]
-        # adjoint lanes: batches of requests, each circuit on its own host
-        # thread and stream inside the engine
+        # adjoint lanes: one engine each (its streams and buffer pool persist
+        # across the requests the lane serves)
         self.adj_engines = [BatchEngine(self.precision, tile_bits=self.tile_bits,
                                         wave_bytes=int(budget_bytes * adjoint_share))
                             for _ in range(self.adjoint_lanes)]
@@ -156,7 +160,7 @@ class Server:
         lane_of = np.zeros(R, np.int32)
         batches: list = []
         lock = threading.Lock()
-        nl = 2 + self.adjoint_lanes
+        nl = 3  # two forward lanes; one queue shared by the adjoint lanes
         queues = [collections.deque() for _ in range(nl)]
         cvs = [threading.Condition() for _ in range(nl)]
         closing = threading.Event()
@@ -217,7 +221,7 @@ class Server:
             eng = self.adj_engines[li - 2]
             try:
                 while True:
-                    got = take(li, self.max_batch)
+                    got = take(2, self.adjoint_take)
                     if not got:
                         return
                     ts = now()
@@ -242,7 +246,6 @@ class Server:
                     for k in range(self.adjoint_lanes)]
         for th in threads:
             th.start()
-        rr = 0  # round robin over the adjoint lanes
         for r in range(R):
             if errors:
                 break
@@ -250,8 +253,7 @@ class Server:
             if wait > 0:
                 time.sleep(wait)
             if self.adjoint[r]:
-                li = 2 + rr
-                rr = (rr + 1) % self.adjoint_lanes
+                li = 2
             else:
                 li = 1 if packed.num_qubits[r] >= self.big else 0
             with cvs[li]:

@@ -316,9 +316,9 @@ __device__ __forceinline__ const PassOpRec<T, STAGE> *op_records(unsigned char *
 // Y|Z bits.  XR = the flip as a register-slot mask (compile time, so both
 // slots stay in registers).  Products and the running sum in double-float
 // (complex64 / double-float registers) or FP64 (complex128 in FP64).
-template <class T, int XR, int N>
+template <class T, int XR, bool RE, int N>
 __device__ __forceinline__ double reduce_slots(const cx<T> (&a)[N], const cx<T> (&b)[N], const Layout &l,
-                                               u32 pm, u32 pv, u32 yz, unsigned gpar, bool want_re) {
+                                               u32 pm, u32 pv, u32 yz, unsigned gpar) {
     if constexpr (XR >= N) {
         return 0.0; // no such register bit at this register count
     }
@@ -327,8 +327,8 @@ __device__ __forceinline__ double reduce_slots(const cx<T> (&a)[N], const cx<T> 
 #pragma unroll
         for (int i = 0; i < N; i++) {
             const cx<double> p = b[i], q = a[i ^ XR];
-            const double qa = want_re ? q.x : q.y, qb = want_re ? q.y : q.x, pb = want_re ? p.y : -p.y;
-            double z = fma(pb, qb, p.x * qa);
+            // Re: px qx + py qy;  Im: px qy - py qx
+            double z = RE ? fma(p.y, q.y, p.x * q.x) : fma(-p.y, q.x, p.x * q.y);
             z = sflip(z, (static_cast<unsigned>(__popc(l.at(i ^ XR) & yz)) ^ gpar) & 1u);
             acc += ((l.at(i) & pm) == pv) ? z : 0.0;
         }
@@ -343,9 +343,8 @@ __device__ __forceinline__ double reduce_slots(const cx<T> (&a)[N], const cx<T> 
             } else {
                 px = df(b[i].x), py = df(b[i].y), qx = df(a[i ^ XR].x), qy = df(a[i ^ XR].y);
             }
-            // Re: px qx + py qy;  Im: px qy - py qx  (operands selected, one chain)
-            const df qa = want_re ? qx : qy, qb = want_re ? qy : qx, pb = want_re ? py : -py;
-            df z = df_fma(px * qa, pb, qb);
+            // Re: px qx + py qy;  Im: px qy - py qx
+            df z = RE ? df_fma(px * qx, py, qy) : df_fma(px * qy, -py, qx);
             z = sflip(z, (static_cast<unsigned>(__popc(l.at(i ^ XR) & yz)) ^ gpar) & 1u);
             if ((l.at(i) & pm) != pv) { // outside the projector: adds zero
                 z = df{0.f, 0.f};
@@ -578,12 +577,20 @@ __device__ __forceinline__ void tile_reg_run(const cx<SI> *ain, cx<SO> *aout, co
                         const unsigned gpar = static_cast<unsigned>(__popcll(gbase & ro.pmask) & 1);
                         const bool want_re = (ro.mode & 1) != 0;
                         double z;
-                        switch (ro.tcmask) {
-                        case 0: z = reduce_slots<T, 0>(v, vb, cur, ro.rcmask, ro.lcval, ro.lo0, gpar, want_re); break;
-                        case 1: z = reduce_slots<T, 1>(v, vb, cur, ro.rcmask, ro.lcval, ro.lo0, gpar, want_re); break;
-                        case 2: z = reduce_slots<T, 2>(v, vb, cur, ro.rcmask, ro.lcval, ro.lo0, gpar, want_re); break;
-                        case 4: z = reduce_slots<T, 4>(v, vb, cur, ro.rcmask, ro.lcval, ro.lo0, gpar, want_re); break;
-                        default: z = reduce_slots<T, 8>(v, vb, cur, ro.rcmask, ro.lcval, ro.lo0, gpar, want_re); break;
+                        // the flip slot mask and Re / Im as compile-time cases
+                        // (the register count of the adjoint kernel: XR <= 4)
+                        const u32 pm = ro.rcmask, pv = ro.lcval, yz = ro.lo0;
+                        switch (ro.tcmask * 2 + (want_re ? 1 : 0)) {
+                        case 0: z = reduce_slots<T, 0, false>(v, vb, cur, pm, pv, yz, gpar); break;
+                        case 1: z = reduce_slots<T, 0, true>(v, vb, cur, pm, pv, yz, gpar); break;
+                        case 2: z = reduce_slots<T, 1, false>(v, vb, cur, pm, pv, yz, gpar); break;
+                        case 3: z = reduce_slots<T, 1, true>(v, vb, cur, pm, pv, yz, gpar); break;
+                        case 4: z = reduce_slots<T, 2, false>(v, vb, cur, pm, pv, yz, gpar); break;
+                        case 5: z = reduce_slots<T, 2, true>(v, vb, cur, pm, pv, yz, gpar); break;
+                        case 8: z = reduce_slots<T, 4, false>(v, vb, cur, pm, pv, yz, gpar); break;
+                        case 9: z = reduce_slots<T, 4, true>(v, vb, cur, pm, pv, yz, gpar); break;
+                        case 16: z = reduce_slots<T, 8, false>(v, vb, cur, pm, pv, yz, gpar); break;
+                        default: z = reduce_slots<T, 8, true>(v, vb, cur, pm, pv, yz, gpar); break;
                         }
                         if (ro.mode & 2) {
                             z = -z;

@@ -194,6 +194,17 @@ int plgb_set_c128_fp64_passes(int on);
  * resident warps, some spills).  Returns the previous setting, or -1 for a
  * bad precision (no counterpart in the reference). */
 int plgb_set_tile_variant(int precision, int occ);
+/* Lazy fusion of per-gate calls (no counterpart in the reference; on by
+ * default): on a lazy handle the gate calls (plgb_sv_apply_operation,
+ * _controlled_operation, _matrix, _controlled_matrix) validate their
+ * arguments and queue the gate; the next call that reads or rewrites the
+ * state first runs the queue as fused tile passes.  Results are those of
+ * the gates applied one by one within the precision's tolerance.
+ * plgb_set_lazy_fusion sets the default for handles created afterwards and
+ * returns the previous default; plgb_sv_set_lazy switches one handle (its
+ * queue runs first). */
+int plgb_set_lazy_fusion(int on);
+int plgb_sv_set_lazy(plgb_sv *sv, int on);
 /* Plan introspection (no device needed): the tile passes plgb_sv_apply_operations
  * would run for `ops` on num_qubits at precision / tile_bits, as a JSON array
  * with one object per pass (tile size, op counts, execution stages). */

@@ -6,6 +6,7 @@
 #include "host.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -19,6 +20,11 @@ struct plgb_sv {
     int precision;
     std::unique_ptr<StateVector<float>> f;
     std::unique_ptr<StateVector<double>> d;
+    // deferred gate calls (lazy fusion): their primitives, run as fused tile
+    // passes by the next call that reads or rewrites the state
+    bool lazy{false};
+    std::vector<plgb::Prim<float>> pend_f;
+    std::vector<plgb::Prim<double>> pend_d;
 };
 struct plgb_obs {
     ObsPtr node;
@@ -69,13 +75,81 @@ void need(const void *p, const char *what) {
     }
 }
 
+// Lazy fusion of per-gate calls (the call pattern of lightning.qubit's
+// Python device, one binding call per gate): a gate call validates and
+// lowers the gate at once (errors surface at that call) and queues its
+// primitives; the next call that reads or rewrites the state first runs the
+// queue, as fused register-tile passes when it holds at least
+// kLazyFuseMin primitives on a register of at least 2^9 amplitudes, else
+// primitive by primitive.
+std::atomic<int> g_lazy_fusion{1};
+constexpr size_t kLazyFuseMin = 16;
+template <class T> void run_pending(StateVector<T> &s, std::vector<Prim<T>> &pend) {
+    if (pend.empty()) {
+        return;
+    }
+    std::vector<Prim<T>> prims;
+    prims.swap(pend); // the queue is empty whatever happens next
+    if (s.num_qubits() >= kMinRegTileBits && prims.size() >= kLazyFuseMin) {
+        s.apply_prims_fused(prims, sizeof(T) == 8 ? 11 : 12);
+    } else {
+        for (const auto &p : prims) {
+            s.run_prim(p);
+        }
+    }
+}
+void flush_sv(plgb_sv *sv) {
+    if (sv->precision == 128) {
+        run_pending(*sv->d, sv->pend_d);
+    } else {
+        run_pending(*sv->f, sv->pend_f);
+    }
+}
+
 template <class F> int with_sv(plgb_sv *sv, F &&f) {
+    return guard([&] {
+        need(sv, "state vector");
+        flush_sv(sv);
+        if (sv->precision == 128) {
+            f(*sv->d);
+        } else {
+            f(*sv->f);
+        }
+    });
+}
+// Queries of the register's shape: no need to run the queue.
+template <class F> int with_sv_meta(plgb_sv *sv, F &&f) {
     return guard([&] {
         need(sv, "state vector");
         if (sv->precision == 128) {
             f(*sv->d);
         } else {
             f(*sv->f);
+        }
+    });
+}
+// A gate call: queued when the handle is lazy, applied at once otherwise.
+template <class F> int with_sv_gate(plgb_sv *sv, F &&f) {
+    return guard([&] {
+        need(sv, "state vector");
+        if (!sv->lazy) {
+            if (sv->precision == 128) {
+                f(*sv->d);
+            } else {
+                f(*sv->f);
+            }
+            return;
+        }
+        if (sv->precision == 128) {
+            auto &s = *sv->d;
+            auto prims = s.capture_prims([&] { f(s); });
+            sv->pend_d.insert(sv->pend_d.end(), std::make_move_iterator(prims.begin()),
+                              std::make_move_iterator(prims.end()));
+        } else {
+            auto &s = *sv->f;
+            auto prims = s.capture_prims([&] { f(s); });
+            sv->pend_f.insert(sv->pend_f.end(), std::make_move_iterator(prims.begin()),
+                              std::make_move_iterator(prims.end()));
         }
     });
 }
@@ -182,6 +256,7 @@ int plgb_sv_create(int num_qubits, int precision, plgb_sv **out) {
         }
         auto h = std::make_unique<plgb_sv>();
         h->precision = precision;
+        h->lazy = g_lazy_fusion.load() != 0;
         if (precision == 128) {
             h->d = std::make_unique<StateVector<double>>(num_qubits);
         } else {
@@ -198,6 +273,7 @@ int plgb_sv_create_raw(void *device_data, int num_qubits, int precision, plgb_sv
         PLGB_REQUIRE(precision == 64 || precision == 128, "precision must be 64 or 128");
         auto h = std::make_unique<plgb_sv>();
         h->precision = precision;
+        h->lazy = g_lazy_fusion.load() != 0;
         if (precision == 128) {
             h->d = std::make_unique<StateVector<double>>(static_cast<cx<double> *>(device_data), num_qubits);
         } else {
@@ -211,8 +287,10 @@ int plgb_sv_clone(const plgb_sv *src, plgb_sv **out) {
     return guard([&] {
         need(src, "source");
         need(out, "out");
+        flush_sv(const_cast<plgb_sv *>(src));
         auto h = std::make_unique<plgb_sv>();
         h->precision = src->precision;
+        h->lazy = src->lazy;
         if (src->precision == 128) {
             h->d = std::make_unique<StateVector<double>>(src->d->num_qubits());
             h->d->copy_from(*src->d);
@@ -228,7 +306,7 @@ int plgb_sv_destroy(plgb_sv *sv) {
     return guard([&] { delete sv; });
 }
 int plgb_sv_num_qubits(const plgb_sv *sv, int *out) {
-    return with_sv(const_cast<plgb_sv *>(sv), [&](auto &s) {
+    return with_sv_meta(const_cast<plgb_sv *>(sv), [&](auto &s) {
         need(out, "out");
         *out = s.num_qubits();
     });
@@ -241,7 +319,7 @@ int plgb_sv_precision(const plgb_sv *sv, int *out) {
     });
 }
 int plgb_sv_length(const plgb_sv *sv, uint64_t *out) {
-    return with_sv(const_cast<plgb_sv *>(sv), [&](auto &s) {
+    return with_sv_meta(const_cast<plgb_sv *>(sv), [&](auto &s) {
         need(out, "out");
         *out = s.length();
     });
@@ -294,7 +372,7 @@ int plgb_sv_get_state(const plgb_sv *sv, void *host_out, uint64_t len) {
 }
 int plgb_sv_apply_operation(plgb_sv *sv, const char *name, const int64_t *wires, int nw, int inverse,
                             const double *params, int np) {
-    return with_sv(sv, [&](auto &s) {
+    return with_sv_gate(sv, [&](auto &s) {
         need(name, "name");
         s.apply_operation(name, vec(wires, nw), inverse != 0, dvec(params, np));
     });
@@ -302,14 +380,14 @@ int plgb_sv_apply_operation(plgb_sv *sv, const char *name, const int64_t *wires,
 int plgb_sv_apply_controlled_operation(plgb_sv *sv, const char *name, const int64_t *cwires, const uint8_t *cvals,
                                        int ncw, const int64_t *wires, int nw, int inverse, const double *params,
                                        int np) {
-    return with_sv(sv, [&](auto &s) {
+    return with_sv_gate(sv, [&](auto &s) {
         need(name, "name");
         s.apply_controlled_operation(name, vec(cwires, ncw), bvec(cvals, ncw), vec(wires, nw), inverse != 0,
                                      dvec(params, np));
     });
 }
 int plgb_sv_apply_matrix(plgb_sv *sv, const double *matrix, const int64_t *wires, int nw, int inverse) {
-    return with_sv(sv, [&](auto &s) {
+    return with_sv_gate(sv, [&](auto &s) {
         PLGB_REQUIRE(nw >= 1 && nw <= 12, "Number of wires must be larger than 0 (and at most 12)");
         const auto m = cmat(matrix, size_t{1} << (2 * nw));
         s.apply_matrix(m.data(), vec(wires, nw), inverse != 0);
@@ -317,7 +395,7 @@ int plgb_sv_apply_matrix(plgb_sv *sv, const double *matrix, const int64_t *wires
 }
 int plgb_sv_apply_controlled_matrix(plgb_sv *sv, const double *matrix, const int64_t *cwires, const uint8_t *cvals,
                                     int ncw, const int64_t *wires, int nw, int inverse) {
-    return with_sv(sv, [&](auto &s) {
+    return with_sv_gate(sv, [&](auto &s) {
         PLGB_REQUIRE(nw >= 1 && nw <= 12, "Number of wires must be larger than 0 (and at most 12)");
         const auto m = cmat(matrix, size_t{1} << (2 * nw));
         s.apply_matrix(m.data(), vec(wires, nw), inverse != 0, vec(cwires, ncw), bvec(cvals, ncw));
@@ -484,6 +562,10 @@ int plgb_set_tile_variant(int precision, int occ) {
         return -1;
     }
     return set_tile_variant_occ(precision, occ != 0) ? 1 : 0;
+}
+int plgb_set_lazy_fusion(int on) { return g_lazy_fusion.exchange(on != 0 ? 1 : 0); }
+int plgb_sv_set_lazy(plgb_sv *sv, int on) {
+    return with_sv(sv, [&](auto &) { sv->lazy = on != 0; }); // runs the queue first
 }
 int plgb_set_c128_fp64_passes(int on) {
     const bool prev = c128_fp64_passes();

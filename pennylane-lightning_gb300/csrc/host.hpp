@@ -209,6 +209,21 @@ template <class T> class StateVector {
 
     // lowering: the primitives an operation expands to, without running them
     std::vector<Prim<T>> lower_op(const OpRec &op, bool inverse);
+    // the primitives any gate-applying call f() would run (validated exactly
+    // as when it runs), without running them
+    template <class F> std::vector<Prim<T>> capture_prims(F &&f) {
+        std::vector<Prim<T>> out;
+        auto *saved = sink_;
+        sink_ = &out;
+        try {
+            f();
+        } catch (...) {
+            sink_ = saved;
+            throw;
+        }
+        sink_ = saved;
+        return out;
+    }
     void run_prim(const Prim<T> &p);
     // fused application of a primitive list in shared-memory tile passes
     // (host_fusion.cpp); tile_bits = log2 of the amplitudes a CTA stages

@@ -84,6 +84,14 @@ def set_tile_variant(precision: int, occ: bool) -> bool:
     return bool(rc)
 
 
+def set_lazy_fusion(on: bool) -> bool:
+    """Default for new state vectors: per-gate calls are queued and run as
+    fused tile passes by the next call that reads or rewrites the state (on,
+    the default) or applied one at a time (off).  Returns the previous
+    default."""
+    return bool(lib().plgb_set_lazy_fusion(1 if on else 0))
+
+
 def set_c128_fp64_passes(on: bool) -> bool:
     """Fused complex128 passes in FP64 (True) or double-float arithmetic on
     the FP32 pipe (False, the default); returns the previous setting."""
@@ -178,6 +186,11 @@ class _StateVectorBase:
 
     def synchronize(self) -> None:
         call("plgb_sv_synchronize", self._h)
+
+    def set_lazy(self, on: bool) -> None:
+        """Queue per-gate calls and run them fused at the next state read
+        (on) or apply each gate at once (off); the queue runs first."""
+        call("plgb_sv_set_lazy", self._h, 1 if on else 0)
 
     def cuda_stream(self) -> int:
         """Address of the cudaStream_t this state vector's kernels run on."""

@@ -281,6 +281,24 @@ def gpu_arm(args) -> dict | None:
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     h2d = (1 << n) * 16 + sum(o.matrix.nbytes for o in circuit if o.matrix is not None)
     d2h = (1 << n) * 16
+    # the same through one binding call per gate (lightning.qubit's device
+    # call pattern; queued and fused by the binding's lazy fusion)
+    def per_gate_step():
+        sv.updateData(hin)
+        for o in circuit:
+            if o.matrix is not None:
+                sv.applyMatrix(o.matrix, o.wires, False)
+            else:
+                getattr(sv, o.name)(o.wires, False, o.params)
+        sv.getState(hout)
+
+    per_gate_step()  # warm-up
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        per_gate_step()
+    barrier()
+    pg_s = (time.perf_counter() - t0) / e2e_steps
     del sv
 
     res = {
@@ -297,7 +315,9 @@ def gpu_arm(args) -> dict | None:
                    "tile_bits": best_tb, "passes_per_step": passes,
                    "tuning_ms_per_step": {str(k): round(v, 1) for k, v in sorted(tune.items())}},
         "e2e": {"value": alg_bytes / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
+                "per_gate_calls": {"value": alg_bytes / pg_s / 1e9, "unit": UNIT, "ms_per_step": pg_s * 1e3,
+                                   "path": f"{len(circuit)} binding calls per step (one per gate), lazy fusion"}},
         "roofline": {"kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_source": f"{peak_src} hbm_gbs", "traffic": traffic,
                      "algorithmic_bytes_per_launch": pass_bytes, "avg_launch_ms": avg_launch_s * 1e3,

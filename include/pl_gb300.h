@@ -202,9 +202,12 @@ int plgb_set_tile_variant(int precision, int occ);
  * the gates applied one by one within the precision's tolerance.
  * plgb_set_lazy_fusion sets the default for handles created afterwards and
  * returns the previous default; plgb_sv_set_lazy switches one handle (its
- * queue runs first). */
+ * queue runs first).  Handles on fewer than plgb_set_lazy_min_qubits qubits
+ * (default 17) apply each gate at its call; the setter returns the previous
+ * value, or -1 for q < 1. */
 int plgb_set_lazy_fusion(int on);
 int plgb_sv_set_lazy(plgb_sv *sv, int on);
+int plgb_set_lazy_min_qubits(int q);
 /* Plan introspection (no device needed): the tile passes plgb_sv_apply_operations
  * would run for `ops` on num_qubits at precision / tile_bits, as a JSON array
  * with one object per pass (tile size, op counts, execution stages). */

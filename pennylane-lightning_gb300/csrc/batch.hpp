@@ -42,16 +42,6 @@ template <class T> struct BatchRedItem {
 
 constexpr u64 kBatchRedChunk = 4096; // amplitudes or pairs per reduction block
 
-// one merged-diagonal table to expand on the device (batch engine)
-struct DevRecipe {
-    void *dst;          // first entry of the table in the program arena
-    const TableFactor *fac;
-    int t, nfac;
-    u64 entry_begin;    // first global entry index of this table in the launch
-};
-// enc: 0 = complex64, 1 = complex128, 2 = complex128 as double-float pairs
-void launch_expand_tables(cudaStream_t s, const DevRecipe *recipes, int nrec, u64 total_entries, int enc);
-
 template <class T>
 void launch_tile_reg_batch(cudaStream_t s, int t, const BatchTileItem<T> *items, int nitems, u64 total_tiles,
                            int max_ops);

@@ -81,8 +81,13 @@ void need(const void *p, const char *what) {
 // primitives; the next call that reads or rewrites the state first runs the
 // queue, as fused register-tile passes when it holds at least
 // kLazyFuseMin primitives on a register of at least 2^9 amplitudes, else
-// primitive by primitive.
+// primitive by primitive.  Registers below g_lazy_min_qubits apply each gate
+// at its call: their kernels are shorter than a binding call, so launching
+// at once overlaps the caller's per-gate cost, while a fused program adds
+// its compilation to the read (measured on 12-16 qubit config-0 circuits;
+// from 17 qubits on the fused program is ahead).
 std::atomic<int> g_lazy_fusion{1};
+std::atomic<int> g_lazy_min_qubits{17};
 constexpr size_t kLazyFuseMin = 16;
 template <class T> void run_pending(StateVector<T> &s, std::vector<Prim<T>> &pend) {
     if (pend.empty()) {
@@ -132,7 +137,9 @@ template <class F> int with_sv_meta(plgb_sv *sv, F &&f) {
 template <class F> int with_sv_gate(plgb_sv *sv, F &&f) {
     return guard([&] {
         need(sv, "state vector");
-        if (!sv->lazy) {
+        const int nq = sv->precision == 128 ? sv->d->num_qubits() : sv->f->num_qubits();
+        if (!sv->lazy || nq < g_lazy_min_qubits.load()) {
+            flush_sv(sv);
             if (sv->precision == 128) {
                 f(*sv->d);
             } else {
@@ -564,6 +571,7 @@ int plgb_set_tile_variant(int precision, int occ) {
     return set_tile_variant_occ(precision, occ != 0) ? 1 : 0;
 }
 int plgb_set_lazy_fusion(int on) { return g_lazy_fusion.exchange(on != 0 ? 1 : 0); }
+int plgb_set_lazy_min_qubits(int q) { return q < 1 ? -1 : g_lazy_min_qubits.exchange(q); }
 int plgb_sv_set_lazy(plgb_sv *sv, int on) {
     return with_sv(sv, [&](auto &) { sv->lazy = on != 0; }); // runs the queue first
 }

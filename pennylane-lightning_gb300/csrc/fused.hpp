@@ -142,6 +142,15 @@ struct TableRecipe {
     int t;         // 2^t entries
     int fac_begin, nfac;
 };
+// one merged-diagonal table to expand on the device
+struct DevRecipe {
+    void *dst;          // first entry of the table in the program arena
+    const TableFactor *fac;
+    int t, nfac;
+    u64 entry_begin;    // first global entry index of this table in the launch
+};
+// enc: 0 = complex64, 1 = complex128, 2 = complex128 as double-float pairs
+void launch_expand_tables(cudaStream_t s, const DevRecipe *recipes, int nrec, u64 total_entries, int enc);
 
 // Register-tile kernel variant per precision (64 or 128): false = up to 255
 // registers per thread, true = at most 128 (twice the resident warps).

@@ -559,7 +559,10 @@ bool plan_stages(std::vector<TileOp<T>> &ops, const std::vector<DiagForm<T>> &fo
 template <class T>
 std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>> &in, int tile_bits, bool upload,
                                                bool recipes) {
-    PLGB_REQUIRE(!(upload && recipes), "fusion: table recipes are for host-side programs");
+    // Uploaded programs also describe their merged-diagonal tables by
+    // factors: expanding 2^t-entry tables on the host cost several times the
+    // rest of the compilation.
+    const bool use_recipes = recipes || upload;
     auto prog = std::make_shared<FusedProgram<T>>();
     prog->n = n;
     // a tile of 2^t amplitudes must fit the 200 KiB of shared memory the tile
@@ -653,6 +656,12 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
                             }
                         }
                         ok = nglob == 0 || (nloc == 0 && nglob <= 4) || (nglob == 1 && nloc == 1);
+                        if (!ok && __builtin_popcountll(pp.local | gbits) <= tmax && !(gbits & frozen)) {
+                            // no fused form across the boundary: make its bits local
+                            pp.local |= gbits;
+                            gbits = 0;
+                            ok = true;
+                        }
                         // one- and two-bit diagonals stay valid when a bit turns
                         // local; wider ones pin their global bits
                         if (ok && dd.bits.size() >= 3) {
@@ -842,7 +851,7 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
             }
             // recipe mode: the table's factors instead of its 2^t values
             // (possible while every multi-bit local factor has <= 4 bits)
-            bool as_recipe = recipes;
+            bool as_recipe = use_recipes;
             for (auto &dg : pend) {
                 bool all_local = true;
                 for (int b : dg.bits) {
@@ -1162,81 +1171,118 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
         return prog;
     }
 
-    // ---- upload
+    // ---- upload: one block [ops][forms][stages][recipes][df recipes][factors][tables],
+    // the first five in one copy; host-built table chunks copied in place;
+    // recipe tables expanded on the device
+    bool all_tile = !prog->segs.empty(), all_reg = !prog->segs.empty();
+    for (const auto &seg : prog->segs) {
+        all_reg = all_reg && seg.tile && seg.reg;
+        all_tile = all_tile && seg.tile;
+    }
+    const bool want_df = std::is_same_v<T, double> && all_tile;
+    const size_t nrec = prog->h_recipes.size();
+    const size_t nfac = prog->h_factors.size();
     const size_t b_ops = align_up(std::max<size_t>(1, ops.size()) * sizeof(TileOp<T>));
     const size_t b_forms = align_up(std::max<size_t>(1, forms.size()) * sizeof(DiagForm<T>));
-    const size_t b_tab = align_up(std::max<size_t>(1, tables.size()) * sizeof(cx<T>));
     const size_t b_st = align_up(std::max<size_t>(1, stages.size()) * sizeof(StageDesc));
-    prog->dev = dev_alloc(b_ops + b_forms + b_tab + b_st);
+    const size_t b_rec = align_up(std::max<size_t>(1, 2 * nrec) * sizeof(DevRecipe));
+    const size_t b_fac = align_up(std::max<size_t>(1, nfac) * sizeof(TableFactor));
+    const size_t b_tab = align_up(std::max<size_t>(1, prog->table_entries) * sizeof(cx<T>));
+    const size_t b_head = b_ops + b_forms + b_st + b_rec + b_fac;
+    prog->dev = dev_alloc(b_head + b_tab);
     char *base = static_cast<char *>(prog->dev);
     prog->d_ops = reinterpret_cast<TileOp<T> *>(base);
     prog->d_forms = reinterpret_cast<DiagForm<T> *>(base + b_ops);
-    prog->d_tables = reinterpret_cast<cx<T> *>(base + b_ops + b_forms);
-    prog->d_stages = reinterpret_cast<StageDesc *>(base + b_ops + b_forms + b_tab);
-    if (!stages.empty()) {
-        cuda_check(cudaMemcpy(prog->d_stages, stages.data(), stages.size() * sizeof(StageDesc),
+    prog->d_stages = reinterpret_cast<StageDesc *>(base + b_ops + b_forms);
+    auto *d_rec = reinterpret_cast<DevRecipe *>(base + b_ops + b_forms + b_st);
+    auto *d_fac = reinterpret_cast<TableFactor *>(base + b_ops + b_forms + b_st + b_rec);
+    prog->d_tables = reinterpret_cast<cx<T> *>(base + b_head);
+    char *bd = nullptr;
+    if (want_df) {
+        // the same tables re-encoded as double-float (same 16-byte layout)
+        static_assert(sizeof(TileOp<double>) == sizeof(TileOp<df>) && sizeof(DiagForm<double>) == sizeof(DiagForm<df>) &&
+                          sizeof(cx<double>) == sizeof(cx<df>),
+                      "double-float op tables must share the double layout");
+        prog->dev_df = dev_alloc(b_ops + b_forms + b_tab);
+        bd = static_cast<char *>(prog->dev_df);
+        prog->d_ops_df = bd;
+        prog->d_forms_df = bd + b_ops;
+        prog->d_tables_df = bd + b_ops + b_forms;
+    }
+    std::vector<char> head(b_head, 0);
+    auto put = [](char *dst, const auto &v) {
+        if (!v.empty()) {
+            std::memcpy(static_cast<void *>(dst), v.data(), v.size() * sizeof(v[0]));
+        }
+    };
+    put(head.data(), ops);
+    put(head.data() + b_ops, forms);
+    put(head.data() + b_ops + b_forms, stages);
+    u64 rec_entries = 0;
+    {
+        auto *hr = reinterpret_cast<DevRecipe *>(head.data() + b_ops + b_forms + b_st);
+        for (size_t i = 0; i < nrec; i++) {
+            const TableRecipe &r = prog->h_recipes[i];
+            DevRecipe d{};
+            d.dst = prog->d_tables + r.table_off;
+            d.fac = d_fac + r.fac_begin;
+            d.t = r.t;
+            d.nfac = r.nfac;
+            d.entry_begin = rec_entries;
+            rec_entries += u64{1} << r.t;
+            hr[i] = d;
+            if (want_df) {
+                d.dst = reinterpret_cast<cx<df> *>(bd + b_ops + b_forms) + r.table_off;
+                hr[nrec + i] = d;
+            }
+        }
+        put(head.data() + b_ops + b_forms + b_st + b_rec, prog->h_factors);
+    }
+    cuda_check(cudaMemcpy(base, head.data(), b_head, cudaMemcpyHostToDevice), "H2D");
+    for (const auto &ch : prog->h_table_chunks) {
+        cuda_check(cudaMemcpy(prog->d_tables + ch[0], tables.data() + ch[1], ch[2] * sizeof(cx<T>),
                               cudaMemcpyHostToDevice), "H2D");
     }
-    if (!ops.empty()) {
-        cuda_check(cudaMemcpy(prog->d_ops, ops.data(), ops.size() * sizeof(TileOp<T>), cudaMemcpyHostToDevice), "H2D");
-    }
-    if (!forms.empty()) {
-        cuda_check(cudaMemcpy(prog->d_forms, forms.data(), forms.size() * sizeof(DiagForm<T>), cudaMemcpyHostToDevice),
-                   "H2D");
-    }
-    if (!tables.empty()) {
-        cuda_check(cudaMemcpy(prog->d_tables, tables.data(), tables.size() * sizeof(cx<T>), cudaMemcpyHostToDevice),
-                   "H2D");
+    if (nrec) {
+        launch_expand_tables(nullptr, d_rec, static_cast<int>(nrec), rec_entries, std::is_same_v<T, float> ? 0 : 1);
     }
     if constexpr (std::is_same_v<T, double>) {
-        bool all_reg = !prog->segs.empty(), all_tile = !prog->segs.empty();
-        for (const auto &seg : prog->segs) {
-            all_reg = all_reg && seg.tile && seg.reg;
-            all_tile = all_tile && seg.tile;
-        }
         prog->df_reg = all_reg;
-        if (all_tile) {
-            // the same tables re-encoded as double-float (same 16-byte layout)
-            static_assert(sizeof(TileOp<double>) == sizeof(TileOp<df>) && sizeof(DiagForm<double>) == sizeof(DiagForm<df>),
-                          "double-float op tables must share the double layout");
+        if (want_df) {
             auto cdf = [](cx<double> v) { return cx<df>{df(v.x), df(v.y)}; };
-            std::vector<TileOp<df>> ops_df(ops.size());
+            std::vector<char> hd(b_ops + b_forms, 0);
+            auto *ops_df = reinterpret_cast<TileOp<df> *>(hd.data());
             for (size_t i = 0; i < ops.size(); i++) {
                 std::memcpy(static_cast<void *>(&ops_df[i]), &ops[i], sizeof(TileOp<double>));
                 for (int k = 0; k < 16; k++) {
                     ops_df[i].m[k] = cdf(ops[i].m[k]);
                 }
             }
-            std::vector<DiagForm<df>> forms_df(forms.size());
+            auto *forms_df = reinterpret_cast<DiagForm<df> *>(hd.data() + b_ops);
             for (size_t i = 0; i < forms.size(); i++) {
                 std::memcpy(static_cast<void *>(&forms_df[i]), &forms[i], sizeof(DiagForm<double>));
                 for (int k = 0; k < 16; k++) {
                     forms_df[i].tab[k] = cdf(forms[i].tab[k]);
                 }
             }
-            std::vector<cx<df>> tables_df(tables.size());
-            for (size_t i = 0; i < tables.size(); i++) {
-                tables_df[i] = cdf(tables[i]);
+            cuda_check(cudaMemcpy(bd, hd.data(), hd.size(), cudaMemcpyHostToDevice), "H2D");
+            auto *tdf = reinterpret_cast<cx<df> *>(bd + b_ops + b_forms);
+            for (const auto &ch : prog->h_table_chunks) {
+                std::vector<cx<df>> c(ch[2]);
+                for (size_t i = 0; i < ch[2]; i++) {
+                    c[i] = cdf(tables[ch[1] + i]);
+                }
+                cuda_check(cudaMemcpy(tdf + ch[0], c.data(), c.size() * sizeof(cx<df>), cudaMemcpyHostToDevice), "H2D");
             }
-            prog->dev_df = dev_alloc(b_ops + b_forms + b_tab);
-            char *bd = static_cast<char *>(prog->dev_df);
-            prog->d_ops_df = bd;
-            prog->d_forms_df = bd + b_ops;
-            prog->d_tables_df = bd + b_ops + b_forms;
-            if (!ops_df.empty()) {
-                cuda_check(cudaMemcpy(bd, ops_df.data(), ops_df.size() * sizeof(TileOp<df>), cudaMemcpyHostToDevice),
-                           "H2D");
-            }
-            if (!forms_df.empty()) {
-                cuda_check(cudaMemcpy(bd + b_ops, forms_df.data(), forms_df.size() * sizeof(DiagForm<df>),
-                                      cudaMemcpyHostToDevice), "H2D");
-            }
-            if (!tables_df.empty()) {
-                cuda_check(cudaMemcpy(bd + b_ops + b_forms, tables_df.data(), tables_df.size() * sizeof(cx<df>),
-                                      cudaMemcpyHostToDevice), "H2D");
+            if (nrec) {
+                launch_expand_tables(nullptr, d_rec + nrec, static_cast<int>(nrec), rec_entries, 2);
             }
             prog->df_ok = true;
         }
+    }
+    if (nrec) {
+        // the passes run on the register's own (non-blocking) stream
+        cuda_check(cudaStreamSynchronize(nullptr), "table expansion");
     }
     return prog;
 }

@@ -65,6 +65,7 @@ SIGNATURES = {
     "plgb_set_tile_variant": (C.c_int, [C.c_int, C.c_int]),
     "plgb_set_lazy_fusion": (C.c_int, [C.c_int]),
     "plgb_sv_set_lazy": (C.c_int, [VP, C.c_int]),
+    "plgb_set_lazy_min_qubits": (C.c_int, [C.c_int]),
     "plgb_meas_expval_sparse": (C.c_int, [VP, I64P, C.c_int64, I64P, DP, C.c_int64, DP]),
     "plgb_meas_expval_obs": (C.c_int, [VP, VP, DP]),
     "plgb_meas_var_obs": (C.c_int, [VP, VP, DP]),

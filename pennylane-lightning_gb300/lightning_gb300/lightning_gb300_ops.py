@@ -92,6 +92,15 @@ def set_lazy_fusion(on: bool) -> bool:
     return bool(lib().plgb_set_lazy_fusion(1 if on else 0))
 
 
+def set_lazy_min_qubits(q: int) -> int:
+    """Smallest register (in qubits) whose per-gate calls are queued for
+    lazy fusion; smaller ones apply each gate at its call.  Returns the
+    previous value."""
+    if int(q) < 1:
+        raise ValueError("min_qubits must be >= 1")
+    return int(lib().plgb_set_lazy_min_qubits(int(q)))
+
+
 def set_c128_fp64_passes(on: bool) -> bool:
     """Fused complex128 passes in FP64 (True) or double-float arithmetic on
     the FP32 pipe (False, the default); returns the previous setting."""

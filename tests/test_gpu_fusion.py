@@ -147,3 +147,36 @@ def test_c128_double_float_passes_match_fp64(ops_module):
             ops_module.set_c128_fp64_passes(prev)
     assert_close(outs[False], outs[True], np.complex128, scale=50, what="double-float vs FP64 passes")
     assert not np.array_equal(outs[False], outs[True])  # the two arithmetics did run
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+@pytest.mark.parametrize("fp64", [False, True])
+def test_wide_local_diagonals_fused(ops_module, oracle, dt, fp64):
+    # merged diagonals whose all-local factors span more than 4 bits (here
+    # multi-controlled phases) are tabulated on the host; narrower ones are
+    # expanded on the device from their factors: both kinds in one program,
+    # for both complex128 pass kinds
+    rng = np.random.default_rng(seed_of("wide-diag", dt.__name__, fp64))
+    n = 13
+    ops = []
+    for layer in range(6):
+        for q in range(n):
+            ops.append(dict(name=str(rng.choice(["RX", "RY", "RZ", "PhaseShift"])), wires=[q],
+                            params=[float(rng.uniform(0, 2 * np.pi))]))
+        k = int(rng.integers(5, 8))
+        w = [n - 9 + int(x) for x in rng.choice(9, size=k, replace=False)]  # amplitude bits 0-8: in the tile
+        ops.append(dict(name=str(rng.choice(["PhaseShift", "RZ"])), wires=w[:1], params=[float(rng.uniform(0, 6))],
+                        cwires=w[1:], cvals=[bool(x) for x in rng.integers(0, 2, size=k - 1)]))
+        ops.append(dict(name="MultiRZ", wires=w, params=[float(rng.uniform(0, 2 * np.pi))]))
+        ops.append(dict(name="IsingZZ", wires=[layer % n, (layer + 5) % n], params=[float(rng.uniform(0, 6))]))
+        ops.append(dict(name="CNOT", wires=[layer % n, (layer + 1) % n]))
+    st = rand_state(rng, n, dt)
+    sv = sv_class(ops_module, dt)(n)
+    sv.updateData(st)
+    prev = ops_module.set_c128_fp64_passes(fp64)
+    try:
+        sv.applyOperations(ops_struct(ops_module, dt, ops), 11)
+    finally:
+        ops_module.set_c128_fp64_passes(prev)
+    ref = oracle_apply(oracle, n, dt, st, ops)
+    assert_close(sv.state(), ref, dt, scale=50, what=f"wide diagonals fp64={fp64}")

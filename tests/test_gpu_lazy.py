@@ -11,6 +11,14 @@ from helpers import DTYPES, assert_close, meas_class, rand_unitary, seed_of, sv_
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(autouse=True)
+def queue_small_registers(ops_module):
+    # the queue normally starts at 17 qubits; these tests run it on small ones
+    prev = ops_module.set_lazy_min_qubits(1)
+    yield
+    ops_module.set_lazy_min_qubits(prev)
+
+
 def _circuit(rng, n, depth):
     ops = []
     for _ in range(depth):
@@ -90,3 +98,33 @@ def test_lazy_errors_surface_at_the_call(ops_module):
     sv.getState(a)
     ref.getState(b)
     assert_close(a, b, np.complex128)
+
+
+def test_small_registers_apply_at_the_call(ops_module):
+    # below the threshold a gate call launches its kernel at once; at or
+    # above it the call only queues
+    ops_module.set_lazy_min_qubits(17)
+    small = sv_class(ops_module, np.complex128)(12)
+    small.set_lazy(True)
+    k0 = ops_module.kernel_launches()
+    small.RX([3], False, [0.2])
+    assert ops_module.kernel_launches() > k0
+    big = sv_class(ops_module, np.complex128)(17)
+    big.set_lazy(True)
+    k1 = ops_module.kernel_launches()
+    big.RX([3], False, [0.2])
+    big.RY([4], False, [0.3])
+    assert ops_module.kernel_launches() == k1
+    big.synchronize()  # runs the queue
+    assert ops_module.kernel_launches() > k1
+    ref = sv_class(ops_module, np.complex128)(17)
+    ref.set_lazy(False)
+    ref.RX([3], False, [0.2])
+    ref.RY([4], False, [0.3])
+    a = np.zeros(1 << 17, dtype=np.complex128)
+    b = np.zeros(1 << 17, dtype=np.complex128)
+    big.getState(a)
+    ref.getState(b)
+    assert_close(a, b, np.complex128)
+    with pytest.raises(ValueError):
+        ops_module.set_lazy_min_qubits(0)

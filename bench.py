@@ -480,6 +480,15 @@ def serve_leg(seconds: float) -> dict:
     res = srv.run(packed, arrival, adjoint)
     out = {"metric": "config4 requests/s", **res.summary(), "window_s": seconds,
            "offered_per_s": packed.num_circuits / seconds}
+    # the same stream shape offered below capacity: latency without a backlog
+    cap = out["throughput_per_s"]
+    if cap > 0:
+        rate = 0.7 * cap
+        p2, a2, adj2 = config4_packed(rate=rate, duration=seconds, seed=1005)
+        r2 = srv.run(p2, a2, adj2).summary()
+        out["below_capacity"] = {"offered_per_s": p2.num_circuits / seconds, "requests": r2["requests"],
+                                 "throughput_per_s": r2["throughput_per_s"], "p50_ms": r2["p50_ms"],
+                                 "p99_ms": r2["p99_ms"], "rate": "0.7 x the measured throughput above"}
     names = {v: k for k, v in gate_codes().items()}
     srv.packed, srv.adjoint = packed, adjoint
     lat = []

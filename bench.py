@@ -403,7 +403,11 @@ def batched_leg(ops, prec: int, plain_every: int = 32) -> dict:
     st = eng.stats()
     lat = np.asarray(st["wave_done_ms"])[np.asarray(st["wave_of"], int)]
     sample = list(range(0, packed.num_circuits, plain_every))
-    _plain_circuit(ops, packed, sample[0], names, prec)
+    # warm-up of both per-call paths on the widest sampled circuit (first
+    # launches of the fused kernels, pools)
+    widest = max(sample, key=lambda r: int(packed.num_qubits[r]))
+    _plain_circuit(ops, packed, widest, names, prec)
+    _plain_circuit(ops, packed, widest, names, prec, lazy=True)
     plat = []
     t = time.perf_counter()
     for r in sample:

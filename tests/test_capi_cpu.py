@@ -65,3 +65,19 @@ def test_invalid_arguments_are_rejected_on_the_host(ops_module):
                                                   ops_module.observables.NamedObsC128("PauliZ", [0])])
     with pytest.raises(RuntimeError, match="unknown observable"):
         ops_module.observables.NamedObsC128("NotAnObservable", [0])
+
+
+def test_process_wide_settings_roundtrip(ops_module):
+    # lazy fusion default, its qubit threshold and the tile variant are host
+    # settings: set, read back through the previous value, restore
+    from lightning_gb300 import _capi
+
+    prev = ops_module.set_lazy_min_qubits(20)
+    assert ops_module.set_lazy_min_qubits(prev) == 20
+    assert _capi.lib().plgb_set_lazy_min_qubits(0) == -1  # rejected, unchanged
+    assert ops_module.set_lazy_min_qubits(prev) == prev
+    with pytest.raises(ValueError):
+        ops_module.set_lazy_min_qubits(0)
+    on = ops_module.set_lazy_fusion(False)
+    assert ops_module.set_lazy_fusion(on) is False
+    assert _capi.lib().plgb_set_tile_variant(32, 1) == -1  # no such precision

@@ -118,6 +118,34 @@ template <class F> int with_sv(void *h, F &&f) {
     });
 }
 
+template <class T>
+std::vector<orc::Op<T>> parse_ops(int nops, const char **names, const double *params, const int *nparams,
+                                  const int64_t *wires, const int *nwires, const uint8_t *inverses,
+                                  const double *mats, const int64_t *mat_sizes, const int64_t *cwires,
+                                  const int *ncwires, const uint8_t *cvals) {
+    std::vector<orc::Op<T>> ops(static_cast<size_t>(nops));
+    size_t ip = 0, iw = 0, im = 0, ic = 0;
+    for (int k = 0; k < nops; k++) {
+        auto &op = ops[static_cast<size_t>(k)];
+        op.name = names[k];
+        for (int i = 0; i < nparams[k]; i++) {
+            op.params.push_back(static_cast<T>(params[ip++]));
+        }
+        for (int i = 0; i < nwires[k]; i++) {
+            op.wires.push_back(static_cast<size_t>(wires[iw++]));
+        }
+        op.inverse = inverses[k] != 0;
+        op.matrix = cvec<T>(mats + 2 * im, static_cast<size_t>(mat_sizes[k]));
+        im += static_cast<size_t>(mat_sizes[k]);
+        for (int i = 0; i < ncwires[k]; i++) {
+            op.cwires.push_back(static_cast<size_t>(cwires[ic]));
+            op.cvals.push_back(cvals[ic] != 0);
+            ic++;
+        }
+    }
+    return ops;
+}
+
 } // namespace
 
 extern "C" {
@@ -327,26 +355,8 @@ int orc_adjoint(void *h, int nops, const char **names, const double *params,
                 int apply_ops, double *jac_out) {
     return with_sv(h, [&](auto &sv) {
         using T = typename std::decay_t<decltype(sv.data[0])>::value_type;
-        std::vector<orc::Op<T>> ops(static_cast<size_t>(nops));
-        size_t ip = 0, iw = 0, im = 0, ic = 0;
-        for (int k = 0; k < nops; k++) {
-            auto &op = ops[static_cast<size_t>(k)];
-            op.name = names[k];
-            for (int i = 0; i < nparams[k]; i++) {
-                op.params.push_back(static_cast<T>(params[ip++]));
-            }
-            for (int i = 0; i < nwires[k]; i++) {
-                op.wires.push_back(static_cast<size_t>(wires[iw++]));
-            }
-            op.inverse = inverses[k] != 0;
-            op.matrix = cvec<T>(mats + 2 * im, static_cast<size_t>(mat_sizes[k]));
-            im += static_cast<size_t>(mat_sizes[k]);
-            for (int i = 0; i < ncwires[k]; i++) {
-                op.cwires.push_back(static_cast<size_t>(cwires[ic]));
-                op.cvals.push_back(cvals[ic] != 0);
-                ic++;
-            }
-        }
+        const auto ops = parse_ops<T>(nops, names, params, nparams, wires, nwires, inverses, mats,
+                                      mat_sizes, cwires, ncwires, cvals);
         std::vector<orc::ObsPtr<T>> obs;
         for (int i = 0; i < nobs; i++) {
             obs.push_back(parse_obs<T>(obs_specs[i], cdata, idata));
@@ -356,6 +366,25 @@ int orc_adjoint(void *h, int nops, const char **names, const double *params,
         orc::adjoint_jacobian<T>(jac, sv, ops, obs, tp, apply_ops != 0);
         for (size_t i = 0; i < jac.size(); i++) {
             jac_out[i] = static_cast<double>(jac[i]);
+        }
+    });
+}
+int orc_vjp(void *h, int nops, const char **names, const double *params,
+            const int *nparams, const int64_t *wires, const int *nwires,
+            const uint8_t *inverses, const double *mats,
+            const int64_t *mat_sizes, const int64_t *cwires,
+            const int *ncwires, const uint8_t *cvals, const double *dy,
+            const int64_t *trainable, int ntp, int apply_ops, double *out) {
+    return with_sv(h, [&](auto &sv) {
+        using T = typename std::decay_t<decltype(sv.data[0])>::value_type;
+        const auto ops = parse_ops<T>(nops, names, params, nparams, wires, nwires, inverses, mats,
+                                      mat_sizes, cwires, ncwires, cvals);
+        const std::vector<std::complex<T>> cot = cvec<T>(dy, sv.len());
+        std::vector<std::complex<T>> w;
+        orc::vjp<T>(w, sv, ops, cot, vec(trainable, ntp), apply_ops != 0);
+        for (size_t i = 0; i < w.size(); i++) {
+            out[2 * i] = static_cast<double>(w[i].real());
+            out[2 * i + 1] = static_cast<double>(w[i].imag());
         }
     });
 }

@@ -1444,4 +1444,66 @@ void adjoint_jacobian(std::vector<T> &jac, const StateVec<T> &state,
     jac.swap(t);
 }
 
+// VectorJacobianProduct.hpp:79-160 (lightning_qubit/algorithms): w_j =
+// <dy| d psi / d theta_j>.  The cotangent mu = dy and lambda = psi are swept
+// back together (U^dagger on both, last op first); at a trainable
+// parameter's op, with G its generator and s its scale (negated for an
+// inverse op), w = i s <G mu | lambda>.
+template <class T>
+void vjp(std::vector<C<T>> &out, const StateVec<T> &state,
+         const std::vector<Op<T>> &ops, const std::vector<C<T>> &dy,
+         const std::vector<size_t> &tp, bool apply_ops) {
+    ORC_CHECK(dy.size() == state.len(), "dy must have the state's length");
+    const size_t ntp = tp.size();
+    out.assign(ntp, C<T>{0, 0});
+    if (ntp == 0) {
+        return;
+    }
+    size_t num_param_ops = 0;
+    for (const auto &op : ops) {
+        num_param_ops += op.params.empty() ? 0 : 1;
+    }
+    StateVec<T> lambda(state);
+    if (apply_ops) {
+        for (const auto &op : ops) {
+            apply_op(lambda, op, op.inverse);
+        }
+    }
+    StateVec<T> mu(state.n);
+    mu.data = dy;
+    StateVec<T> gmu(state.n);
+    size_t slot = ntp - 1;
+    size_t cur = num_param_ops - 1;
+    auto tp_it = tp.rbegin();
+    for (long op_idx = static_cast<long>(ops.size()) - 1; op_idx >= 0; op_idx--) {
+        const auto &op = ops[static_cast<size_t>(op_idx)];
+        ORC_CHECK(op.params.size() <= 1,
+                  "The operation is not supported using the adjoint "
+                  "differentiation method");
+        if (op.name == "StatePrep" || op.name == "BasisState") {
+            continue;
+        }
+        if (tp_it == tp.rend()) {
+            break;
+        }
+        if (!op.params.empty()) {
+            if (cur == *tp_it) {
+                gmu.data = mu.data;
+                const T scale =
+                    apply_generator<T>(gmu.ptr(), gmu.n, op.name, op.cwires,
+                                       op.cvals, op.wires) *
+                    (op.inverse ? -1 : 1);
+                out[slot] = C<T>{0, scale} *
+                            inner_prod_c(gmu.data.data(), lambda.data.data(),
+                                         lambda.len());
+                slot--;
+                ++tp_it;
+            }
+            cur--;
+        }
+        apply_op(lambda, op, !op.inverse);
+        apply_op(mu, op, !op.inverse);
+    }
+}
+
 } // namespace orc

@@ -101,6 +101,16 @@ int ORC_FN(adjoint)(void *sv, int nops, const char **names,
                     const char **obs_specs, const double *cdata,
                     const int64_t *idata, const int64_t *trainable, int ntp,
                     int apply_ops, double *jac_out);
+/* VectorJacobianProduct (lightning_qubit/algorithms/VectorJacobianProduct.hpp:79):
+ * w_j = <dy| d psi / d theta_j> for the trainable parameters, complex
+ * (re, im) pairs in out; dy is 2^n interleaved (re, im) doubles. */
+int ORC_FN(vjp)(void *sv, int nops, const char **names, const double *params,
+                const int *nparams, const int64_t *wires, const int *nwires,
+                const uint8_t *inverses, const double *mats,
+                const int64_t *mat_sizes, const int64_t *cwires,
+                const int *ncwires, const uint8_t *cvals, const double *dy,
+                const int64_t *trainable, int ntp, int apply_ops,
+                double *out);
 int ORC_FN(num_threads)(void);
 
 #ifdef __cplusplus

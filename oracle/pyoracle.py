@@ -72,6 +72,8 @@ def _load(kind: str) -> C.CDLL:
         "adjoint": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_char_p), _DP, _IP, _I64P, _IP, _U8P, _DP, _I64P,
                               _I64P, _IP, _U8P, C.c_int, C.POINTER(C.c_char_p), _DP, _I64P, _I64P, C.c_int,
                               C.c_int, _DP]),
+        "vjp": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_char_p), _DP, _IP, _I64P, _IP, _U8P, _DP, _I64P,
+                          _I64P, _IP, _U8P, _DP, _I64P, C.c_int, C.c_int, _DP]),
         "num_threads": (C.c_int, []),
     }
     for name, (res, args) in sig.items():
@@ -299,6 +301,35 @@ class OracleSV:
         out = np.empty(max(1, shots * self.n), dtype=np.int64)
         self.o._check(self.o._fn("mcmc_samples")(self.h, kernel.encode(), burnin, shots, seed, _p(out, _I64P)))
         return out[: shots * self.n].reshape(shots, self.n)
+
+    @staticmethod
+    def _ops_arrays(ops):
+        names = (C.c_char_p * max(1, len(ops)))(*[o["name"].encode() for o in ops])
+        params = _f64([p for o in ops for p in o.get("params", ())] or [0.0])
+        nparams = np.array([len(o.get("params", ())) for o in ops] or [0], dtype=np.int32)
+        wires = _i64([w for o in ops for w in o["wires"]] or [0])
+        nwires = np.array([len(o["wires"]) for o in ops] or [0], dtype=np.int32)
+        inv = _u8([int(o.get("inverse", False)) for o in ops] or [0])
+        mats = [(_c128(o["matrix"]) if o.get("matrix") is not None else np.zeros(0, np.complex128)) for o in ops]
+        mat_sizes = _i64([m.size for m in mats] or [0])
+        mflat = np.ascontiguousarray((np.concatenate(mats) if sum(m.size for m in mats) else np.zeros(1, np.complex128)).view(np.float64))
+        cw = _i64([w for o in ops for w in o.get("cwires", ())] or [0])
+        ncw = np.array([len(o.get("cwires", ())) for o in ops] or [0], dtype=np.int32)
+        cv = _u8([int(v) for o in ops for v in o.get("cvals", ())] or [0])
+        return (names, _p(params, _DP), nparams.ctypes.data_as(_IP), _p(wires, _I64P), nwires.ctypes.data_as(_IP),
+                _p(inv, _U8P), _p(mflat, _DP), _p(mat_sizes, _I64P), _p(cw, _I64P), ncw.ctypes.data_as(_IP),
+                _p(cv, _U8P)), (params, nparams, wires, nwires, inv, mflat, mat_sizes, cw, ncw, cv)
+
+    def vjp(self, ops, dy, trainable, apply_ops=False) -> np.ndarray:
+        """VectorJacobianProduct: w_j = <dy| d psi / d theta_j> (complex), ops as for adjoint."""
+        args, keep = self._ops_arrays(ops)
+        d = np.ascontiguousarray(np.asarray(dy, dtype=np.complex128).reshape(-1))
+        tp = _i64(trainable or [0])
+        out = np.zeros(2 * max(1, len(trainable)))
+        self.o._check(self.o._fn("vjp")(self.h, len(ops), *args, _p(d.view(np.float64), _DP), _p(tp, _I64P),
+                                        len(trainable), int(apply_ops), _p(out, _DP)))
+        del keep
+        return out[: 2 * len(trainable)].view(np.complex128).copy()
 
     def adjoint(self, ops, obs_specs, trainable, od: ObsData | None = None, apply_ops=False) -> np.ndarray:
         """ops: list of dicts {name, params, wires, inverse, matrix, cwires, cvals}."""

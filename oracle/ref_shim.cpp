@@ -12,6 +12,7 @@
 //   Measurements                  .../lightning_qubit/measurements/MeasurementsLQubit.hpp
 //   NamedObs/HermitianObs/...     .../lightning_qubit/observables/ObservablesLQubit.hpp
 //   AdjointJacobian               .../lightning_qubit/algorithms/AdjointJacobianLQubit.hpp
+//   VectorJacobianProduct         .../lightning_qubit/algorithms/VectorJacobianProduct.hpp
 //   OpsData / JacobianData        pennylane_lightning/core/algorithms/JacobianData.hpp
 #define ORC_PREFIX ref_
 #include "oracle_api.h"
@@ -22,6 +23,7 @@
 #include "MeasurementsLQubit.hpp"
 #include "ObservablesLQubit.hpp"
 #include "StateVectorLQubitManaged.hpp"
+#include "VectorJacobianProduct.hpp"
 
 #include <cstring>
 #include <numeric>
@@ -131,6 +133,46 @@ auto parse_obs(const char *spec, const double *cdata, const int64_t *idata) {
     Builder<T> b;
     orc_spec::Parser<Builder<T>> p(b, spec, cdata, idata);
     return p.parse();
+}
+
+template <class SVT>
+OpsData<SVT> make_ops(int nops, const char **names, const double *params, const int *nparams,
+                      const int64_t *wires, const int *nwires, const uint8_t *inverses, const double *mats,
+                      const int64_t *mat_sizes, const int64_t *cwires, const int *ncwires, const uint8_t *cvals) {
+    using T = typename SVT::PrecisionT;
+    std::vector<std::string> on;
+    std::vector<std::vector<T>> op;
+    std::vector<std::vector<std::size_t>> ow, ocw;
+    std::vector<bool> oi;
+    std::vector<std::vector<std::complex<T>>> om;
+    std::vector<std::vector<bool>> ocv;
+    std::size_t ip = 0, iw = 0, im = 0, ic = 0;
+    for (int k = 0; k < nops; k++) {
+        on.emplace_back(names[k]);
+        std::vector<T> p;
+        for (int i = 0; i < nparams[k]; i++) {
+            p.push_back(static_cast<T>(params[ip++]));
+        }
+        op.push_back(p);
+        std::vector<std::size_t> w;
+        for (int i = 0; i < nwires[k]; i++) {
+            w.push_back(static_cast<std::size_t>(wires[iw++]));
+        }
+        ow.push_back(w);
+        oi.push_back(inverses[k] != 0);
+        om.push_back(cvec<T>(mats + 2 * im, static_cast<std::size_t>(mat_sizes[k])));
+        im += static_cast<std::size_t>(mat_sizes[k]);
+        std::vector<std::size_t> cw;
+        std::vector<bool> cv;
+        for (int i = 0; i < ncwires[k]; i++) {
+            cw.push_back(static_cast<std::size_t>(cwires[ic]));
+            cv.push_back(cvals[ic] != 0);
+            ic++;
+        }
+        ocw.push_back(cw);
+        ocv.push_back(cv);
+    }
+    return OpsData<SVT>{on, op, ow, oi, om, ocw, ocv};
 }
 
 } // namespace
@@ -353,39 +395,8 @@ int ref_adjoint(void *h, int nops, const char **names, const double *params,
     return with_sv(h, [&](auto &sv) {
         using SVT = std::decay_t<decltype(sv)>;
         using T = typename SVT::PrecisionT;
-        std::vector<std::string> on;
-        std::vector<std::vector<T>> op;
-        std::vector<std::vector<std::size_t>> ow, ocw;
-        std::vector<bool> oi;
-        std::vector<std::vector<std::complex<T>>> om;
-        std::vector<std::vector<bool>> ocv;
-        std::size_t ip = 0, iw = 0, im = 0, ic = 0;
-        for (int k = 0; k < nops; k++) {
-            on.emplace_back(names[k]);
-            std::vector<T> p;
-            for (int i = 0; i < nparams[k]; i++) {
-                p.push_back(static_cast<T>(params[ip++]));
-            }
-            op.push_back(p);
-            std::vector<std::size_t> w;
-            for (int i = 0; i < nwires[k]; i++) {
-                w.push_back(static_cast<std::size_t>(wires[iw++]));
-            }
-            ow.push_back(w);
-            oi.push_back(inverses[k] != 0);
-            om.push_back(cvec<T>(mats + 2 * im, static_cast<std::size_t>(mat_sizes[k])));
-            im += static_cast<std::size_t>(mat_sizes[k]);
-            std::vector<std::size_t> cw;
-            std::vector<bool> cv;
-            for (int i = 0; i < ncwires[k]; i++) {
-                cw.push_back(static_cast<std::size_t>(cwires[ic]));
-                cv.push_back(cvals[ic] != 0);
-                ic++;
-            }
-            ocw.push_back(cw);
-            ocv.push_back(cv);
-        }
-        OpsData<SVT> ops{on, op, ow, oi, om, ocw, ocv};
+        const OpsData<SVT> ops = make_ops<SVT>(nops, names, params, nparams, wires, nwires, inverses, mats,
+                                               mat_sizes, cwires, ncwires, cvals);
         std::vector<std::shared_ptr<Observable<SVT>>> obs;
         for (int i = 0; i < nobs; i++) {
             obs.push_back(parse_obs<T>(obs_specs[i], cdata, idata));
@@ -398,6 +409,29 @@ int ref_adjoint(void *h, int nops, const char **names, const double *params,
         adj.adjointJacobian(std::span{jac}, jd, sv, apply_ops != 0);
         for (std::size_t i = 0; i < jac.size(); i++) {
             jac_out[i] = static_cast<double>(jac[i]);
+        }
+    });
+}
+int ref_vjp(void *h, int nops, const char **names, const double *params,
+            const int *nparams, const int64_t *wires, const int *nwires,
+            const uint8_t *inverses, const double *mats,
+            const int64_t *mat_sizes, const int64_t *cwires,
+            const int *ncwires, const uint8_t *cvals, const double *dy,
+            const int64_t *trainable, int ntp, int apply_ops, double *out) {
+    return with_sv(h, [&](auto &sv) {
+        using SVT = std::decay_t<decltype(sv)>;
+        using T = typename SVT::PrecisionT;
+        const OpsData<SVT> ops = make_ops<SVT>(nops, names, params, nparams, wires, nwires, inverses, mats,
+                                               mat_sizes, cwires, ncwires, cvals);
+        const std::vector<std::complex<T>> cot = cvec<T>(dy, sv.getLength());
+        std::vector<std::size_t> tp = vec(trainable, ntp);
+        std::vector<std::complex<T>> w(tp.size());
+        JacobianData<SVT> jd{ops.getTotalNumParams(), sv.getLength(), sv.getData(), {}, ops, tp};
+        VectorJacobianProduct<SVT> v;
+        v(std::span{w}, jd, std::span<const std::complex<T>>{cot}, apply_ops != 0);
+        for (std::size_t i = 0; i < w.size(); i++) {
+            out[2 * i] = static_cast<double>(w[i].real());
+            out[2 * i + 1] = static_cast<double>(w[i].imag());
         }
     });
 }

@@ -87,3 +87,46 @@ def test_vjp_subset_and_errors(ops_module):
     assert ops_module.algorithms.VectorJacobianProductC128()(sv, S, dy, []).shape == (0,)
     with pytest.raises(ops_module.LightningException):
         ops_module.algorithms.VectorJacobianProductC128()(sv, S, np.ones(4), [0])
+
+
+def _oracle_circuit(rng, n):
+    # plain, two-wire, multi-wire and controlled generators, some inverted
+    ops = []
+    for layer in range(3):
+        for q in range(n):
+            ops.append(dict(name=str(rng.choice(["RX", "RY", "RZ", "PhaseShift"])), wires=[q],
+                            params=[float(rng.uniform(0, 2 * np.pi))], inverse=bool(rng.integers(0, 2))))
+        ops.append(dict(name="CNOT", wires=[layer % n, (layer + 1) % n], params=[]))
+        ops.append(dict(name="IsingXX", wires=[0, n - 1], params=[float(rng.uniform(0, 6))]))
+        ops.append(dict(name="CRY", wires=[1, 2], params=[float(rng.uniform(0, 6))], inverse=True))
+        ops.append(dict(name="MultiRZ", wires=[0, 2, 3], params=[float(rng.uniform(0, 6))]))
+        ops.append(dict(name="RX", wires=[3], params=[float(rng.uniform(0, 6))], cwires=[0, 4], cvals=[True, False]))
+    return ops
+
+
+@pytest.mark.parametrize("prec,tol", [(128, 1e-12), (64, 1e-5)])
+def test_vjp_matches_oracle(ops_module, oracle, prec, tol):
+    # against the oracle's restatement of VectorJacobianProduct.hpp:79-160,
+    # itself pinned to the reference's build
+    from helpers import rand_state
+
+    rng = np.random.default_rng(seed_of("vjp-oracle", prec))
+    n = 5
+    ops = _oracle_circuit(rng, n)
+    dt = np.complex128 if prec == 128 else np.complex64
+    s = "C128" if prec == 128 else "C64"
+    OS = getattr(ops_module, "OpsStruct" + s)
+    S = OS([o["name"] for o in ops], [o["params"] for o in ops], [o["wires"] for o in ops],
+           [o.get("inverse", False) for o in ops], [None] * len(ops), [o.get("cwires", []) for o in ops],
+           [o.get("cvals", []) for o in ops])
+    sv = getattr(ops_module, "StateVector" + s)(n)
+    for o in ops:
+        sv.applyOperation(o["name"], o["wires"], o.get("inverse", False), o["params"], o.get("cwires", ()),
+                          o.get("cvals", ()))
+    npar = sum(1 for o in ops if o["params"])
+    tp = sorted(int(x) for x in rng.choice(npar, size=npar // 2, replace=False))
+    dy = rand_state(rng, n, dt)
+    w = getattr(ops_module.algorithms, "VectorJacobianProduct" + s)()(sv, S, dy, tp)
+    ref = oracle.sv(n, dt).vjp(ops, dy.astype(np.complex128), tp, apply_ops=True)
+    assert np.asarray(w).shape == (len(tp),)
+    assert np.max(np.abs(np.asarray(w) - ref)) <= 50 * tol * max(1.0, np.max(np.abs(ref)))

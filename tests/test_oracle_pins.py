@@ -239,3 +239,61 @@ def test_restatement_vs_reference_adjoint(oracle):
     ja = oracle.sv(6).adjoint(ops, specs, tp, apply_ops=True)
     jb = ref.sv(6).adjoint(ops, specs, tp, apply_ops=True)
     assert np.max(np.abs(ja - jb)) < 1e-11
+
+
+def _vjp_circuit(rng, n):
+    # parametric gates of several generator kinds (plain, two-wire, multi-wire,
+    # controlled by name and by control wires), some inverted, plus CNOTs
+    ops = []
+    for layer in range(3):
+        for q in range(n):
+            name = str(rng.choice(["RX", "RY", "RZ", "PhaseShift"]))
+            ops.append(dict(name=name, wires=[q], params=[float(rng.uniform(0, 2 * np.pi))],
+                            inverse=bool(rng.integers(0, 2))))
+        ops.append(dict(name="CNOT", wires=[layer % n, (layer + 1) % n]))
+        ops.append(dict(name="IsingXX", wires=[0, n - 1], params=[float(rng.uniform(0, 6))]))
+        ops.append(dict(name="CRY", wires=[1, 2], params=[float(rng.uniform(0, 6))], inverse=True))
+        ops.append(dict(name="MultiRZ", wires=[0, 2, 3], params=[float(rng.uniform(0, 6))]))
+        ops.append(dict(name="RX", wires=[3], params=[float(rng.uniform(0, 6))], cwires=[0, 4], cvals=[True, False]))
+    return ops
+
+
+@pytest.mark.parametrize("dt,tol", [(np.complex128, 1e-12), (np.complex64, 1e-5)])
+def test_restatement_vs_reference_vjp(oracle, dt, tol):
+    ref = _ref()
+    rng = np.random.default_rng(seed_of("vjp-pin", dt.__name__))
+    n = 5
+    ops = _vjp_circuit(rng, n)
+    npar = sum(1 for o in ops if o.get("params"))
+    tp = sorted(int(x) for x in rng.choice(npar, size=npar // 2, replace=False))
+    dy = rand_state(rng, n, np.complex128)
+    wa = oracle.sv(n, dt).vjp(ops, dy, tp, apply_ops=True)
+    wb = ref.sv(n, dt).vjp(ops, dy, tp, apply_ops=True)
+    assert wa.shape == (len(tp),)
+    assert np.max(np.abs(wa - wb)) < tol * max(1.0, np.max(np.abs(wb)))
+
+
+def test_vjp_restatement_matches_finite_differences(oracle):
+    # w_j = <dy| d psi / d theta_j>: central differences of the state (c128)
+    rng = np.random.default_rng(seed_of("vjp-fd"))
+    n = 5
+    ops = _vjp_circuit(rng, n)
+    dy = rand_state(rng, n, np.complex128)
+    pidx = [i for i, o in enumerate(ops) if o.get("params")]
+    tp = [0, 3, 7, len(pidx) - 1]
+    w = oracle.sv(n, np.complex128).vjp(ops, dy, tp, apply_ops=True)
+
+    def state(shift_op, h):
+        o2 = [dict(o) for o in ops]
+        if shift_op is not None:
+            o2[shift_op]["params"] = [o2[shift_op]["params"][0] + h]
+        s = oracle.sv(n, np.complex128)
+        for o in o2:
+            s.apply(o["name"], o["wires"], o.get("inverse", False), o.get("params", ()), o.get("cwires", ()),
+                    o.get("cvals", ()))
+        return s.state()
+
+    h = 1e-5
+    for k, j in enumerate(tp):
+        d = (state(pidx[j], h) - state(pidx[j], -h)) / (2 * h)
+        assert abs(np.vdot(dy, d) - w[k]) < 1e-8

@@ -156,6 +156,13 @@ def main() -> int:
                                            apply_ops=True)
     arrays["config3_small_jac"] = jac[0]
     meta["config3_small"] = {"n": 8, "layers": 3, "seed": 1003, "nterms": 20}
+    # VectorJacobianProduct on the same circuit: seeded cotangent, every other parameter
+    dy = rand_state(np.random.default_rng(1005), 8, np.complex128)
+    tpv = tp[::2]
+    arrays["config3_small_vjp_dy"] = dy
+    arrays["config3_small_vjp"] = ref.sv(8, np.complex128).vjp([o.as_dict() for o in circuit], dy, tpv,
+                                                               apply_ops=True)
+    meta["config3_small_vjp"] = {"dy_seed": 1005, "trainable": "every other parameter"}
 
     arrays["meta"] = np.array(json.dumps(meta))
     np.savez_compressed(OUT, **arrays)

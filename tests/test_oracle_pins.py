@@ -297,3 +297,15 @@ def test_vjp_restatement_matches_finite_differences(oracle):
     for k, j in enumerate(tp):
         d = (state(pidx[j], h) - state(pidx[j], -h)) / (2 * h)
         assert abs(np.vdot(dy, d) - w[k]) < 1e-8
+
+
+def test_golden_vjp_config3_small(oracle, golden):
+    # the reference's VectorJacobianProduct on the reduced config-3 circuit
+    from lightning_gb300.workloads import config3
+
+    g, _ = golden
+    circuit, _ = config3(8, 3, seed=1003, nterms=20)
+    tp = list(range(sum(1 for op in circuit if op.params)))[::2]
+    w = oracle.sv(8, np.complex128).vjp([op.as_dict() for op in circuit], g["config3_small_vjp_dy"], tp,
+                                        apply_ops=True)
+    assert np.max(np.abs(w - g["config3_small_vjp"])) < 1e-12

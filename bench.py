@@ -1,17 +1,20 @@
 #!/usr/bin/env python3
-"""Benchmark: gate-application bandwidth of the 30-qubit complex128 random
-circuit (20 cycles of a Haar SU(2) on every qubit followed by CZ on 15
-disjoint pairs), the single-large-circuit configuration the GB300 target is
-quoted on.
+"""Benchmark: gate application on the 30-qubit complex128 random circuit (20
+cycles of a Haar SU(2) on every qubit followed by CZ on 15 disjoint pairs),
+the single-large-circuit configuration the GB300 target is quoted on.
 
 A *step* applies the whole circuit (600 SU(2) + 300 CZ gates) to a state that
-is resident in HBM, through StateVector.applyOperations: either one kernel per
-gate or fused shared-memory tile passes, whichever the warm-up measured
-faster.  ``value`` is the unfused algorithmic traffic of the
-step (sum over gates of 2 f N S, f = fraction of amplitudes a gate changes)
-divided by the step time, in GB/s; ``e2e`` is the same metric through the
-public binding with the state copied in from pinned host memory and back out
-every step.  The 16 GiB state is far larger than L2, so no flush is needed.
+is resident in HBM, through StateVector.applyOperations as fused tile passes
+computing in FP64 (the reference's arithmetic).  ``value`` counts the work
+the circuit defines, independent of how it is executed: amplitude updates,
+sum over gates of f * 2^n (f = fraction of amplitudes a gate changes: 1 for
+SU(2), 1/4 for CZ), per second, in units of 1e9.  The CPU reference arm
+counts the same units, so the two are directly comparable.  ``roofline``
+gives the bytes the fused passes actually move (2 N S per pass) against the
+measured HBM peak, ``fusion_gain`` the unfused-equivalent bytes, and
+``e2e`` the same metric through the public binding with the state copied in
+from pinned host memory and back out every step.  The 16 GiB state is far
+larger than L2, so no flush is needed.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -34,8 +37,8 @@ import numpy as np
 REPO = Path(__file__).resolve().parent
 sys.path[:0] = [str(REPO), str(REPO / "pennylane-lightning_gb300")]
 
-METRIC = "30q c128 gate GB/s (unfused-equivalent algorithmic bytes / s)"
-UNIT = "GB/s"
+METRIC = "30q c128 gate throughput (amplitude updates per second: sum over gates of f * 2^n, f = 1 for SU(2), 1/4 for CZ)"
+UNIT = "G amplitude-updates/s"
 
 
 def parse():
@@ -141,11 +144,26 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------------- workload
+def config1_circuit(n, cycles):
+    from lightning_gb300.workloads import config1
+
+    return config1(n, cycles, seed=1001)
+
+
 def workload(n, cycles):
     from lightning_gb300.workloads import config1, unfused_bytes
 
     circuit, ham = config1(n, cycles, seed=1001)
     return circuit, ham, unfused_bytes
+
+
+def rel_err(a, b):
+    """(norm-relative difference, max relative difference over amplitudes
+    with |b| >= 1e-2 max|b|) of two states."""
+    nr = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    mag = np.abs(b)
+    sel = mag >= 1e-2 * mag.max()
+    return nr, float(np.max(np.abs(a[sel] - b[sel]) / mag[sel]))
 
 
 def profile_value(kernel_tag: str, key: str):
@@ -184,7 +202,8 @@ def gpu_arm(args) -> dict | None:
 
     n, cycles = args.qubits, args.cycles
     circuit, ham, unfused_bytes = workload(n, cycles)
-    alg_bytes = unfused_bytes(circuit, n, 16)
+    alg_bytes = unfused_bytes(circuit, n, 16)  # unfused-equivalent bytes (gate by gate)
+    updates = alg_bytes / 32.0  # amplitude updates: 2 f N S per gate with S = 16
 
     def ops_struct(cls):
         return cls([o.name for o in circuit], [o.params for o in circuit], [o.wires for o in circuit],
@@ -208,8 +227,8 @@ def gpu_arm(args) -> dict | None:
     S128 = ops_struct(ops.OpsStructC128)
     sv = ops.StateVectorC128(n)
     stream = torch.cuda.ExternalStream(sv.cuda_stream())
-    # warm-up doubles as the tile-size choice: unfused (0) vs fused tiles of 2^t
-    candidates = [0, 10, 11, 12] if args.tile_bits is None else [args.tile_bits]
+    # warm-up doubles as the tile-size choice among fused tiles of 2^t
+    candidates = [10, 11, 12] if args.tile_bits is None else [args.tile_bits]
     tune = {}
     for w in range(max(args.warmup, 1)):
         tb = candidates[w % len(candidates)] if w < len(candidates) else best_tb
@@ -238,22 +257,26 @@ def gpu_arm(args) -> dict | None:
     pass_bytes = 2.0 * (1 << n) * 16
     avg_launch_s = (total_s / args.steps) / passes
     achieved = pass_bytes / avg_launch_s / 1e9
-    fp64_passes = bool(ops.set_c128_fp64_passes(False))
-    ops.set_c128_fp64_passes(fp64_passes)
-    if best_tb >= 9 and not fp64_passes:
-        kernel, tag = ("k_tile_reg_df<df, df> (register-blocked fused tile pass, double-float arithmetic)",
-                       "k_tile_reg_df_c128")
-    elif best_tb >= 9:
-        kernel, tag = "k_tile_reg<double> (register-blocked fused tile pass)", "k_tile_reg_c128"
-    elif best_tb:
-        kernel, tag = "k_tile_pass<double> (fused tile pass)", "k_tile_pass_c128"
+    fp64_passes = bool(ops.set_c128_fp64_passes(True))  # the default; returns the setting in force
+    if best_tb >= 9:
+        kernel, tag = "k_tile_reg<double> (register-blocked fused tile pass, FP64)", "k_tile_reg_c128"
     else:
-        kernel, tag = "k_1q<double, DENSE> and k_1q<double, NEG1>", "k_1q_dense_c128"
+        kernel, tag = "k_tile_pass<double> (fused tile pass, FP64)", "k_tile_pass_c128"
     traffic = traffic_from_profiles(tag)
     if traffic is not None:  # recorded for a 30-qubit launch; traffic grows with the amplitudes
         traffic *= float(1 << n) / float(1 << 30)
+    fp64_per_amp = profile_value(tag, "fp64_instructions_per_amplitude_per_pass")
 
-    # expectation value of the 64-term Hamiltonian (one read per flip-mask group)
+    # unfused per-gate kernels on the first cycle (a cycle's gates are the
+    # same mix in every cycle): the time of the whole circuit gate by gate
+    per_cycle = len(circuit) // cycles
+    S_cycle = ops.OpsStructC128([o.name for o in circuit[:per_cycle]], [o.params for o in circuit[:per_cycle]],
+                                [o.wires for o in circuit[:per_cycle]], [False] * per_cycle,
+                                [o.matrix for o in circuit[:per_cycle]])
+    timed_step(sv, S_cycle, stream, 0)
+    unfused_ms = timed_step(sv, S_cycle, stream, 0)[0] * cycles
+
+    # expectation value of the 64-term Hamiltonian
     H = ops.observables.HamiltonianC128(
         ham.coeffs, [ops.observables.TensorProdObsC128(
             [ops.observables.NamedObsC128({"X": "PauliX", "Y": "PauliY", "Z": "PauliZ"}[c], [w])
@@ -263,6 +286,29 @@ def gpu_arm(args) -> dict | None:
     t = time.perf_counter()
     ev_val = m.expval(H)
     expval_ms = (time.perf_counter() - t) * 1e3
+
+    # opt-in double-float passes: time, and accuracy against the FP64
+    # passes on the same circuit at 26 qubits
+    ops.set_c128_fp64_passes(False)
+    try:
+        timed_step(sv, S128, stream, best_tb)
+        df_ms = min(timed_step(sv, S128, stream, best_tb)[0] for _ in range(2))
+        n_acc = min(n, 26)
+        circ_acc, _ = config1_circuit(n_acc, cycles)
+        S_acc = ops.OpsStructC128([o.name for o in circ_acc], [o.params for o in circ_acc],
+                                  [o.wires for o in circ_acc], [False] * len(circ_acc),
+                                  [o.matrix for o in circ_acc])
+        states = {}
+        for fp64 in (False, True):
+            ops.set_c128_fp64_passes(fp64)
+            a_sv = ops.StateVectorC128(n_acc)
+            a_sv.applyOperations(S_acc, best_tb)
+            states[fp64] = a_sv.state()
+            del a_sv
+        df_nr, df_pr = rel_err(states[False], states[True])
+        del states
+    finally:
+        ops.set_c128_fp64_passes(fp64_passes)
 
     # e2e through the binding: pinned host state in, circuit, state out
     host_in = torch.empty(1 << n, dtype=torch.complex128, pin_memory=True)
@@ -301,33 +347,46 @@ def gpu_arm(args) -> dict | None:
     pg_s = (time.perf_counter() - t0) / e2e_steps
     del sv
 
+    step_s = total_s / args.steps
+    fused_gbs = passes * pass_bytes / step_s / 1e9
     res = {
-        "metric": METRIC, "value": replica_value(alg_bytes * args.steps, ws, total_s) / 1e9, "unit": UNIT, "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps,
+        "metric": METRIC, "value": replica_value(updates * args.steps, ws, total_s) / 1e9, "unit": UNIT,
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c128 (f64 arithmetic)" if fp64_passes else "c128 (double-float arithmetic in fused passes)",
         "data": "synthetic (seeded Haar SU(2) + CZ circuit, seed 1001)",
         "config": {"workload": f"config1: {n} qubits complex128, {cycles} cycles x ({n} Haar SU(2) + {n // 2} CZ)",
-                   "qubits": n, "gates_per_step": len(circuit), "algorithmic_bytes_per_step": alg_bytes,
+                   "qubits": n, "gates_per_step": len(circuit), "amplitude_updates_per_step": updates,
                    "l2": (f"inputs larger than L2 ({(1 << n) * 16 / 2**30:g} GiB state)" if (1 << n) * 16 > 129e6
                           else f"state of {(1 << n) * 16 / 2**20:g} MiB fits L2"), "parallelism": f"replicas x{ws}",
-                   "path": f"fused tile passes, 2^{best_tb} amplitudes per tile" if best_tb else "unfused per-gate kernels",
+                   "path": f"fused tile passes (FP64), 2^{best_tb} amplitudes per tile",
                    "tile_bits": best_tb, "passes_per_step": passes,
                    "tuning_ms_per_step": {str(k): round(v, 1) for k, v in sorted(tune.items())}},
-        "e2e": {"value": alg_bytes / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
+        "e2e": {"value": updates / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
-                "per_gate_calls": {"value": alg_bytes / pg_s / 1e9, "unit": UNIT, "ms_per_step": pg_s * 1e3,
+                "per_gate_calls": {"value": updates / pg_s / 1e9, "unit": UNIT, "ms_per_step": pg_s * 1e3,
                                    "path": f"{len(circuit)} binding calls per step (one per gate), lazy fusion"}},
         "roofline": {"kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_source": f"{peak_src} hbm_gbs", "traffic": traffic,
                      "algorithmic_bytes_per_launch": pass_bytes, "avg_launch_ms": avg_launch_s * 1e3,
-                     "note": "fused-actual bytes (2 N S per pass): the pass is instruction-bound on the FP32 "
-                             "pipe (double-float arithmetic; GB300 runs FP64 at 1/64 of FP32), not HBM-bound; the "
-                             "unfused-equivalent rate is `value`",
+                     "note": "fused-actual bytes (2 N S per pass) over the mean pass time.  A complex128 pass "
+                             "computes in FP64, which GB300 executes at 1/64 of its FP32 rate (about 0.63 T "
+                             "DFMA/s): the pass is bound by the FP64 pipe, not by HBM (fp64_pipe below)",
+                     "fp64_pipe": {"fp64_instructions_per_amplitude_per_pass": fp64_per_amp,
+                                   "source": f"profiles/{tag}.md (ncu)",
+                                   "frac": profile_value(tag, "fp64_pipe_frac")},
                      "issue": {"metric": "smsp__issue_active (ncu, fraction of peak instruction issue)",
                                "frac": profile_value(tag, "issue_active_frac"),
                                "source": f"profiles/{tag}.md"}},
-        "unfused": {"ms_per_step": tune.get(0), "value": alg_bytes / (tune[0] / 1e3) / 1e9 if tune.get(0) else None},
+        "fusion_gain": {"unfused_equivalent_gbs": alg_bytes / step_s / 1e9, "fused_actual_gbs": fused_gbs,
+                        "bytes_ratio": alg_bytes / (passes * pass_bytes), "unfused_ms_per_step": unfused_ms,
+                        "time_ratio": unfused_ms / (step_s * 1e3),
+                        "unfused_note": f"per-gate FP64 kernels on the first cycle x {cycles}"},
+        "double_float": {"ms_per_step": df_ms, "value": updates / (df_ms / 1e3) / 1e9, "unit": UNIT,
+                         "arithmetic": "double-float (hi + lo floats, ~48 significant bits, FP32 exponent range), "
+                                       "opt-in (set_c128_fp64_passes(False))",
+                         "accuracy_vs_fp64": {"qubits": n_acc, "norm_rel": df_nr, "per_amplitude_rel": df_pr,
+                                              "per_amplitude_floor": "|a| >= 1e-2 max|a|"}},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "expval_64_terms": {"value": ev_val, "ms": expval_ms},
@@ -338,11 +397,11 @@ def gpu_arm(args) -> dict | None:
         sv64 = ops.StateVectorC64(n)
         s64 = torch.cuda.ExternalStream(sv64.cuda_stream())
         t64 = {}
-        for tb in ((0, 11, 12) if args.tile_bits is None else (args.tile_bits,)):
+        for tb in ((11, 12) if args.tile_bits is None else (args.tile_bits,)):
             timed_step(sv64, S64, s64, tb)
             t64[tb] = timed_step(sv64, S64, s64, tb)[0]
         b64 = min(t64, key=t64.get)
-        res["c64"] = {"value": unfused_bytes(circuit, n, 8) / (t64[b64] / 1e3) / 1e9, "unit": UNIT,
+        res["c64"] = {"value": updates / (t64[b64] / 1e3) / 1e9, "unit": UNIT,
                       "ms_per_step": t64[b64], "tile_bits": b64,
                       "tuning_ms_per_step": {str(k): round(v, 1) for k, v in sorted(t64.items())}}
         del sv64
@@ -524,25 +583,38 @@ def cpu_setup():
     return Oracle("orc")
 
 
-def cpu_sample(orc, n_cpu: int, reps: int = 1):
-    """Config-1's first cycle at `n_cpu` qubits, timed on the host cores."""
-    from lightning_gb300.workloads import config1, unfused_bytes
+def cpu_sample_ops(n: int, cycles: int):
+    """The CPU sample of the config-1 circuit: the first cycle's first 10
+    SU(2) gates and first 5 CZ gates (the cycle's 2:1 mix of the two)."""
+    circuit, _ = config1_circuit(n, cycles)
+    first = circuit[: len(circuit) // cycles]
+    su2 = [o for o in first if o.matrix is not None][:10]
+    cz = [o for o in first if o.matrix is None][:5]
+    return su2 + cz
 
-    circuit, _ = config1(n_cpu, 1, seed=1001)
-    sv = orc.sv(n_cpu, np.complex128)
-    for op in circuit[:2]:
-        sv.apply_matrix(op.matrix, op.wires) if op.matrix is not None else sv.apply(op.name, op.wires)
-    times = []
-    for _ in range(reps):
-        t = time.perf_counter()
-        for op in circuit:
-            if op.matrix is not None:
-                sv.apply_matrix(op.matrix, op.wires)
-            else:
-                sv.apply(op.name, op.wires)
-        times.append(time.perf_counter() - t)
-    b = unfused_bytes(circuit, n_cpu, 16)
-    return b, statistics.median(times), len(circuit), orc.num_threads()
+
+def cpu_sample(orc, n_cpu: int, cycles: int, sv=None):
+    """Time the CPU sample at n_cpu qubits on the host cores; returns
+    (amplitude updates, seconds, gates, threads, state handle)."""
+    from lightning_gb300.workloads import amplitude_updates
+
+    ops_ = cpu_sample_ops(n_cpu, cycles)
+    if sv is None:
+        sv = orc.sv(n_cpu, np.complex128)
+    t = time.perf_counter()
+    for op in ops_:
+        if op.matrix is not None:
+            sv.apply_matrix(op.matrix, op.wires)
+        else:
+            sv.apply(op.name, op.wires)
+    dt = time.perf_counter() - t
+    return amplitude_updates(ops_, n_cpu), dt, len(ops_), orc.num_threads(), sv
+
+
+def cpu_description(n_cpu: int, ng: int) -> str:
+    return (f"{ng} gates of the config-1 circuit per step (the first cycle's first 10 Haar SU(2) and first 5 CZ) "
+            f"at {n_cpu} qubits complex128; the LM-kernel restatement of lightning.qubit's algorithm with OpenMP on "
+            f"the host cores (no AVX kernels on this host)")
 
 
 def reference_arm(args) -> None:
@@ -550,29 +622,41 @@ def reference_arm(args) -> None:
     if rank != 0:
         return
     orc = cpu_setup()
-    n_cpu = min(args.qubits, 28)
+    n_cpu = args.qubits
+    sv = None
     for _ in range(args.warmup):
-        cpu_sample(orc, n_cpu)
+        *_, sv = cpu_sample(orc, n_cpu, args.cycles, sv)
     vals = []
     t_total = 0.0
     for _ in range(args.steps):
-        b, t, ng, threads = cpu_sample(orc, n_cpu)
-        vals.append(b / t / 1e9)
+        u, t, ng, threads, sv = cpu_sample(orc, n_cpu, args.cycles, sv)
+        vals.append(u / t / 1e9)
         t_total += t
     v = statistics.median(vals)
-    sample = (f"first cycle of the config-1 circuit ({ng} gates) at {n_cpu} qubits complex128 per step; "
-              f"LM-kernel restatement with OpenMP (port of lightning.qubit's algorithm; no AVX on this host)")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_total * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64 arithmetic)", "data": "synthetic",
         "config": {"workload": f"config1: {args.qubits} qubits complex128, {args.cycles} cycles x ({args.qubits} "
                                f"Haar SU(2) + {args.qubits // 2} CZ)", "qubits": args.qubits,
-                   "sample": f"first cycle at {n_cpu} qubits per step (the unfused-equivalent bytes of the "
+                   "sample": f"{ng} of the circuit's gates per step at {n_cpu} qubits (amplitude updates of the "
                              f"sampled gates over their time: the same metric)"},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": cpu_description(n_cpu, ng), "host": host_cpu()},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
+
+
+def host_cpu() -> str:
+    """The host CPU model (lscpu) and core count, for the CPU numbers."""
+    model = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        fields = {ln.split(":", 1)[0].strip(): ln.split(":", 1)[1].strip() for ln in out.splitlines() if ":" in ln}
+        model = fields.get("Model name") or fields.get("Vendor ID", "")
+    except (OSError, subprocess.TimeoutExpired):
+        pass
+    return f"{model or 'unknown'}, {os.cpu_count()} logical cores"
 
 
 def main():
@@ -585,16 +669,17 @@ def main():
         # child process of the CPU baseline: OpenMP thread binding stays out
         # of the GPU process (its host threads compile circuits in parallel)
         orc = cpu_setup()
-        n_cpu = min(args.qubits, 28)
-        b, t, ng, threads = cpu_sample(orc, n_cpu)
-        print(json.dumps({"value": b / t / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-                          "sample": f"first cycle of the config-1 circuit ({ng} gates) at {n_cpu} qubits "
-                                    f"complex128, {t:.1f} s; LM-kernel restatement with OpenMP on the host cores"}))
+        n_cpu = args.qubits
+        *_, sv = cpu_sample(orc, n_cpu, args.cycles)  # first touch of the host state
+        u, t, ng, threads, _ = cpu_sample(orc, n_cpu, args.cycles, sv)
+        print(json.dumps({"value": u / t / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+                          "sample": cpu_description(n_cpu, ng) + f", {t:.1f} s", "host": host_cpu()}))
         return
     cpu = None
     if rank == 0 and not args.no_cpu:
         out = subprocess.run([sys.executable, str(Path(__file__).resolve()), "--impl", "cpu-sample", "--qubits",
-                              str(args.qubits)], capture_output=True, text=True, check=True)
+                              str(args.qubits), "--cycles", str(args.cycles)], capture_output=True, text=True,
+                             check=True)
         cpu = json.loads(out.stdout.strip().splitlines()[-1])
     res = gpu_arm(args)
     if rank == 0 and res is not None:

@@ -54,6 +54,10 @@ int plgb_runtime_info(char *buf, size_t len);
 int plgb_device_count(int *out);
 /* number of kernels this library has launched in the process (monotonic) */
 int plgb_kernel_launches(uint64_t *out);
+/* number of device-memory requests this library has made in the process
+ * (monotonic; every request, whether cudaMalloc or a reuse-pool hit): a
+ * diagnostic with no counterpart in the reference */
+int plgb_device_allocations(uint64_t *out);
 
 /* ---- state vector (StateVectorLQubitManaged.hpp:52-188,
  *      StateVectorLQubit.hpp:359-1036, Bindings.hpp:870-922,
@@ -184,10 +188,13 @@ int plgb_ops_num_par_ops(const plgb_ops *ops, int *out);
  * passes are cached on `ops` per register size, precision and t).
  * *passes_out (optional) receives the number of kernel passes per call. */
 int plgb_sv_apply_operations(plgb_sv *sv, plgb_ops *ops, int tile_bits, int *passes_out);
-/* Arithmetic of fused complex128 passes (no counterpart in the reference):
- * on = 0 (default) runs them in double-float arithmetic on the FP32 pipe
- * (about 48 significant bits; GB300 executes FP64 at 1/64 of its FP32
- * rate), on = 1 in FP64.  Process-wide; returns the previous setting. */
+/* Arithmetic of complex128 fused passes, batched passes and the fused
+ * adjoint sweep (no counterpart in the reference): on = 1 (default) runs
+ * them in FP64, like the reference's kernels; on = 0 opts into double-float
+ * arithmetic on the FP32 pipe (about 48 significant bits, FP32 exponent
+ * range: |amplitude| < 2^127, magnitudes below 2^-126 flush to zero; GB300
+ * executes FP64 at 1/64 of its FP32 rate).  Process-wide; returns the
+ * previous setting. */
 int plgb_set_c128_fp64_passes(int on);
 /* Register-tile kernel variant for a precision (64 or 128): occ = 0 lets a
  * thread use up to 255 registers, occ = 1 caps it at 128 (twice the
@@ -283,10 +290,13 @@ const char *plgb_gate_name(int code);
  * scratch with cudaMalloc (after a cudaFree, which waits for the device);
  * this variant uses one fixed device array per device instead, for callers
  * that have filled the device up to a memory budget.  Same result as
- * plgb_meas_expval_matrix.  nw > 5 returns PLGB_ERR_INVALID.  The first call
- * on a device resolves the array's address (make it before any stream
- * capture).  Overlapping calls on one device race on the shared array:
- * serialise them. */
+ * plgb_meas_expval_matrix.  nw > 5 returns PLGB_ERR_INVALID, and so does a
+ * lazy handle with gates still queued (running them would compile and
+ * upload a fused program, which allocates; plgb_sv_synchronize runs them).
+ * The first call on a device resolves the array's address.  Every call
+ * copies the matrix in and synchronises the state vector's stream, so it
+ * must not be called while any stream is being captured.  Overlapping calls
+ * on one device race on the shared array: serialise them. */
 int plgb_meas_expval_matrix_noalloc(plgb_sv *sv, const double *matrix, const int64_t *wires, int nw, double *out);
 
 #ifdef __cplusplus

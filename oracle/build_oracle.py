@@ -23,7 +23,9 @@ from concurrent.futures import ThreadPoolExecutor
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF_ROOT = Path(os.environ.get("PL_REFERENCE_ROOT", "/root/reference"))
+# the reference checkout: PL_REFERENCE_ROOT, else a "reference" directory
+# beside this repository's root
+REF_ROOT = Path(os.environ.get("PL_REFERENCE_ROOT", HERE.parent.parent / "reference"))
 REF_OUT = HERE / "_ref"
 
 # -ffp-contract=off: no FMA contraction, so the restatement rounds like the

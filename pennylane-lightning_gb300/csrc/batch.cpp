@@ -128,6 +128,7 @@ template <class T> void *BatchEngine<T>::grow(void *&buf, size_t &cap, size_t ne
     if (pinned) {
         cuda_check(cudaMallocHost(&buf, want), "cudaMallocHost(batch)");
     } else {
+        count_device_allocation();
         cuda_check(cudaMalloc(&buf, want), "cudaMalloc(batch)");
     }
     cap = want;

@@ -225,6 +225,12 @@ int plgb_kernel_launches(uint64_t *out) {
         *out = launch_count();
     });
 }
+int plgb_device_allocations(uint64_t *out) {
+    return guard([&] {
+        need(out, "out");
+        *out = device_allocation_count();
+    });
+}
 
 int plgb_backend_info(char *buf, size_t len) {
     return copy_text("{\"NAME\": \"lightning.gb300\", \"ARCH\": \"sm_103a\", \"REFERENCE\": \"lightning.qubit\"}", buf,
@@ -583,8 +589,12 @@ int plgb_set_c128_fp64_passes(int on) {
 
 int plgb_meas_expval_matrix_noalloc(plgb_sv *sv, const double *matrix, const int64_t *wires, int nw, double *out) {
     // no host containers on the success path: the matrix and wires are read
-    // in place (noalloc.cu)
-    return with_sv(sv, [&](auto &s) {
+    // in place (noalloc.cu).  Gates queued on a lazy handle are not run here:
+    // running them compiles and uploads a fused program, which allocates.
+    return with_sv_meta(sv, [&](auto &s) {
+        PLGB_REQUIRE(sv->pend_d.empty() && sv->pend_f.empty(),
+                     "plgb_meas_expval_matrix_noalloc: gates are queued on this state vector and running them "
+                     "allocates device memory; run them first (plgb_sv_synchronize)");
         need(out, "out");
         need(matrix, "matrix");
         if (nw > 0) {

@@ -104,6 +104,10 @@ class ReuseScope {
     ReusePool *prev_;
 };
 void *dev_alloc(size_t bytes);
+// every request for device memory the library makes (dev_alloc, the batch
+// engine's arena) is counted; the count is a diagnostic of the C ABI
+void count_device_allocation();
+unsigned long long device_allocation_count();
 void dev_free(void *p);
 void *pinned_alloc(size_t bytes);
 void pinned_free(void *p);
@@ -265,8 +269,10 @@ template <class T> struct FusedProgram;
 template <class T>
 std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>> &prims, int tile_bits,
                                                bool upload = true, bool recipes = false);
-// Arithmetic of fused complex128 passes: double-float on the FP32 pipe
-// (default) or FP64.
+// Arithmetic of fused complex128 passes (and of the batch engine and the
+// fused adjoint sweep): FP64 (default) or, opted into, double-float on the
+// FP32 pipe (hi + lo floats: ~48 significant bits, |x| < 2^127, magnitudes
+// below 2^-126 flush to zero).
 void set_c128_fp64_passes(bool on);
 bool c128_fp64_passes();
 // JSON description of a compiled program's passes (plan introspection)

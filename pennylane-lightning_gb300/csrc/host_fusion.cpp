@@ -1288,7 +1288,9 @@ std::shared_ptr<FusedProgram<T>> compile_fused(int n, const std::vector<Prim<T>>
 }
 
 namespace {
-std::atomic<bool> g_c128_fp64{false};
+// complex128 fused passes compute in FP64 unless a caller opts into the
+// double-float arithmetic (about 48 significant bits, FP32 exponent range)
+std::atomic<bool> g_c128_fp64{true};
 }
 void set_c128_fp64_passes(bool on) { g_c128_fp64 = on; }
 bool c128_fp64_passes() { return g_c128_fp64; }

@@ -95,7 +95,14 @@ void ReusePool::recycle() {
 ReuseScope::ReuseScope(ReusePool &pool) : prev_(tl_pool) { tl_pool = &pool; }
 ReuseScope::~ReuseScope() { tl_pool = prev_; }
 
+namespace {
+std::atomic<unsigned long long> g_dev_allocs{0};
+}
+void count_device_allocation() { g_dev_allocs.fetch_add(1, std::memory_order_relaxed); }
+unsigned long long device_allocation_count() { return g_dev_allocs.load(std::memory_order_relaxed); }
+
 void *dev_alloc(size_t bytes) {
+    count_device_allocation();
     if (tl_pool) {
         return tl_pool->take(bytes, false);
     }

@@ -16,8 +16,13 @@
 //    complex128); larger requests are rejected with PLGB_ERR_INVALID.
 //  * The first call on each device does the set-up: it resolves the
 //    device address of the array with cudaGetSymbolAddress, with that device
-//    current.  That may load this module's device code, so make the first
-//    call on a device before any stream capture begins.
+//    current.
+//  * Every call copies the matrix in from the host stack and synchronises
+//    the state vector's stream before it returns, so no call may be made
+//    while any stream is being captured.
+//  * A lazy handle with gates still queued is rejected (PLGB_ERR_INVALID):
+//    running the queue compiles and uploads a fused program, which
+//    allocates.
 //  * Nothing in the array needs to start at zero: the matrix is copied in
 //    before each launch, every reduction block writes its own partial slot,
 //    and the final reduction overwrites the result slot.

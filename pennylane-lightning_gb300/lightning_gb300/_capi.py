@@ -25,6 +25,7 @@ SIGNATURES = {
     "plgb_runtime_info": (C.c_int, [C.c_char_p, C.c_size_t]),
     "plgb_device_count": (C.c_int, [IP]),
     "plgb_kernel_launches": (C.c_int, [C.POINTER(C.c_uint64)]),
+    "plgb_device_allocations": (C.c_int, [C.POINTER(C.c_uint64)]),
     "plgb_sv_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(VP)]),
     "plgb_sv_create_raw": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(VP)]),
     "plgb_sv_clone": (C.c_int, [VP, C.POINTER(VP)]),

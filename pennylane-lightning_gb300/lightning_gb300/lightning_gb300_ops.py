@@ -102,8 +102,10 @@ def set_lazy_min_qubits(q: int) -> int:
 
 
 def set_c128_fp64_passes(on: bool) -> bool:
-    """Fused complex128 passes in FP64 (True) or double-float arithmetic on
-    the FP32 pipe (False, the default); returns the previous setting."""
+    """Fused complex128 passes (and batched passes and the fused adjoint
+    sweep) in FP64 (True, the default) or, opted into, double-float
+    arithmetic on the FP32 pipe (False: ~48 significant bits, FP32 exponent
+    range); returns the previous setting."""
     return bool(lib().plgb_set_c128_fp64_passes(1 if on else 0))
 
 

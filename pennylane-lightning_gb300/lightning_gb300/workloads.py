@@ -125,6 +125,12 @@ def unfused_bytes(ops: list[Op], n: int, itemsize: int) -> float:
     return sum(2.0 * frac.get(op.name, 1.0) * N * itemsize for op in ops)
 
 
+def amplitude_updates(ops: list[Op], n: int) -> float:
+    """Work of applying `ops`, independent of how it is executed: sum over
+    gates of f * 2^n amplitude updates (f as in unfused_bytes)."""
+    return unfused_bytes(ops, n, 1) / 2.0
+
+
 # --------------------------------------------------------------------- config 2
 @dataclass
 class BatchCircuit:

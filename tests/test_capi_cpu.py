@@ -81,3 +81,14 @@ def test_process_wide_settings_roundtrip(ops_module):
     on = ops_module.set_lazy_fusion(False)
     assert ops_module.set_lazy_fusion(on) is False
     assert _capi.lib().plgb_set_tile_variant(32, 1) == -1  # no such precision
+
+
+def test_cpp_api_header_compiles():
+    # include/pl_gb300.hpp (the C++ API) and its test program compile; the
+    # program itself runs under -m gpu (test_gpu_cpp_api.py)
+    import subprocess
+
+    from cpp_build import compile_cmd
+
+    proc = subprocess.run(compile_cmd(REPO / "unused", syntax_only=True), capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr

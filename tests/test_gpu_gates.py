@@ -51,7 +51,7 @@ def test_one_wire_every_wire(ops_module, oracle, name, dt):
         p = gate_params(name, rng)
         getattr(sv, name)([w], False, p)
         o.apply(name, [w], False, p)
-    assert_close(sv.state(), o.state(), dt, scale=4, what=name)
+    assert_close(sv.state(), o.state(), dt, what=name)
 
 
 @pytest.mark.parametrize("dt", DTYPES)
@@ -65,7 +65,7 @@ def test_two_wire_every_pair(ops_module, oracle, name, dt):
         p = gate_params(name, rng)
         getattr(sv, name)([a, b], False, p)
         o.apply(name, [a, b], False, p)
-    assert_close(sv.state(), o.state(), dt, scale=20, what=name)
+    assert_close(sv.state(), o.state(), dt, what=name)
 
 
 @pytest.mark.parametrize("dt", DTYPES)
@@ -136,7 +136,7 @@ def test_apply_matrix(ops_module, oracle, k, inverse, dt):
         else:
             sv.applyMatrix(U, w, inverse)
         o.apply_matrix(U, w, inverse, cw, cv)
-        assert_close(sv.state(), o.state(), dt, scale=1 << k, what=f"matrix k={k} nc={nc}")
+        assert_close(sv.state(), o.state(), dt, what=f"matrix k={k} nc={nc}")
 
 
 @pytest.mark.parametrize("dt", DTYPES)
@@ -153,7 +153,7 @@ def test_apply_sparse_matrix(ops_module, oracle, dt):
     sv, o = _pair(ops_module, oracle, n, dt, st)
     sv.applySparseMatrix(indptr, cols, data, w)
     o.apply_sparse(indptr, cols, data, w)
-    assert_close(sv.state(), o.state(), dt, scale=8, what="sparse op")
+    assert_close(sv.state(), o.state(), dt, what="sparse op")
 
 
 @pytest.mark.parametrize("dt", DTYPES)

@@ -61,7 +61,7 @@ def test_lazy_equals_eager(ops_module, dt):
     b = np.zeros(1 << n, dtype=dt)
     eager.getState(a)
     lazy.getState(b)
-    assert_close(b, a, dt, scale=20, what="lazy state")
+    assert_close(b, a, dt, what="lazy state")
     # a read in the middle sees every gate queued before it
     half = len(ops) // 2
     e2 = sv_class(ops_module, dt)(n)
@@ -70,13 +70,13 @@ def test_lazy_equals_eager(ops_module, dt):
     l2.set_lazy(True)
     _apply(e2, ops[:half])
     _apply(l2, ops[:half])
-    assert_close(meas_class(ops_module, dt)(l2).probs(), meas_class(ops_module, dt)(e2).probs(), dt, scale=20,
+    assert_close(meas_class(ops_module, dt)(l2).probs(), meas_class(ops_module, dt)(e2).probs(), dt,
                  what="probs mid-circuit")
     _apply(e2, ops[half:])
     _apply(l2, ops[half:])
     e2.getState(a)
     l2.getState(b)
-    assert_close(b, a, dt, scale=20, what="state after mid-circuit read")
+    assert_close(b, a, dt, what="state after mid-circuit read")
 
 
 def test_lazy_errors_surface_at_the_call(ops_module):

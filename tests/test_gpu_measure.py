@@ -11,7 +11,7 @@ the oracle draws them.
 import numpy as np
 import pytest
 
-from helpers import DTYPES, assert_close, meas_class, obs_ns, rand_hermitian, rand_state, seed_of, sv_class
+from helpers import DTYPES, assert_close, assert_scalar, meas_class, obs_ns, rand_hermitian, rand_state, seed_of, sv_class
 
 pytestmark = pytest.mark.gpu
 
@@ -44,8 +44,10 @@ def test_expval_var_named(ops_module, oracle, dt):
     _, sv, m, o = _setup(ops_module, oracle, 6, dt, seed_of("named", dt.__name__))
     for name in ("PauliX", "PauliY", "PauliZ", "Hadamard", "Identity"):
         for w in range(6):
-            assert_close(m.expval(name, [w]), o.expval_named(name, [w]), dt, scale=10, what=f"E {name}{w}")
-            assert_close(m.var(name, [w]), o.var_named(name, [w]), dt, scale=10, what=f"V {name}{w}")
+            # a one-wire observable has norm 1: its expval / var errors are
+            # relative to 1 (both can be exactly 0 for Identity)
+            assert_scalar(m.expval(name, [w]), o.expval_named(name, [w]), dt, mag=1.0, what=f"E {name}{w}")
+            assert_scalar(m.var(name, [w]), o.var_named(name, [w]), dt, mag=1.0, what=f"V {name}{w}")
 
 
 @pytest.mark.parametrize("dt", DTYPES)
@@ -54,8 +56,10 @@ def test_expval_var_matrix(ops_module, oracle, k, dt):
     rng, sv, m, o = _setup(ops_module, oracle, 8, dt, seed_of("hmat", k, dt.__name__))
     H = rand_hermitian(rng, k)
     w = [int(x) for x in rng.choice(8, size=k, replace=False)]
-    assert_close(m.expval(H, w), o.expval_matrix(H, w), dt, scale=100, what="E herm")
-    assert_close(m.var(H, w), o.var_matrix(H, w), dt, scale=1000, what="V herm")
+    # errors of <H> and var(H) = <H^2> - <H>^2 scale with ||H|| and ||H||^2
+    hn = float(np.linalg.norm(H, 2))
+    assert_scalar(m.expval(H, w), o.expval_matrix(H, w), dt, mag=hn, what="E herm")
+    assert_scalar(m.var(H, w), o.var_matrix(H, w), dt, mag=hn * hn, what="V herm")
 
 
 def _pauli_terms(rng, n, nterms, maxw=4):
@@ -84,8 +88,11 @@ def test_expval_pauli_hamiltonian(ops_module, oracle, dt):
     terms += [(0.5, "XZ", [1, 4]), (-0.25, "XZ", [1, 7]), (0.75, "YY", [2, 3]), (0.1, "XX", [2, 3])]
     H = _ham_obs(ops_module, dt, terms)
     spec = pauli_sum_spec(terms)
-    assert_close(m.expval(H), o.expval_obs(spec), dt, scale=100, what="E ham")
-    assert_close(m.var(H), o.var_obs(spec), dt, scale=1000, what="V ham")
+    # the error of a Pauli-sum expectation is relative to sum |c| (each word
+    # has norm 1), that of the variance to (sum |c|)^2
+    c1 = sum(abs(t[0]) for t in terms)
+    assert_scalar(m.expval(H), o.expval_obs(spec), dt, mag=c1, what="E ham")
+    assert_scalar(m.var(H), o.var_obs(spec), dt, mag=c1 * c1, what="V ham")
 
 
 @pytest.mark.parametrize("dt", DTYPES)
@@ -102,11 +109,12 @@ def test_expval_mixed_observables(ops_module, oracle, dt):
                Prod([Named("Hadamard", [1]), Named("PauliZ", [6])])])
     spec = (f"ham 3 0.5 prod 2 named PauliX 0 herm 2 3 5 {off} -1.25 named PauliY 2 "
             f"0.3 prod 2 named Hadamard 1 named PauliZ 6")
-    assert_close(m.expval(obs), o.expval_obs(spec, od), dt, scale=100, what="E mixed")
-    assert_close(m.var(obs), o.var_obs(spec, od), dt, scale=1000, what="V mixed")
+    c1 = 0.5 * float(np.linalg.norm(H2, 2)) + 1.25 + 0.3  # sum of |c| x term norms
+    assert_scalar(m.expval(obs), o.expval_obs(spec, od), dt, mag=c1, what="E mixed")
+    assert_scalar(m.var(obs), o.var_obs(spec, od), dt, mag=c1 * c1, what="V mixed")
     single = Prod([Named("PauliZ", [0]), Named("PauliZ", [1]), Named("PauliZ", [2])])
-    assert_close(m.expval(single), o.expval_obs("prod 3 named PauliZ 0 named PauliZ 1 named PauliZ 2"), dt,
-                 scale=10, what="E ZZZ")
+    assert_scalar(m.expval(single), o.expval_obs("prod 3 named PauliZ 0 named PauliZ 1 named PauliZ 2"), dt,
+                  mag=1.0, what="E ZZZ")
 
 
 @pytest.mark.parametrize("dt", DTYPES)
@@ -117,11 +125,12 @@ def test_expval_sparse(ops_module, oracle, dt):
     A = sp.random(128, 128, density=0.05, random_state=3) + 1j * sp.random(128, 128, density=0.05, random_state=4)
     A = (A + A.conj().T).tocsr()
     A.sort_indices()
-    assert_close(m.expval(A.indptr, A.indices, A.data), o.expval_sparse(A.indptr, A.indices, A.data), dt,
-                 scale=100, what="E sparse")
+    an = float(np.linalg.norm(A.toarray(), 2))
+    assert_scalar(m.expval(A.indptr, A.indices, A.data), o.expval_sparse(A.indptr, A.indices, A.data), dt,
+                  mag=an, what="E sparse")
     *_, Sparse = obs_ns(ops_module, dt)
     obs = Sparse(A.data, A.indices, A.indptr, list(range(7)))
-    assert_close(m.expval(obs), o.expval_sparse(A.indptr, A.indices, A.data), dt, scale=100, what="E sparseH")
+    assert_scalar(m.expval(obs), o.expval_sparse(A.indptr, A.indices, A.data), dt, mag=an, what="E sparseH")
 
 
 @pytest.mark.parametrize("dt", DTYPES)
@@ -205,5 +214,6 @@ def test_large_pauli_sum_apply_chunks(ops_module, oracle, dt):
     Named, _, Prod, Ham, _ = obs_ns(ops_module, dt)
     H = Ham([t[0] for t in terms], [Prod([Named("Pauli" + c, [w]) for c, w in zip(t[1], t[2])]) for t in terms])
     spec = pauli_sum_spec(terms)
-    assert_close(m.expval(H), o.expval_obs(spec), dt, scale=400, what="E big H")
-    assert_close(m.var(H), o.var_obs(spec), dt, scale=4000, what="var big H")
+    c1 = sum(abs(t[0]) for t in terms)
+    assert_scalar(m.expval(H), o.expval_obs(spec), dt, mag=c1, what="E big H")
+    assert_scalar(m.var(H), o.var_obs(spec), dt, mag=c1 * c1, what="var big H")

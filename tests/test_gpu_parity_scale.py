@@ -1,0 +1,148 @@
+"""Parity at the workloads' own sizes, on the default paths, at the stated
+tolerance (1e-12 relative for complex128, 1e-5 for complex64; the checks of
+helpers.assert_state / assert_scalar, no multipliers).
+
+* config 1 (20 cycles of Haar SU(2) on every qubit + CZ on disjoint pairs)
+  at 24 qubits: through one compiled applyOperations call and through one
+  binding call per gate (the lightning.qubit device's pattern, which the
+  lazy handle fuses), complex128 in FP64 passes (the default) and
+  complex64; the 64-term Pauli Hamiltonian <H> on the result;
+* the same circuit in the opt-in double-float passes, whose accuracy figure
+  is printed and bounded separately;
+* config 3 (Rot + CNOT-range layers) at 20 qubits with its 200-term
+  Hamiltonian: the full adjoint Jacobian;
+* samples at 20 qubits, all wires and a wire subset: exactly the oracle's
+  integers for the same seed.
+
+The oracle runs the reference's algorithm gate by gate on the host cores.
+"""
+import numpy as np
+import pytest
+
+from helpers import assert_scalar, assert_state, rel_errors, rand_state, seed_of
+from lightning_gb300.workloads import config1, config3
+from test_gpu_fusion import oracle_apply, ops_struct
+
+pytestmark = pytest.mark.gpu
+
+N1 = 24  # config-1 register for the parity runs (2^24 amplitudes, 256 MiB c128)
+N3 = 20  # config-3 register
+
+
+def _ham_obs(ops, dt, ham):
+    s = "C128" if np.dtype(dt) == np.complex128 else "C64"
+    o = ops.observables
+    Named, Prod, Ham = getattr(o, "NamedObs" + s), getattr(o, "TensorProdObs" + s), getattr(o, "Hamiltonian" + s)
+    names = {"X": "PauliX", "Y": "PauliY", "Z": "PauliZ"}
+    return Ham(list(ham.coeffs),
+               [Prod([Named(names[c], [w]) for c, w in zip(wd, ws)]) for wd, ws in zip(ham.words, ham.wires)])
+
+
+@pytest.fixture(scope="module")
+def config1_ref(oracle):
+    """Oracle states (c128, c64) and <H> of the 24-qubit config-1 circuit."""
+    from oracle.pyoracle import pauli_sum_spec
+
+    circuit, ham = config1(N1, 20, seed=1001)
+    ops = [op.as_dict() for op in circuit]
+    out = {"ops": ops, "ham": ham}
+    for dt in (np.complex128, np.complex64):
+        st = np.zeros(1 << N1, dt)
+        st[0] = 1
+        o = oracle.sv(N1, dt)
+        o.set_state(st)
+        for op in ops:
+            if op.get("matrix") is not None:
+                o.apply_matrix(op["matrix"], op["wires"], False)
+            else:
+                o.apply(op["name"], op["wires"], False, op.get("params", ()))
+        out[dt] = o.state()
+        out[(dt, "E")] = o.expval_obs(pauli_sum_spec(ham.terms()))
+    return out
+
+
+@pytest.mark.parametrize("dt", [np.complex128, np.complex64])
+def test_config1_24q_compiled(ops_module, config1_ref, dt):
+    SV = ops_module.StateVectorC128 if dt == np.complex128 else ops_module.StateVectorC64
+    sv = SV(N1)
+    passes = sv.applyOperations(ops_struct(ops_module, dt, config1_ref["ops"]), 11)
+    assert passes > 1
+    st = sv.state()
+    nr, pr = rel_errors(st, config1_ref[dt], dt)
+    print(f"config-1 {N1}q {np.dtype(dt).name} compiled: norm-rel {nr:.3e}, per-amplitude {pr:.3e}")
+    assert_state(st, config1_ref[dt], dt, what="config-1 state")
+    M = ops_module.MeasurementsC128(sv) if dt == np.complex128 else ops_module.MeasurementsC64(sv)
+    e = M.expval(_ham_obs(ops_module, dt, config1_ref["ham"]))
+    print(f"config-1 {N1}q {np.dtype(dt).name} <H>: {e!r} vs {config1_ref[(dt, 'E')]!r}")
+    assert_scalar(e, config1_ref[(dt, "E")], dt, what="config-1 <H> (64 terms)")
+
+
+def test_config1_24q_per_gate_calls(ops_module, config1_ref):
+    # the lightning.qubit device applies a circuit with one binding call per
+    # gate; at 24 qubits the handle queues them and runs fused passes
+    sv = ops_module.StateVectorC128(N1)
+    for op in config1_ref["ops"]:
+        if op.get("matrix") is not None:
+            sv.applyMatrix(op["matrix"], op["wires"], False)
+        else:
+            getattr(sv, op["name"])(op["wires"], False, op.get("params", []))
+    st = sv.state()
+    nr, pr = rel_errors(st, config1_ref[np.complex128], np.complex128)
+    print(f"config-1 {N1}q c128 per-gate calls: norm-rel {nr:.3e}, per-amplitude {pr:.3e}")
+    assert_state(st, config1_ref[np.complex128], np.complex128, what="config-1 state, per-gate calls")
+
+
+def test_config1_24q_double_float_opt_in(ops_module, config1_ref):
+    # the opt-in double-float passes (~48 significant bits): within 1e-12
+    # norm-relative of the FP64 oracle; per amplitude they are looser than
+    # FP64 passes (the bound below is this arithmetic's stated accuracy)
+    prev = ops_module.set_c128_fp64_passes(False)
+    try:
+        sv = ops_module.StateVectorC128(N1)
+        sv.applyOperations(ops_struct(ops_module, np.complex128, config1_ref["ops"]), 11)
+        st = sv.state()
+    finally:
+        ops_module.set_c128_fp64_passes(prev)
+    nr, pr = rel_errors(st, config1_ref[np.complex128], np.complex128)
+    print(f"config-1 {N1}q c128 double-float passes: norm-rel {nr:.3e}, per-amplitude {pr:.3e}")
+    assert nr <= 1e-12
+    assert pr <= 1e-10
+
+
+def test_config3_20q_adjoint_jacobian(ops_module, oracle):
+    from oracle.pyoracle import pauli_sum_spec
+
+    circuit, ham = config3(N3, 12, seed=1003, nterms=200)
+    names = [o.name for o in circuit]
+    S = ops_module.OpsStructC128(names, [o.params for o in circuit], [o.wires for o in circuit],
+                                 [False] * len(circuit), [None] * len(circuit))
+    tp = list(range(sum(1 for o in circuit if o.params)))
+    H = _ham_obs(ops_module, np.complex128, ham)
+    jac = np.asarray(ops_module.AdjointJacobianC128()(ops_module.StateVectorC128(N3), [H], S, tp, True))
+    ref = oracle.sv(N3, np.complex128).adjoint([o.as_dict() for o in circuit], [pauli_sum_spec(ham.terms())], tp,
+                                               apply_ops=True)[0]
+    nr, pr = rel_errors(jac, ref, np.complex128)
+    print(f"config-3 {N3}q Jacobian ({len(tp)} params, 200 terms): norm-rel {nr:.3e}, per-entry {pr:.3e}")
+    assert_state(np.ravel(jac), np.ravel(ref), np.complex128, what="config-3 Jacobian")
+
+
+@pytest.mark.parametrize("dt", [np.complex128, np.complex64])
+def test_samples_20q_exact(ops_module, oracle, dt):
+    # the alias table is built from the GPU's probabilities; the integers
+    # equal the oracle's for the same seed, for all wires and for a subset
+    n = 20
+    rng = np.random.default_rng(seed_of("samples20", np.dtype(dt).name))
+    st = rand_state(rng, n, dt)
+    SV = ops_module.StateVectorC128 if dt == np.complex128 else ops_module.StateVectorC64
+    sv = SV(n)
+    sv.updateData(st)
+    o = oracle.sv(n, dt)
+    o.set_state(st)
+    M = ops_module.MeasurementsC128(sv) if dt == np.complex128 else ops_module.MeasurementsC64(sv)
+    M.set_random_seed(4242)
+    s = M.generate_samples(n, 20000)
+    assert np.array_equal(s.astype(np.int64), o.samples(20000, 4242))
+    for wires in ([17, 3, 9], [0, 19, 7, 12, 5, 2]):
+        assert_state(M.probs(wires), o.probs(wires), dt, what=f"probs {wires}")
+        s = M.generate_samples(wires, 20000)
+        assert np.array_equal(s.astype(np.int64), o.samples(20000, 4242, wires)), wires

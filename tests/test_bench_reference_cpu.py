@@ -17,8 +17,10 @@ def test_reference_arm_json_line():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["steps"] == 1 and d["warmup"] == 1
-    assert d["unit"] == "GB/s" and d["higher_is_better"] is True and d["value"] > 0
-    assert d["metric"].startswith("30q c128 gate GB/s")
+    import bench
+
+    assert d["unit"] == bench.UNIT and d["higher_is_better"] is True and d["value"] > 0
+    assert d["metric"] == bench.METRIC
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}

@@ -196,6 +196,12 @@ int plgb_sv_apply_operations(plgb_sv *sv, plgb_ops *ops, int tile_bits, int *pas
  * executes FP64 at 1/64 of its FP32 rate).  Process-wide; returns the
  * previous setting. */
 int plgb_set_c128_fp64_passes(int on);
+/* Dense complex64 gates on six wires without controls (applyMatrix and the
+ * unfused path) on the tensor cores (tcgen05, split-TF32 operands: about
+ * 2^-21 relative accuracy per gate) when on = 1 (default), or on the CUDA
+ * cores.  No counterpart in the reference.  Process-wide; returns the
+ * previous setting. */
+int plgb_set_tc_dense(int on);
 /* Register-tile kernel variant for a precision (64 or 128): occ = 0 lets a
  * thread use up to 255 registers, occ = 1 caps it at 128 (twice the
  * resident warps, some spills).  Returns the previous setting, or -1 for a

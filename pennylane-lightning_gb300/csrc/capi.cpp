@@ -4,6 +4,7 @@
 #include "batch.hpp"
 #include "fused.hpp"
 #include "host.hpp"
+#include "kernels_tc.hpp"
 
 #include <algorithm>
 #include <atomic>
@@ -581,6 +582,7 @@ int plgb_set_lazy_min_qubits(int q) { return q < 1 ? -1 : g_lazy_min_qubits.exch
 int plgb_sv_set_lazy(plgb_sv *sv, int on) {
     return with_sv(sv, [&](auto &) { sv->lazy = on != 0; }); // runs the queue first
 }
+int plgb_set_tc_dense(int on) { return set_tc_dense_enabled(on != 0) ? 1 : 0; }
 int plgb_set_c128_fp64_passes(int on) {
     const bool prev = c128_fp64_passes();
     set_c128_fp64_passes(on != 0);

@@ -339,40 +339,25 @@ std::vector<double> Measure<T>::probs(StateVector<T> &sv, const std::vector<int6
     std::sort(s.begin(), s.end());
     PLGB_REQUIRE(std::adjacent_find(s.begin(), s.end()) == s.end(), "wires must be unique");
     PLGB_REQUIRE(wires.size() <= 30, "marginal probabilities over at most 30 wires");
-    TBits tb{};
-    PLGB_REQUIRE(wires.size() <= 16 || true, "");
+    // every entry summed in the reference's order in the working precision
+    // (bit-exact, so seeded samples of a wire subset equal the reference's)
     const int k = static_cast<int>(wires.size());
     const size_t D = size_t{1} << k;
-    std::vector<double> out(D);
-    if (k <= 16) {
-        for (int m = 0; m < k; m++) {
-            tb.b[m] = sv.bit_of(wires[static_cast<size_t>(m)]);
-        }
-        sv.scratch().ensure_mat(D * sizeof(double));
-        double *dp = static_cast<double *>(sv.scratch().mat);
-        launch_probs_marginal<T>(sv.stream(), sv.data(), N, k, tb, dp);
-        cuda_check(cudaMemcpyAsync(out.data(), dp, D * sizeof(double), cudaMemcpyDeviceToHost, sv.stream()), "D2H");
-        sv.synchronize();
-    } else {
-        // many wires: reduce on the host from the full distribution
-        auto all = probs(sv, {}, true);
-        std::vector<int> bits(static_cast<size_t>(k));
-        for (int m = 0; m < k; m++) {
-            bits[static_cast<size_t>(m)] = sv.bit_of(wires[static_cast<size_t>(m)]);
-        }
-        for (u64 i = 0; i < N; i++) {
-            u64 j = 0;
-            for (int m = 0; m < k; m++) {
-                j = (j << 1) | ((i >> bits[static_cast<size_t>(m)]) & 1U);
-            }
-            out[j] += all[i];
-        }
+    MarginalGeom g{};
+    g.k = k;
+    u64 wmask = 0;
+    for (int m = 0; m < k; m++) {
+        g.wb[m] = sv.bit_of(wires[static_cast<size_t>(m)]);
+        wmask |= u64{1} << g.wb[m];
     }
-    // the reference returns PrecisionT values
-    for (auto &x : out) {
-        x = static_cast<double>(static_cast<T>(x));
-    }
-    return out;
+    g.cmask = (N - 1) & ~wmask;
+    sv.scratch().ensure_mat(D * sizeof(T));
+    T *dp = static_cast<T *>(sv.scratch().mat);
+    launch_probs_marginal_serial<T>(sv.stream(), sv.data(), g, dp);
+    std::vector<T> hp(D);
+    cuda_check(cudaMemcpyAsync(hp.data(), dp, D * sizeof(T), cudaMemcpyDeviceToHost, sv.stream()), "D2H");
+    sv.synchronize();
+    return std::vector<double>(hp.begin(), hp.end());
 }
 
 template <class T>

@@ -5,6 +5,7 @@
 // formed on the host in the working precision T with the same formulas, then
 // each gate is lowered to one of the streaming kernels of kernels_gates.cu.
 #include "host.hpp"
+#include "kernels_tc.hpp"
 
 #include <algorithm>
 #include <atomic>
@@ -511,6 +512,25 @@ template <class T> void StateVector<T>::run_prim(const Prim<T> &p) {
     case Prim<T>::DenseK: {
         const size_t k = p.tbits.size();
         const size_t D = size_t{1} << k;
+        if constexpr (std::is_same_v<T, float>) {
+            // complex64, six targets, no controls: the tensor-core kernel
+            TcGeom tg{};
+            if (k == 6 && p.cmask == 0 && tc_dense_enabled() && tc_geom_for(n_, p.tbits.data(), tg)) {
+                std::vector<unsigned short> img(tc_a_image_bytes() / sizeof(unsigned short));
+                tc_build_a_image(p.m.data(), img.data());
+                const auto bufs = scratch_.carve({tc_a_image_bytes(), sizeof(int)});
+                int *derr = reinterpret_cast<int *>(bufs[1]);
+                cuda_check(cudaMemcpyAsync(bufs[0], img.data(), tc_a_image_bytes(), cudaMemcpyHostToDevice, s_),
+                           "H2D matrix image");
+                cuda_check(cudaMemsetAsync(derr, 0, sizeof(int), s_), "clear error word");
+                launch_dense6_tc(s_, d_, tg, reinterpret_cast<const unsigned short *>(bufs[0]), derr);
+                int herr = 0;
+                cuda_check(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s_), "D2H error word");
+                synchronize(); // the scratch image is reused by the next call
+                PLGB_REQUIRE(herr == 0, "tensor-core dense block: a CTA timed out waiting for its MMAs");
+                return;
+            }
+        }
         LocalOffsets lo{};
         std::vector<u64> loc(D);
         for (size_t j = 0; j < D; j++) {

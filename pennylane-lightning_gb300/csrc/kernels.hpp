@@ -138,7 +138,14 @@ template <class T>
 void launch_mcmc_chain_local(cudaStream_t s, const cx<T> *sv, const unsigned char *site, const unsigned char *value,
                              const T *ran, u64 steps, u64 burnin, u64 *out);
 void launch_index_bits(cudaStream_t s, const u64 *idx, u64 shots, int n, long long *out);
-template <class T>
-void launch_probs_marginal(cudaStream_t s, const cx<T> *sv, u64 N, int k, const TBits &tb, double *out);
+// Marginal probabilities in the reference's summation order (bit-exact): k
+// wires at bit positions wb (wb[0] = most significant output bit), cmask =
+// the other bits
+struct MarginalGeom {
+    int k;
+    int wb[64];
+    u64 cmask;
+};
+template <class T> void launch_probs_marginal_serial(cudaStream_t s, const cx<T> *sv, const MarginalGeom &g, T *out);
 
 } // namespace plgb

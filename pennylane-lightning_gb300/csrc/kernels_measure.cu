@@ -459,50 +459,42 @@ template <class T> void launch_probs_all(cudaStream_t s, const cx<T> *sv, u64 N,
 
 // Marginal over k wires: shared-memory histogram for k <= 12, global
 // atomics beyond.  Output index bit (k-1-m) is wire m of the request.
+// Marginal probabilities summed in the reference's order, bit for bit: one
+// thread per output entry adds |a_idx|^2 (rounded as std::norm) in the
+// working precision over the indices with that entry's wire bits, in
+// increasing index order, starting from zero (MeasurementsLQubit.hpp:
+// 142-161 for five wires and more, and probs_bitshift in
+// MeasurementKernels.hpp for one to four wires, which sums in that order on
+// one thread).  The serial chain per entry is what makes the rounding equal.
 template <class T>
-__global__ void __launch_bounds__(256) k_probs_marginal(const cx<T> *__restrict__ a, u64 N, int k, TBits tb, double *out) {
-    extern __shared__ double hist[];
-    const int D = 1 << k;
-    const bool use_smem = k <= 12;
-    if (use_smem) {
-        for (int i = threadIdx.x; i < D; i += blockDim.x) {
-            hist[i] = 0.0;
-        }
-        __syncthreads();
+__global__ void __launch_bounds__(128) k_probs_marginal_serial(const cx<T> *__restrict__ a, MarginalGeom g, T *out) {
+    const u64 j = static_cast<u64>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j >= (u64{1} << g.k)) {
+        return;
     }
-    GRID_STRIDE(i, N) {
-        const cx<T> x = a[i];
-        const double p = static_cast<double>(x.x) * x.x + static_cast<double>(x.y) * x.y;
-        unsigned j = 0;
-        for (int m = 0; m < k; m++) {
-            j = (j << 1) | static_cast<unsigned>((i >> tb.b[m]) & 1U);
-        }
-        if (use_smem) {
-            atomicAdd(&hist[j], p);
+    u64 base = 0;
+    for (int m = 0; m < g.k; m++) {
+        base |= ((j >> (g.k - 1 - m)) & 1u) << g.wb[m];
+    }
+    const u64 cm = g.cmask;
+    T acc = 0;
+    u64 sub = 0;
+    do {
+        const cx<T> x = a[base | sub];
+        if constexpr (sizeof(T) == 8) {
+            acc = __dadd_rn(acc, norm_rn(x));
         } else {
-            atomicAdd(&out[j], p);
+            acc = __fadd_rn(acc, norm_rn(x));
         }
-    }
-    if (use_smem) {
-        __syncthreads();
-        for (int i = threadIdx.x; i < D; i += blockDim.x) {
-            if (hist[i] != 0.0) {
-                atomicAdd(&out[i], hist[i]);
-            }
-        }
-    }
+        sub = (sub - cm) & cm; // next subset of the complement bits, increasing
+    } while (sub != 0);
+    out[j] = acc;
 }
-template <class T>
-void launch_probs_marginal(cudaStream_t s, const cx<T> *sv, u64 N, int k, const TBits &tb, double *out) {
-    cuda_check(cudaMemsetAsync(out, 0, sizeof(double) << k, s), "probs memset");
-    const size_t smem = k <= 12 ? (sizeof(double) << k) : 0;
-    if (smem > 48 * 1024) {
-        cuda_check(cudaFuncSetAttribute(k_probs_marginal<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        static_cast<int>(smem)),
-                   "probs smem attribute");
-    }
-    k_probs_marginal<T><<<grid_for(N, 256, 2), 256, smem, s>>>(sv, N, k, tb, out);
-    cuda_check(cudaGetLastError(), "k_probs_marginal launch");
+template <class T> void launch_probs_marginal_serial(cudaStream_t s, const cx<T> *sv, const MarginalGeom &g, T *out) {
+    const u64 D = u64{1} << g.k;
+    const unsigned grid = static_cast<unsigned>((D + 127) / 128);
+    k_probs_marginal_serial<T><<<grid, 128, 0, s>>>(sv, g, out);
+    cuda_check(cudaGetLastError(), "k_probs_marginal_serial launch");
     note_launch();
 }
 
@@ -522,7 +514,7 @@ void launch_probs_marginal(cudaStream_t s, const cx<T> *sv, u64 N, int k, const 
     template void launch_pauli_apply<T>(cudaStream_t, const cx<T> *, cx<T> *, u64, const PauliGroupHdr *, int,    \
                                         const PauliTermDF *, int, bool);                                          \
     template void launch_probs_all<T>(cudaStream_t, const cx<T> *, u64, T *);                                    \
-    template void launch_probs_marginal<T>(cudaStream_t, const cx<T> *, u64, int, const TBits &, double *);
+    template void launch_probs_marginal_serial<T>(cudaStream_t, const cx<T> *, const MarginalGeom &, T *);
 
 PLGB_INST_MEAS(float)
 PLGB_INST_MEAS(double)

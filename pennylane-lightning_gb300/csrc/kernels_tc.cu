@@ -1,0 +1,451 @@
+// Dense 6-wire blocks of complex64 gates on the 5th-generation tensor cores.
+//
+// A dense 64 x 64 complex matrix U on six target bits maps every group of 64
+// amplitudes (the indices that differ only in those bits) to U times the
+// group.  Over a tile of 64 groups that is one real GEMM:
+//     D[128 x 64] = A[128 x 128] . B[128 x 64]
+// with A the real form of U (rows 2r + out-component, columns 2c +
+// in-component: [[Ur, -Ui], [Ui, Ur]] interleaved) and B the tile's groups
+// (column n = group, row 2c + component).  It runs as tcgen05.mma with
+// kind::f16 on BF16 operands (M = 128, N = 64, K = 16 per instruction), the
+// FP32 accumulator in tensor memory.  BF16 keeps 8 significant bits, so
+// every FP32 operand is split into three: x = h + m + l, h = bf16(x),
+// m = bf16(x - h), l = bf16(x - h - m), each rounded to nearest, which
+// represents the 24-bit significand exactly.  D is the sum of the six
+// products whose split indices add up to at most 2 (l.h, h.l, m.m, m.h,
+// h.m, h.h, smallest first); the three omitted ones are below 2^-24 of the
+// result, so a block is as accurate as an FP32 matrix product.
+//
+// Per CTA (256 threads, one per SM): the three splits of A (32 KiB each)
+// stay in shared memory for every tile; per tile the 4096 amplitudes are
+// loaded coalesced, split and written to the three B operands in the
+// canonical no-swizzle K-major layout (8 x 16-byte core matrices), one
+// thread issues the 48 MMAs and commits them to an mbarrier, all threads
+// read D back from tensor memory (tcgen05.ld), stage the tile in shared
+// memory in global order and store it coalesced.
+//
+// Tile geometry: the tile's 12 local bits are the six block bits and the
+// six lowest other bits; local index jj enumerates them in ascending global
+// position, so consecutive threads touch consecutive addresses.  The member
+// index i (row of U) and group index g are bit permutations of jj, split
+// into a thread part and a per-register part.
+//
+// Every wait is bounded: an mbarrier that does not complete within the
+// limit sets the error word, and the CTA stops issuing, frees its tensor
+// memory and returns; the host reads the word after the launch.
+#include "kernels_tc.hpp"
+
+#include <cuda_bf16.h>
+
+#include <atomic>
+#include <cstring>
+#include <vector>
+
+namespace plgb {
+
+namespace {
+
+constexpr int kTcThreads = 256;
+constexpr int kTcTileBits = 12;                  // 4096 amplitudes per tile
+constexpr int kTcPerThread = (1 << kTcTileBits) / kTcThreads; // 16
+constexpr unsigned kTcASplitBytes = 128u * 128u * 2u;         // one BF16 split of A: 32 KiB
+constexpr unsigned kTcBSplitBytes = 64u * 128u * 2u;          // one split of B: 16 KiB
+constexpr unsigned kTcSmemBytes = 3 * kTcASplitBytes + 3 * kTcBSplitBytes + 64;
+constexpr unsigned kTcTmemCols = 64;             // the 128 x 64 FP32 accumulator
+constexpr long long kTcWaitLimit = 1ll << 22;    // mbarrier polls before giving up
+
+// byte offset of element (row, k) in a no-swizzle K-major operand with 128
+// K elements of 2 bytes: core matrix (row / 8, k / 8) of 8 rows x 16 bytes;
+// K-adjacent core matrices 128 B apart (LBO), 8-row groups 2048 B apart (SBO)
+__host__ __device__ constexpr unsigned kmajor_off(unsigned row, unsigned k) {
+    return ((row >> 3) * 16u + (k >> 3)) * 128u + (row & 7u) * 16u + (k & 7u) * 2u;
+}
+constexpr unsigned kLbo = 128u, kSbo = 2048u;
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor (tcgen05): start address, leading
+// (K-direction) and stride (M/N-direction) byte offsets, all >> 4; bits
+// 46-47 = 1 (descriptor version); layout type 0 = no swizzle.
+__device__ __forceinline__ unsigned long long smem_desc(unsigned addr, unsigned lbo, unsigned sbo) {
+    unsigned long long d = 0;
+    d |= static_cast<unsigned long long>((addr >> 4) & 0x3FFFu);
+    d |= static_cast<unsigned long long>((lbo >> 4) & 0x3FFFu) << 16;
+    d |= static_cast<unsigned long long>((sbo >> 4) & 0x3FFFu) << 32;
+    d |= 1ull << 46;
+    return d;
+}
+
+// Instruction descriptor, kind::f16: D in FP32 (bits 4-5 = 1), A and B
+// BF16 (bits 7-9 and 10-12 = 1), both K-major, N >> 3 at bits 17-22,
+// M >> 4 at bits 24-28.
+constexpr unsigned kIdescBf16 = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+// true once the barrier's phase with parity `phase` has completed
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned phase) {
+    unsigned ok = 0;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(bar), "r"(phase)
+                 : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void proxy_fence_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_mma_bf16(unsigned dtmem, unsigned long long adesc, unsigned long long bdesc,
+                                            unsigned accumulate) {
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "setp.ne.u32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+                 "l"(adesc), "l"(bdesc), "r"(kIdescBf16), "r"(accumulate)
+                 : "memory");
+}
+__device__ __forceinline__ void tc_commit(unsigned bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+// 32 consecutive FP32 columns of this thread's tensor-memory lane
+__device__ __forceinline__ void tc_ld32(unsigned taddr, float (&v)[32]) {
+    unsigned r[32];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                 "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+                 "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                   "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+                   "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+                   "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int c = 0; c < 32; c++) {
+        v[c] = __uint_as_float(r[c]);
+    }
+}
+
+// x = h + m + l, three BF16 values rounded to nearest (exact for FP32 x);
+// returned as the bit patterns of the three
+__device__ __forceinline__ void split3(float x, unsigned short &h, unsigned short &m, unsigned short &l) {
+    const __nv_bfloat16 bh = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(bh);
+    const __nv_bfloat16 bm = __float2bfloat16_rn(r1);
+    const float r2 = r1 - __bfloat162float(bm);
+    const __nv_bfloat16 bl = __float2bfloat16_rn(r2);
+    h = __bfloat16_as_ushort(bh);
+    m = __bfloat16_as_ushort(bm);
+    l = __bfloat16_as_ushort(bl);
+}
+
+// bits of `v` at the positions of `map` (map[q] = destination bit of source
+// bit q, or -1) gathered into one word
+__device__ __forceinline__ unsigned scatter_bits(unsigned v, const signed char *map, int nbits) {
+    unsigned out = 0;
+    for (int q = 0; q < nbits; q++) {
+        if (map[q] >= 0) {
+            out |= ((v >> q) & 1u) << map[q];
+        }
+    }
+    return out;
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_dense6_tc(float2 *__restrict__ sv, TcGeom geom, const uint4 *__restrict__ a_img, int *__restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    // A splits h, m, l | B splits h, m, l | mbarrier | tensor-memory address
+    unsigned char *A0 = smem;
+    unsigned char *B0 = smem + 3 * kTcASplitBytes;
+    unsigned long long *mbar = reinterpret_cast<unsigned long long *>(B0 + 3 * kTcBSplitBytes);
+    unsigned *tslot = reinterpret_cast<unsigned *>(B0 + 3 * kTcBSplitBytes + 16);
+    float2 *stage = reinterpret_cast<float2 *>(B0); // the tile in local order, after the MMAs (32 of 48 KiB)
+
+    const unsigned tid = threadIdx.x;
+    const unsigned warp = tid >> 5, lane = tid & 31u;
+
+    for (unsigned i = tid; i < 3 * kTcASplitBytes / 16; i += kTcThreads) {
+        reinterpret_cast<uint4 *>(smem)[i] = a_img[i];
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                     "r"(kTcTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        mbar_init(smem_u32(mbar), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    proxy_fence_smem(); // A written by the generic proxy, read by the MMAs
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = *tslot;
+
+    // per-thread parts of the local index jj = r * 256 + tid
+    const unsigned i_t = scatter_bits(tid, geom.ibit, 8), g_t = scatter_bits(tid, geom.gbit, 8);
+    u64 off_t = 0;
+    for (int q = 0; q < 8; q++) {
+        off_t |= static_cast<u64>((tid >> q) & 1u) << geom.lbit[q];
+    }
+    unsigned i_r[kTcPerThread], g_r[kTcPerThread];
+    u64 off_r[kTcPerThread];
+#pragma unroll
+    for (int r = 0; r < kTcPerThread; r++) {
+        i_r[r] = scatter_bits(static_cast<unsigned>(r), geom.ibit + 8, 4);
+        g_r[r] = scatter_bits(static_cast<unsigned>(r), geom.gbit + 8, 4);
+        u64 o = 0;
+        for (int q = 0; q < 4; q++) {
+            o |= static_cast<u64>((r >> q) & 1) << geom.lbit[8 + q];
+        }
+        off_r[r] = o;
+    }
+
+    const unsigned a0 = smem_u32(A0), b0 = smem_u32(B0);
+    const unsigned bar = smem_u32(mbar);
+    unsigned phase = 0;
+    bool failed = false;
+
+    for (u64 tile = blockIdx.x; tile < geom.ntiles && !failed; tile += gridDim.x) {
+        // tile base: the tile number deposited into the non-local bits
+        u64 base = 0;
+        {
+            u64 t = tile;
+            for (int q = 0; q < geom.nglob; q++) {
+                base |= (t & 1u) << geom.glob[q];
+                t >>= 1;
+            }
+        }
+        // load (all sixteen in flight), split, write the two B operands
+        float2 vin[kTcPerThread];
+#pragma unroll
+        for (int r = 0; r < kTcPerThread; r++) {
+            vin[r] = __ldcs(&sv[base | off_t | off_r[r]]);
+        }
+#pragma unroll
+        for (int r = 0; r < kTcPerThread; r++) {
+            const float2 v = vin[r];
+            const unsigned i = i_t | i_r[r], g = g_t | g_r[r];
+            const unsigned o = kmajor_off(g, 2u * i); // (re, im) adjacent: k = 2i, 2i + 1
+            unsigned short xh, xm, xl, yh, ym, yl;
+            split3(v.x, xh, xm, xl);
+            split3(v.y, yh, ym, yl);
+            *reinterpret_cast<unsigned *>(B0 + o) = static_cast<unsigned>(xh) | (static_cast<unsigned>(yh) << 16);
+            *reinterpret_cast<unsigned *>(B0 + kTcBSplitBytes + o) =
+                static_cast<unsigned>(xm) | (static_cast<unsigned>(ym) << 16);
+            *reinterpret_cast<unsigned *>(B0 + 2 * kTcBSplitBytes + o) =
+                static_cast<unsigned>(xl) | (static_cast<unsigned>(yl) << 16);
+        }
+        proxy_fence_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            unsigned acc = 0;
+            // split pairs (A, B), smallest products first: l.h, h.l, m.m, m.h, h.m, h.h
+            const unsigned pa[6] = {2, 0, 1, 1, 0, 0}, pb[6] = {0, 2, 1, 0, 1, 0};
+            for (int p = 0; p < 6; p++) {
+                const unsigned as = a0 + pa[p] * kTcASplitBytes, bs = b0 + pb[p] * kTcBSplitBytes;
+#pragma unroll
+                for (int ks = 0; ks < 8; ks++) { // K = 16 per instruction: two 16-byte core columns
+                    const unsigned long long ad = smem_desc(as + ks * 256u, kLbo, kSbo);
+                    const unsigned long long bd = smem_desc(bs + ks * 256u, kLbo, kSbo);
+                    tc_mma_bf16(tmem, ad, bd, acc);
+                    acc = 1;
+                }
+            }
+            tc_commit(bar);
+        }
+        // wait for the MMAs (bounded)
+        long long polls = 0;
+        while (!mbar_try_wait(bar, phase)) {
+            if (++polls > kTcWaitLimit) {
+                failed = true;
+                break;
+            }
+        }
+        failed = __syncthreads_or(failed) != 0;
+        if (failed) {
+            if (tid == 0) {
+                atomicExch(err, 1);
+            }
+            break;
+        }
+        phase ^= 1u;
+        tc_fence_after();
+        // D row m = 32 (warp % 4) + lane: member i = m / 2, component m % 2;
+        // warps 0-3 read columns 0-31, warps 4-7 columns 32-63
+        float d[32];
+        const unsigned row = 32u * (warp & 3u) + lane;
+        const unsigned col0 = 32u * (warp >> 2);
+        tc_ld32(tmem + ((32u * (warp & 3u)) << 16) + col0, d);
+        // the MMAs have consumed B: the stage (over the B splits) may be written
+        __syncthreads();
+        {
+            const unsigned i = row >> 1, comp = row & 1u;
+            float *st = reinterpret_cast<float *>(stage);
+#pragma unroll
+            for (int c = 0; c < 32; c++) {
+                const unsigned g = col0 + static_cast<unsigned>(c);
+                st[2u * (geom.jj_of_i[i] | geom.jj_of_g[g]) + comp] = d[c];
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < kTcPerThread; r++) {
+            const unsigned jj = static_cast<unsigned>(r) * kTcThreads + tid;
+            __stcs(&sv[base | off_t | off_r[r]], stage[jj]);
+        }
+        __syncthreads(); // the stage is read before the next tile's B writes
+    }
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols)
+                     : "memory");
+    }
+}
+
+} // namespace
+
+bool tc_geom_for(int n, const int *bits6, TcGeom &g) {
+    if (n < kTcTileBits) {
+        return false;
+    }
+    bool blk[64] = {};
+    for (int m = 0; m < 6; m++) {
+        if (bits6[m] < 0 || bits6[m] >= n || blk[bits6[m]]) {
+            return false;
+        }
+        blk[bits6[m]] = true;
+    }
+    // local bits: the block bits and the six lowest others, ascending
+    int lbits[12], nl = 0, ng = 0;
+    int gsel[6];
+    for (int b = 0; b < n && ng < 6; b++) {
+        if (!blk[b]) {
+            gsel[ng++] = b;
+        }
+    }
+    bool loc[64] = {};
+    for (int m = 0; m < 6; m++) {
+        loc[bits6[m]] = true;
+        loc[gsel[m]] = true;
+    }
+    for (int b = 0; b < n; b++) {
+        if (loc[b]) {
+            lbits[nl++] = b;
+        }
+    }
+    std::memset(&g, 0, sizeof(g));
+    g.nglob = 0;
+    for (int b = 0; b < n; b++) {
+        if (!loc[b]) {
+            g.glob[g.nglob++] = b;
+        }
+    }
+    g.ntiles = u64{1} << (n - kTcTileBits);
+    for (int q = 0; q < 12; q++) {
+        g.lbit[q] = lbits[q];
+        g.ibit[q] = -1;
+        g.gbit[q] = -1;
+        for (int m = 0; m < 6; m++) {
+            if (bits6[m] == lbits[q]) {
+                g.ibit[q] = static_cast<signed char>(5 - m); // bits6[0] = most significant member bit
+            }
+            if (gsel[m] == lbits[q]) {
+                g.gbit[q] = static_cast<signed char>(m);
+            }
+        }
+    }
+    for (unsigned v = 0; v < 64; v++) {
+        unsigned ji = 0, jg = 0;
+        for (int q = 0; q < 12; q++) {
+            if (g.ibit[q] >= 0 && ((v >> g.ibit[q]) & 1u)) {
+                ji |= 1u << q;
+            }
+            if (g.gbit[q] >= 0 && ((v >> g.gbit[q]) & 1u)) {
+                jg |= 1u << q;
+            }
+        }
+        g.jj_of_i[v] = static_cast<unsigned short>(ji);
+        g.jj_of_g[v] = static_cast<unsigned short>(jg);
+    }
+    return true;
+}
+
+namespace {
+// FP32 -> BF16 bits, rounded to nearest even (finite inputs)
+unsigned short bf16_rn_bits(float x) {
+    unsigned u;
+    std::memcpy(&u, &x, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return static_cast<unsigned short>(u >> 16);
+}
+float bf16_to_float(unsigned short b) {
+    const unsigned u = static_cast<unsigned>(b) << 16;
+    float x;
+    std::memcpy(&x, &u, 4);
+    return x;
+}
+} // namespace
+
+void tc_build_a_image(const cx<float> *U, unsigned short *img) {
+    for (int m = 0; m < 128; m++) {
+        for (int k = 0; k < 128; k++) {
+            const int r = m >> 1, c = k >> 1;
+            const cx<float> u = U[r * 64 + c];
+            float v;
+            if ((m & 1) == 0) {
+                v = (k & 1) == 0 ? u.x : -u.y; // Re out = Ur Re in - Ui Im in
+            } else {
+                v = (k & 1) == 0 ? u.y : u.x;  // Im out = Ui Re in + Ur Im in
+            }
+            const unsigned short h = bf16_rn_bits(v);
+            const float r1 = v - bf16_to_float(h);
+            const unsigned short mm = bf16_rn_bits(r1);
+            const float r2 = r1 - bf16_to_float(mm);
+            const unsigned short l = bf16_rn_bits(r2);
+            const unsigned o = kmajor_off(static_cast<unsigned>(m), static_cast<unsigned>(k)) / 2u;
+            img[o] = h;
+            img[kTcASplitBytes / 2u + o] = mm;
+            img[kTcASplitBytes + o] = l;
+        }
+    }
+}
+
+size_t tc_a_image_bytes() { return 3 * kTcASplitBytes; }
+
+namespace {
+std::atomic<bool> g_tc_dense{true};
+}
+bool tc_dense_enabled() { return g_tc_dense.load(); }
+bool set_tc_dense_enabled(bool on) { return g_tc_dense.exchange(on); }
+
+void launch_dense6_tc(cudaStream_t s, cx<float> *sv, const TcGeom &geom, const unsigned short *a_img, int *err) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        cuda_check(cudaFuncSetAttribute(k_dense6_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes),
+                   "cudaFuncSetAttribute(k_dense6_tc)");
+        attr_set = true;
+    }
+    const u64 want = geom.ntiles;
+    const u64 cap = static_cast<u64>(LaunchGeom::sm_count());
+    const unsigned grid = static_cast<unsigned>(want < cap ? want : cap);
+    k_dense6_tc<<<grid, kTcThreads, kTcSmemBytes, s>>>(reinterpret_cast<float2 *>(sv), geom,
+                                                        reinterpret_cast<const uint4 *>(a_img), err);
+    cuda_check(cudaGetLastError(), "k_dense6_tc launch");
+    note_launch();
+}
+
+} // namespace plgb

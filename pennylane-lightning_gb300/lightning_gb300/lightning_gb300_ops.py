@@ -109,6 +109,12 @@ def set_c128_fp64_passes(on: bool) -> bool:
     return bool(lib().plgb_set_c128_fp64_passes(1 if on else 0))
 
 
+def set_tc_dense(on: bool) -> bool:
+    """Dense complex64 six-wire gates on the tensor cores (True, the
+    default) or the CUDA cores; returns the previous setting."""
+    return bool(lib().plgb_set_tc_dense(1 if on else 0))
+
+
 def backend_info() -> dict:
     """LQubitBindings.hpp:464-475."""
     return json.loads(_text("plgb_backend_info"))

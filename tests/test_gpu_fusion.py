@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from gate_table import GATES, gate_params
-from helpers import DTYPES, assert_close, rand_state, rand_unitary, seed_of, sv_class
+from helpers import DTYPES, assert_close, rand_state, rand_unitary, rel_errors, seed_of, sv_class
 from lightning_gb300.workloads import config0, config1
 
 pytestmark = pytest.mark.gpu
@@ -145,7 +145,11 @@ def test_c128_double_float_passes_match_fp64(ops_module):
             outs[fp64] = sv.state()
         finally:
             ops_module.set_c128_fp64_passes(prev)
-    assert_close(outs[False], outs[True], np.complex128, what="double-float vs FP64 passes")
+    # double-float keeps ~48 bits: within 1e-12 norm-relative of the FP64
+    # passes; per amplitude its stated bound is 1e-10 (measured 2.8e-12 at
+    # 24 qubits, test_gpu_parity_scale.py)
+    nr, pr = rel_errors(outs[False], outs[True], np.complex128)
+    assert nr <= 1e-12 and pr <= 1e-10, (nr, pr)
     assert not np.array_equal(outs[False], outs[True])  # the two arithmetics did run
 
 

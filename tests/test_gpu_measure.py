@@ -32,11 +32,12 @@ def _setup(ops, oracle, n, dt, seed):
 @pytest.mark.parametrize("dt", DTYPES)
 def test_probs_ordering(ops_module, oracle, dt):
     _, sv, m, o = _setup(ops_module, oracle, 7, dt, seed_of("probs", dt.__name__))
+    # the all-wires distribution is element-wise and every marginal is
+    # summed in the reference's order: bit-exact, in the output order the
+    # wire list gives
     for wires in WIRE_LISTS:
         p = m.probs() if wires is None else m.probs(wires)
-        assert_close(p, o.probs(wires), dt, what=f"probs {wires}")
-    # the all-wires distribution is computed element-wise: bit-exact
-    assert np.array_equal(m.probs().astype(np.float64), o.probs())
+        assert np.array_equal(np.asarray(p, np.float64), o.probs(wires)), wires
 
 
 @pytest.mark.parametrize("dt", DTYPES)

@@ -188,6 +188,21 @@ int plgb_ops_num_par_ops(const plgb_ops *ops, int *out);
  * passes are cached on `ops` per register size, precision and t).
  * *passes_out (optional) receives the number of kernel passes per call. */
 int plgb_sv_apply_operations(plgb_sv *sv, plgb_ops *ops, int tile_bits, int *passes_out);
+/* Dense-block fusion (no counterpart in the reference): the operations of
+ * `ops` merged, in order, into dense blocks on at most block_wires (1..6)
+ * wires, each applied as one dense kernel, i.e. one pass over the state.
+ * complex64 blocks on four to six wires run on the tensor cores (tcgen05,
+ * widened to six wires); the others on the CUDA cores.  The block list is
+ * cached on `ops` per register size, precision and width.  *blocks_out
+ * (optional) receives the number of kernels per call. */
+int plgb_sv_apply_operations_blocks(plgb_sv *sv, plgb_ops *ops, int block_wires, int *blocks_out);
+/* The block list of plgb_sv_apply_operations_blocks as JSON, computed on the
+ * host without a GPU: per block its kind (0 = one-wire pair, 2 = 4x4, 3 =
+ * dense 2^k) and targets (first = most significant local bit), and with
+ * with_matrices its row-major matrix as [re, im] pairs (no counterpart in
+ * the reference). */
+int plgb_ops_block_plan(const plgb_ops *ops, int num_qubits, int precision, int block_wires, int with_matrices,
+                        char *buf, size_t len);
 /* Arithmetic of complex128 fused passes, batched passes and the fused
  * adjoint sweep (no counterpart in the reference): on = 1 (default) runs
  * them in FP64, like the reference's kernels; on = 0 opts into double-float

@@ -40,6 +40,9 @@ struct plgb_ops {
     // compiled fused programs, keyed by (num_qubits, precision, tile bits)
     std::map<std::tuple<int, int, int>, std::shared_ptr<FusedProgram<float>>> prog_f;
     std::map<std::tuple<int, int, int>, std::shared_ptr<FusedProgram<double>>> prog_d;
+    // dense-block programs, keyed by (num_qubits, precision, block width)
+    std::map<std::tuple<int, int, int>, std::shared_ptr<const std::vector<Prim<float>>>> blk_f;
+    std::map<std::tuple<int, int, int>, std::shared_ptr<const std::vector<Prim<double>>>> blk_d;
     std::mutex mu;
 };
 
@@ -877,6 +880,44 @@ int plgb_sv_apply_operations(plgb_sv *sv, plgb_ops *ops, int tile_bits, int *pas
     });
 }
 
+int plgb_sv_apply_operations_blocks(plgb_sv *sv, plgb_ops *ops, int block_wires, int *blocks_out) {
+    return with_sv(sv, [&](auto &s) {
+        need(ops, "ops");
+        using T = decltype(s.data()->x);
+        PLGB_REQUIRE(block_wires >= 1 && block_wires <= 6, "block_wires must be in 1..6");
+        std::shared_ptr<const std::vector<Prim<T>>> prog;
+        {
+            std::lock_guard<std::mutex> lk(ops->mu);
+            const auto key = std::make_tuple(s.num_qubits(), static_cast<int>(sizeof(T)), block_wires);
+            auto &cache = [&]() -> auto & {
+                if constexpr (std::is_same_v<T, double>) {
+                    return ops->blk_d;
+                } else {
+                    return ops->blk_f;
+                }
+            }();
+            auto it = cache.find(key);
+            if (it == cache.end()) {
+                std::vector<Prim<T>> prims;
+                for (const auto &op : ops->list.ops) {
+                    auto p = s.lower_op(op, op.inverse);
+                    prims.insert(prims.end(), std::make_move_iterator(p.begin()), std::make_move_iterator(p.end()));
+                }
+                auto blocks = std::make_shared<const std::vector<Prim<T>>>(
+                    fuse_dense_blocks<T>(prims, s.num_qubits(), block_wires));
+                it = cache.emplace(key, std::move(blocks)).first;
+            }
+            prog = it->second;
+        }
+        for (const auto &p : *prog) {
+            s.run_prim(p);
+        }
+        if (blocks_out) {
+            *blocks_out = static_cast<int>(prog->size());
+        }
+    });
+}
+
 int plgb_ops_fusion_plan(const plgb_ops *ops, int num_qubits, int precision, int tile_bits, char *buf, size_t len) {
     std::string js;
     const int rc = guard([&] {
@@ -892,6 +933,58 @@ int plgb_ops_fusion_plan(const plgb_ops *ops, int num_qubits, int precision, int
                 prims.insert(prims.end(), std::make_move_iterator(p.begin()), std::make_move_iterator(p.end()));
             }
             js = fused_plan_json<T>(*compile_fused<T>(num_qubits, prims, tile_bits, false));
+        };
+        if (precision == 128) {
+            plan(double{});
+        } else {
+            plan(float{});
+        }
+    });
+    if (rc != PLGB_OK) {
+        return rc;
+    }
+    return copy_text(js, buf, len);
+}
+
+int plgb_ops_block_plan(const plgb_ops *ops, int num_qubits, int precision, int block_wires, int with_matrices,
+                        char *buf, size_t len) {
+    std::string js;
+    const int rc = guard([&] {
+        need(ops, "ops");
+        PLGB_REQUIRE(precision == 64 || precision == 128, "precision must be 64 or 128");
+        PLGB_REQUIRE(block_wires >= 1 && block_wires <= 6, "block_wires must be in 1..6");
+        auto plan = [&](auto tag) {
+            using T = decltype(tag);
+            StateVector<T> reg(num_qubits, LowerOnly{});
+            std::vector<Prim<T>> prims;
+            for (const auto &op : ops->list.ops) {
+                auto p = reg.lower_op(op, op.inverse);
+                prims.insert(prims.end(), std::make_move_iterator(p.begin()), std::make_move_iterator(p.end()));
+            }
+            const auto blocks = fuse_dense_blocks<T>(prims, num_qubits, block_wires);
+            js = "[";
+            char tmp[64];
+            for (size_t i = 0; i < blocks.size(); i++) {
+                const auto &p = blocks[i];
+                js += i ? ",{" : "{";
+                js += "\"kind\": " + std::to_string(static_cast<int>(p.kind)) + ", \"targets\": [";
+                for (size_t b = 0; b < p.tbits.size(); b++) {
+                    js += (b ? ", " : "") + std::to_string(p.tbits[b]);
+                }
+                js += "]";
+                if (with_matrices && p.cmask == 0 &&
+                    (p.kind == Prim<T>::Pair || p.kind == Prim<T>::Dense2 || p.kind == Prim<T>::DenseK)) {
+                    js += ", \"matrix\": [";
+                    for (size_t m = 0; m < p.m.size(); m++) {
+                        std::snprintf(tmp, sizeof(tmp), "%s[%.17g, %.17g]", m ? ", " : "",
+                                      static_cast<double>(p.m[m].x), static_cast<double>(p.m[m].y));
+                        js += tmp;
+                    }
+                    js += "]";
+                }
+                js += "}";
+            }
+            js += "]";
         };
         if (precision == 128) {
             plan(double{});

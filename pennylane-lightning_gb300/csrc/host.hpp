@@ -283,6 +283,10 @@ template <class T> void run_fused(StateVector<T> &sv, const FusedProgram<T> &pro
 template <class T>
 void run_fused_adjoint(StateVector<T> &lam, StateVector<T> &hlam, const FusedProgram<T> &prog, double *partials,
                        int G);
+// Dense-block fusion (host_blocks.cpp): the primitives merged into dense
+// blocks on at most kmax bits (Pair / Dense2 / DenseK primitives; others
+// pass through)
+template <class T> std::vector<Prim<T>> fuse_dense_blocks(const std::vector<Prim<T>> &prims, int n, int kmax);
 struct FusedStats {
     size_t passes, unfused, prims;
 };

@@ -17,8 +17,10 @@
 // result, so a block is as accurate as an FP32 matrix product.
 //
 // Per CTA (256 threads, one per SM): the three splits of A (32 KiB each)
-// stay in shared memory for every tile; per tile the 4096 amplitudes are
-// loaded coalesced, split and written to the three B operands in the
+// stay in shared memory for every tile.  Tiles arrive by 16-byte
+// asynchronous copies (cp.async) into two raw buffers, two tiles ahead, so
+// the loads of the next tiles overlap this tile's work.  Per tile the 4096
+// amplitudes are split and written to the three B operands in the
 // canonical no-swizzle K-major layout (8 x 16-byte core matrices), one
 // thread issues the 48 MMAs and commits them to an mbarrier, all threads
 // read D back from tensor memory (tcgen05.ld), stage the tile in shared
@@ -50,7 +52,9 @@ constexpr int kTcTileBits = 12;                  // 4096 amplitudes per tile
 constexpr int kTcPerThread = (1 << kTcTileBits) / kTcThreads; // 16
 constexpr unsigned kTcASplitBytes = 128u * 128u * 2u;         // one BF16 split of A: 32 KiB
 constexpr unsigned kTcBSplitBytes = 64u * 128u * 2u;          // one split of B: 16 KiB
-constexpr unsigned kTcSmemBytes = 3 * kTcASplitBytes + 3 * kTcBSplitBytes + 64;
+constexpr unsigned kTcRawBytes = 4096u * 8u;                 // one tile of complex64: 32 KiB
+constexpr int kTcChunksPerThread = 4096 * 8 / 16 / kTcThreads; // 16-byte copies per thread and tile
+constexpr unsigned kTcSmemBytes = 3 * kTcASplitBytes + 3 * kTcBSplitBytes + 2 * kTcRawBytes + 64;
 constexpr unsigned kTcTmemCols = 64;             // the 128 x 64 FP32 accumulator
 constexpr long long kTcWaitLimit = 1ll << 22;    // mbarrier polls before giving up
 
@@ -160,14 +164,44 @@ __device__ __forceinline__ unsigned scatter_bits(unsigned v, const signed char *
     return out;
 }
 
+__device__ __forceinline__ void cp_async16(unsigned dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// the tile number deposited into the non-local bits
+__device__ __forceinline__ u64 tile_base(const TcGeom &geom, u64 tile) {
+    u64 base = 0;
+    for (int q = 0; q < geom.nglob; q++) {
+        base |= (tile & 1u) << geom.glob[q];
+        tile >>= 1;
+    }
+    return base;
+}
+
+// Copy one tile (4096 amplitudes, local order) into a raw buffer with
+// 16-byte asynchronous copies: chunk c holds amplitudes 2c and 2c + 1, which
+// are adjacent in memory (local bit 0 is index bit 0).
+__device__ __forceinline__ void fetch_tile(const float2 *sv, u64 base, const u64 *coff, unsigned raw) {
+#pragma unroll
+    for (int r = 0; r < kTcChunksPerThread; r++) {
+        const unsigned c = static_cast<unsigned>(r) * kTcThreads + threadIdx.x;
+        cp_async16(raw + c * 16u, sv + (base | coff[r]));
+    }
+}
+
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_dense6_tc(float2 *__restrict__ sv, TcGeom geom, const uint4 *__restrict__ a_img, int *__restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    // A splits h, m, l | B splits h, m, l | mbarrier | tensor-memory address
+    // A splits h, m, l | B splits h, m, l | two raw tile buffers | mbarrier |
+    // tensor-memory address
     unsigned char *A0 = smem;
     unsigned char *B0 = smem + 3 * kTcASplitBytes;
-    unsigned long long *mbar = reinterpret_cast<unsigned long long *>(B0 + 3 * kTcBSplitBytes);
-    unsigned *tslot = reinterpret_cast<unsigned *>(B0 + 3 * kTcBSplitBytes + 16);
+    unsigned char *R0 = B0 + 3 * kTcBSplitBytes;
+    unsigned long long *mbar = reinterpret_cast<unsigned long long *>(R0 + 2 * kTcRawBytes);
+    unsigned *tslot = reinterpret_cast<unsigned *>(R0 + 2 * kTcRawBytes + 16);
     float2 *stage = reinterpret_cast<float2 *>(B0); // the tile in local order, after the MMAs (32 of 48 KiB)
 
     const unsigned tid = threadIdx.x;
@@ -210,31 +244,43 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         off_r[r] = o;
     }
+    // global offsets of this thread's copy chunks: local index 2c with
+    // c = r * 256 + tid (local bits 1-8 from tid, 9-11 from r)
+    u64 coff[kTcChunksPerThread];
+#pragma unroll
+    for (int r = 0; r < kTcChunksPerThread; r++) {
+        const unsigned c = static_cast<unsigned>(r) * kTcThreads + tid;
+        u64 o = 0;
+        for (int q = 0; q < 11; q++) {
+            o |= static_cast<u64>((c >> q) & 1u) << geom.lbit[q + 1];
+        }
+        coff[r] = o;
+    }
 
-    const unsigned a0 = smem_u32(A0), b0 = smem_u32(B0);
+    const unsigned a0 = smem_u32(A0), b0 = smem_u32(B0), r0 = smem_u32(R0);
     const unsigned bar = smem_u32(mbar);
     unsigned phase = 0;
     bool failed = false;
 
-    for (u64 tile = blockIdx.x; tile < geom.ntiles && !failed; tile += gridDim.x) {
-        // tile base: the tile number deposited into the non-local bits
-        u64 base = 0;
-        {
-            u64 t = tile;
-            for (int q = 0; q < geom.nglob; q++) {
-                base |= (t & 1u) << geom.glob[q];
-                t >>= 1;
-            }
+    // prefetch the first two tiles (one commit group each, empty when absent)
+    const u64 stride = gridDim.x;
+    u64 tile = blockIdx.x;
+    for (int k = 0; k < 2; k++) {
+        const u64 t = tile + static_cast<u64>(k) * stride;
+        if (t < geom.ntiles) {
+            fetch_tile(sv, tile_base(geom, t), coff, r0 + static_cast<unsigned>(k) * kTcRawBytes);
         }
-        // load (all sixteen in flight), split, write the two B operands
-        float2 vin[kTcPerThread];
+        cp_async_commit();
+    }
+    for (unsigned buf = 0; tile < geom.ntiles && !failed; tile += stride, buf ^= 1u) {
+        const u64 base = tile_base(geom, tile);
+        cp_async_wait1(); // this tile's group has landed (the next one may be in flight)
+        __syncthreads();
+        // split the tile (local order in the raw buffer) into the B operands
+        const float2 *raw = reinterpret_cast<const float2 *>(R0 + buf * kTcRawBytes);
 #pragma unroll
         for (int r = 0; r < kTcPerThread; r++) {
-            vin[r] = __ldcs(&sv[base | off_t | off_r[r]]);
-        }
-#pragma unroll
-        for (int r = 0; r < kTcPerThread; r++) {
-            const float2 v = vin[r];
+            const float2 v = raw[static_cast<unsigned>(r) * kTcThreads + tid];
             const unsigned i = i_t | i_r[r], g = g_t | g_r[r];
             const unsigned o = kmajor_off(g, 2u * i); // (re, im) adjacent: k = 2i, 2i + 1
             unsigned short xh, xm, xl, yh, ym, yl;
@@ -249,6 +295,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         proxy_fence_smem();
         tc_fence_before();
         __syncthreads();
+        // the raw buffer is consumed: fetch the tile after next into it
+        {
+            const u64 t = tile + 2 * stride;
+            if (t < geom.ntiles) {
+                fetch_tile(sv, tile_base(geom, t), coff, r0 + buf * kTcRawBytes);
+            }
+            cp_async_commit();
+        }
         if (tid == 0) {
             tc_fence_after();
             unsigned acc = 0;
@@ -284,20 +338,19 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         phase ^= 1u;
         tc_fence_after();
         // D row m = 32 (warp % 4) + lane: member i = m / 2, component m % 2;
-        // warps 0-3 read columns 0-31, warps 4-7 columns 32-63
-        float d[32];
-        const unsigned row = 32u * (warp & 3u) + lane;
-        const unsigned col0 = 32u * (warp >> 2);
-        tc_ld32(tmem + ((32u * (warp & 3u)) << 16) + col0, d);
-        // the MMAs have consumed B: the stage (over the B splits) may be written
-        __syncthreads();
+        // warps 0-3 read columns 0-31, warps 4-7 columns 32-63.  The MMAs
+        // have consumed B, so the stage (over the B splits) may be written.
         {
+            float d[32];
+            const unsigned row = 32u * (warp & 3u) + lane;
+            const unsigned col0 = 32u * (warp >> 2);
+            tc_ld32(tmem + ((32u * (warp & 3u)) << 16) + col0, d);
             const unsigned i = row >> 1, comp = row & 1u;
             float *st = reinterpret_cast<float *>(stage);
+            const unsigned ji = geom.jj_of_i[i];
 #pragma unroll
             for (int c = 0; c < 32; c++) {
-                const unsigned g = col0 + static_cast<unsigned>(c);
-                st[2u * (geom.jj_of_i[i] | geom.jj_of_g[g]) + comp] = d[c];
+                st[2u * (ji | geom.jj_of_g[col0 + static_cast<unsigned>(c)]) + comp] = d[c];
             }
         }
         tc_fence_before();
@@ -309,6 +362,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         __syncthreads(); // the stage is read before the next tile's B writes
     }
+    cp_async_wait0(); // no copy into shared memory outlives the CTA
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols)
@@ -346,6 +400,9 @@ bool tc_geom_for(int n, const int *bits6, TcGeom &g) {
         if (loc[b]) {
             lbits[nl++] = b;
         }
+    }
+    if (lbits[0] != 0) { // the 16-byte copies need adjacent amplitude pairs
+        return false;
     }
     std::memset(&g, 0, sizeof(g));
     g.nglob = 0;

@@ -64,6 +64,8 @@ SIGNATURES = {
     "plgb_gate_name": (C.c_char_p, [C.c_int]),
     "plgb_set_c128_fp64_passes": (C.c_int, [C.c_int]),
     "plgb_set_tc_dense": (C.c_int, [C.c_int]),
+    "plgb_sv_apply_operations_blocks": (C.c_int, [VP, VP, C.c_int, C.POINTER(C.c_int)]),
+    "plgb_ops_block_plan": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_char_p, C.c_size_t]),
     "plgb_set_tile_variant": (C.c_int, [C.c_int, C.c_int]),
     "plgb_set_lazy_fusion": (C.c_int, [C.c_int]),
     "plgb_sv_set_lazy": (C.c_int, [VP, C.c_int]),

@@ -289,6 +289,15 @@ class _StateVectorBase:
         call("plgb_sv_apply_operations", self._h, ops._h, int(tile_bits), C.byref(passes))
         return passes.value
 
+    def applyOperationsBlocks(self, ops, block_wires: int) -> int:
+        """Apply an OpsStruct list fused into dense blocks on at most
+        block_wires (1..6) wires, one kernel per block (complex64 blocks of
+        four to six wires on the tensor cores).  Returns the number of
+        kernels the call issued."""
+        blocks = C.c_int()
+        call("plgb_sv_apply_operations_blocks", self._h, ops._h, int(block_wires), C.byref(blocks))
+        return blocks.value
+
     def applyMatrix(self, matrix, wires, inverse: bool = False) -> None:
         m = _cmat(matrix)
         w, nw = _i64(wires)
@@ -673,6 +682,22 @@ class _OpsStructBase:
         buf = C.create_string_buffer(1 << 22)
         call("plgb_ops_fusion_plan", self._h, int(num_qubits), prec, int(tile_bits), buf, len(buf))
         return json.loads(buf.value.decode())
+
+    def block_plan(self, num_qubits: int, block_wires: int, matrices: bool = False) -> list:
+        """The dense blocks applyOperationsBlocks(block_wires) would run (no
+        GPU needed): per block its kind, targets and (optionally) matrix."""
+        prec = 64 if isinstance(self, OpsStructC64) else 128
+        size = 1 << 22
+        while True:
+            buf = C.create_string_buffer(size)
+            rc = lib().plgb_ops_block_plan(self._h, int(num_qubits), prec, int(block_wires), int(bool(matrices)),
+                                           buf, len(buf))
+            if rc == 0:
+                return json.loads(buf.value.decode())
+            msg = lib().plgb_last_error().decode()
+            if msg != "buffer too small":
+                raise LightningException(msg)
+            size <<= 2
 
     def num_par_ops(self) -> int:
         k = C.c_int()

@@ -517,7 +517,7 @@ template <class T> void StateVector<T>::run_prim(const Prim<T> &p) {
             TcGeom tg{};
             if (k == 6 && p.cmask == 0 && tc_dense_enabled() && tc_geom_for(n_, p.tbits.data(), tg)) {
                 std::vector<unsigned short> img(tc_a_image_bytes() / sizeof(unsigned short));
-                tc_build_a_image(p.m.data(), img.data());
+                tc_build_a_image(p.m.data(), tg, img.data());
                 const auto bufs = scratch_.carve({tc_a_image_bytes(), sizeof(int)});
                 int *derr = reinterpret_cast<int *>(bufs[1]);
                 cuda_check(cudaMemcpyAsync(bufs[0], img.data(), tc_a_image_bytes(), cudaMemcpyHostToDevice, s_),

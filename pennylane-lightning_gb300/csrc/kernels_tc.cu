@@ -29,8 +29,11 @@
 // Tile geometry: the tile's 12 local bits are the six block bits and the
 // six lowest other bits; local index jj enumerates them in ascending global
 // position, so consecutive threads touch consecutive addresses.  The member
-// index i (row of U) and group index g are bit permutations of jj, split
-// into a thread part and a per-register part.
+// index u (row of A in member order: bit q = the q-th lowest block bit) and
+// group index g are bit permutations of jj.  The split reads the raw tile
+// per (u, g) so that a warp writes 32 consecutive words of B; the raw
+// buffer and the output stage are XOR-swizzled (TcGeom) so that those reads
+// and the stage writes per tensor-memory lane are free of bank conflicts.
 //
 // Every wait is bounded: an mbarrier that does not complete within the
 // limit sets the error word, and the CTA stops issuing, frees its tensor
@@ -152,18 +155,6 @@ __device__ __forceinline__ void split3(float x, unsigned short &h, unsigned shor
     l = __bfloat16_as_ushort(bl);
 }
 
-// bits of `v` at the positions of `map` (map[q] = destination bit of source
-// bit q, or -1) gathered into one word
-__device__ __forceinline__ unsigned scatter_bits(unsigned v, const signed char *map, int nbits) {
-    unsigned out = 0;
-    for (int q = 0; q < nbits; q++) {
-        if (map[q] >= 0) {
-            out |= ((v >> q) & 1u) << map[q];
-        }
-    }
-    return out;
-}
-
 __device__ __forceinline__ void cp_async16(unsigned dst, const void *src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }
@@ -181,14 +172,15 @@ __device__ __forceinline__ u64 tile_base(const TcGeom &geom, u64 tile) {
     return base;
 }
 
-// Copy one tile (4096 amplitudes, local order) into a raw buffer with
-// 16-byte asynchronous copies: chunk c holds amplitudes 2c and 2c + 1, which
-// are adjacent in memory (local bit 0 is index bit 0).
-__device__ __forceinline__ void fetch_tile(const float2 *sv, u64 base, const u64 *coff, unsigned raw) {
+// Copy one tile (4096 amplitudes) into a raw buffer with 16-byte
+// asynchronous copies: chunk c holds amplitudes 2c and 2c + 1 of the local
+// order, adjacent in memory (local bit 0 is index bit 0), placed at their
+// swizzled position.
+__device__ __forceinline__ void fetch_tile(const float2 *sv, u64 base, const u64 *coff, const unsigned *cdst,
+                                           unsigned raw) {
 #pragma unroll
     for (int r = 0; r < kTcChunksPerThread; r++) {
-        const unsigned c = static_cast<unsigned>(r) * kTcThreads + threadIdx.x;
-        cp_async16(raw + c * 16u, sv + (base | coff[r]));
+        cp_async16(raw + cdst[r], sv + (base | coff[r]));
     }
 }
 
@@ -226,27 +218,49 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     tc_fence_after();
     const unsigned tmem = *tslot;
 
-    // per-thread parts of the local index jj = r * 256 + tid
-    const unsigned i_t = scatter_bits(tid, geom.ibit, 8), g_t = scatter_bits(tid, geom.gbit, 8);
+    // XOR swizzle of a local index (linear in its bits 4-11)
+    auto swz = [&](unsigned jj, const unsigned short *h) {
+        unsigned x = jj;
+#pragma unroll
+        for (int q = 4; q < 12; q++) {
+            x ^= ((jj >> q) & 1u) ? h[q] : 0u;
+        }
+        return x;
+    };
+    // store phase: local index jj = r * 256 + tid, read from the swizzled
+    // stage, written to global memory (consecutive threads, consecutive
+    // addresses)
     u64 off_t = 0;
     for (int q = 0; q < 8; q++) {
         off_t |= static_cast<u64>((tid >> q) & 1u) << geom.lbit[q];
     }
-    unsigned i_r[kTcPerThread], g_r[kTcPerThread];
+    const unsigned st_t = swz(tid, geom.hst);
+    unsigned st_r[kTcPerThread];
     u64 off_r[kTcPerThread];
 #pragma unroll
     for (int r = 0; r < kTcPerThread; r++) {
-        i_r[r] = scatter_bits(static_cast<unsigned>(r), geom.ibit + 8, 4);
-        g_r[r] = scatter_bits(static_cast<unsigned>(r), geom.gbit + 8, 4);
+        st_r[r] = swz(static_cast<unsigned>(r) << 8, geom.hst);
         u64 o = 0;
         for (int q = 0; q < 4; q++) {
             o |= static_cast<u64>((r >> q) & 1) << geom.lbit[8 + q];
         }
         off_r[r] = o;
     }
-    // global offsets of this thread's copy chunks: local index 2c with
-    // c = r * 256 + tid (local bits 1-8 from tid, 9-11 from r)
+    // split phase: this thread handles member u = (lane & 3) | (r << 2) of
+    // group g = (lane >> 2) | (warp << 3), so a warp's B stores are 32
+    // consecutive words; the raw tile is read at its swizzled position
+    const unsigned g_me = (lane >> 2) | (warp << 3);
+    const unsigned raw_t = swz(geom.jj_of_u[lane & 3u] | geom.jj_of_g[g_me], geom.hraw);
+    unsigned raw_r[kTcPerThread];
+#pragma unroll
+    for (int r = 0; r < kTcPerThread; r++) {
+        raw_r[r] = swz(geom.jj_of_u[static_cast<unsigned>(r) << 2], geom.hraw);
+    }
+    const unsigned b_t = (warp * 16u) * 128u + lane * 4u; // kmajor_off(g, 2u) for r = 0
+    // global offsets and swizzled raw positions of this thread's copy
+    // chunks: local index 2c with c = r * 256 + tid
     u64 coff[kTcChunksPerThread];
+    unsigned cdst[kTcChunksPerThread];
 #pragma unroll
     for (int r = 0; r < kTcChunksPerThread; r++) {
         const unsigned c = static_cast<unsigned>(r) * kTcThreads + tid;
@@ -255,7 +269,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             o |= static_cast<u64>((c >> q) & 1u) << geom.lbit[q + 1];
         }
         coff[r] = o;
+        cdst[r] = swz(2u * c, geom.hraw) * 8u; // byte offset of the pair (bit 0 is never swizzled)
     }
+    // stage writes: tensor-memory lane m = 32 (warp % 4) + lane is member
+    // u = m / 2, component m % 2
+    const unsigned row = 32u * (warp & 3u) + lane;
+    const unsigned st_u = geom.st_of_u[row >> 1];
+    const unsigned col0 = 32u * (warp >> 2);
 
     const unsigned a0 = smem_u32(A0), b0 = smem_u32(B0), r0 = smem_u32(R0);
     const unsigned bar = smem_u32(mbar);
@@ -268,7 +288,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     for (int k = 0; k < 2; k++) {
         const u64 t = tile + static_cast<u64>(k) * stride;
         if (t < geom.ntiles) {
-            fetch_tile(sv, tile_base(geom, t), coff, r0 + static_cast<unsigned>(k) * kTcRawBytes);
+            fetch_tile(sv, tile_base(geom, t), coff, cdst, r0 + static_cast<unsigned>(k) * kTcRawBytes);
         }
         cp_async_commit();
     }
@@ -276,13 +296,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const u64 base = tile_base(geom, tile);
         cp_async_wait1(); // this tile's group has landed (the next one may be in flight)
         __syncthreads();
-        // split the tile (local order in the raw buffer) into the B operands
+        // split the tile into the B operands
         const float2 *raw = reinterpret_cast<const float2 *>(R0 + buf * kTcRawBytes);
 #pragma unroll
         for (int r = 0; r < kTcPerThread; r++) {
-            const float2 v = raw[static_cast<unsigned>(r) * kTcThreads + tid];
-            const unsigned i = i_t | i_r[r], g = g_t | g_r[r];
-            const unsigned o = kmajor_off(g, 2u * i); // (re, im) adjacent: k = 2i, 2i + 1
+            const float2 v = raw[raw_t ^ raw_r[r]];
+            const unsigned o = b_t + static_cast<unsigned>(r) * 128u; // (re, im) adjacent: k = 2u, 2u + 1
             unsigned short xh, xm, xl, yh, ym, yl;
             split3(v.x, xh, xm, xl);
             split3(v.y, yh, ym, yl);
@@ -299,7 +318,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         {
             const u64 t = tile + 2 * stride;
             if (t < geom.ntiles) {
-                fetch_tile(sv, tile_base(geom, t), coff, r0 + buf * kTcRawBytes);
+                fetch_tile(sv, tile_base(geom, t), coff, cdst, r0 + buf * kTcRawBytes);
             }
             cp_async_commit();
         }
@@ -337,28 +356,24 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         phase ^= 1u;
         tc_fence_after();
-        // D row m = 32 (warp % 4) + lane: member i = m / 2, component m % 2;
-        // warps 0-3 read columns 0-31, warps 4-7 columns 32-63.  The MMAs
-        // have consumed B, so the stage (over the B splits) may be written.
+        // D row m = 32 (warp % 4) + lane; warps 0-3 read columns 0-31, warps
+        // 4-7 columns 32-63.  The MMAs have consumed B, so the stage (over
+        // the B splits) may be written.
         {
             float d[32];
-            const unsigned row = 32u * (warp & 3u) + lane;
-            const unsigned col0 = 32u * (warp >> 2);
             tc_ld32(tmem + ((32u * (warp & 3u)) << 16) + col0, d);
-            const unsigned i = row >> 1, comp = row & 1u;
             float *st = reinterpret_cast<float *>(stage);
-            const unsigned ji = geom.jj_of_i[i];
+            const unsigned comp = row & 1u;
 #pragma unroll
             for (int c = 0; c < 32; c++) {
-                st[2u * (ji | geom.jj_of_g[col0 + static_cast<unsigned>(c)]) + comp] = d[c];
+                st[2u * (st_u ^ geom.st_of_g[col0 + static_cast<unsigned>(c)]) + comp] = d[c];
             }
         }
         tc_fence_before();
         __syncthreads();
 #pragma unroll
         for (int r = 0; r < kTcPerThread; r++) {
-            const unsigned jj = static_cast<unsigned>(r) * kTcThreads + tid;
-            __stcs(&sv[base | off_t | off_r[r]], stage[jj]);
+            __stcs(&sv[base | off_t | off_r[r]], stage[st_t ^ st_r[r]]);
         }
         __syncthreads(); // the stage is read before the next tile's B writes
     }
@@ -384,59 +399,97 @@ bool tc_geom_for(int n, const int *bits6, TcGeom &g) {
         blk[bits6[m]] = true;
     }
     // local bits: the block bits and the six lowest others, ascending
-    int lbits[12], nl = 0, ng = 0;
-    int gsel[6];
-    for (int b = 0; b < n && ng < 6; b++) {
-        if (!blk[b]) {
+    int bsel[6], gsel[6], nb = 0, ng = 0;
+    for (int b = 0; b < n; b++) {
+        if (blk[b]) {
+            bsel[nb++] = b;
+        } else if (ng < 6) {
             gsel[ng++] = b;
         }
     }
     bool loc[64] = {};
     for (int m = 0; m < 6; m++) {
-        loc[bits6[m]] = true;
+        loc[bsel[m]] = true;
         loc[gsel[m]] = true;
     }
+    std::memset(&g, 0, sizeof(g));
+    int pos[64];
+    int nl = 0;
     for (int b = 0; b < n; b++) {
         if (loc[b]) {
-            lbits[nl++] = b;
-        }
-    }
-    if (lbits[0] != 0) { // the 16-byte copies need adjacent amplitude pairs
-        return false;
-    }
-    std::memset(&g, 0, sizeof(g));
-    g.nglob = 0;
-    for (int b = 0; b < n; b++) {
-        if (!loc[b]) {
+            pos[b] = nl;
+            g.lbit[nl++] = b;
+        } else {
             g.glob[g.nglob++] = b;
         }
     }
+    if (g.lbit[0] != 0) { // the 16-byte copies need adjacent amplitude pairs
+        return false;
+    }
     g.ntiles = u64{1} << (n - kTcTileBits);
-    for (int q = 0; q < 12; q++) {
-        g.lbit[q] = lbits[q];
-        g.ibit[q] = -1;
-        g.gbit[q] = -1;
-        for (int m = 0; m < 6; m++) {
-            if (bits6[m] == lbits[q]) {
-                g.ibit[q] = static_cast<signed char>(5 - m); // bits6[0] = most significant member bit
-            }
-            if (gsel[m] == lbits[q]) {
-                g.gbit[q] = static_cast<signed char>(m);
-            }
-        }
+    int upos[6], gpos[6];
+    for (int q = 0; q < 6; q++) {
+        upos[q] = pos[bsel[q]];
+        gpos[q] = pos[gsel[q]];
     }
     for (unsigned v = 0; v < 64; v++) {
-        unsigned ji = 0, jg = 0;
-        for (int q = 0; q < 12; q++) {
-            if (g.ibit[q] >= 0 && ((v >> g.ibit[q]) & 1u)) {
-                ji |= 1u << q;
-            }
-            if (g.gbit[q] >= 0 && ((v >> g.gbit[q]) & 1u)) {
-                jg |= 1u << q;
+        unsigned ju = 0, jg = 0, mi = 0;
+        for (int q = 0; q < 6; q++) {
+            if ((v >> q) & 1u) {
+                ju |= 1u << upos[q];
+                jg |= 1u << gpos[q];
+                for (int m = 0; m < 6; m++) {
+                    if (bits6[m] == bsel[q]) {
+                        mi |= 1u << (5 - m); // bits6[0] = the matrix's most significant bit
+                    }
+                }
             }
         }
-        g.jj_of_i[v] = static_cast<unsigned short>(ji);
+        g.jj_of_u[v] = static_cast<unsigned short>(ju);
         g.jj_of_g[v] = static_cast<unsigned short>(jg);
+        g.mat_of_u[v] = static_cast<unsigned short>(mi);
+    }
+    // Swizzles: the jj bits that vary across the lanes of a half-warp at
+    // positions 4 and up are mapped onto the free positions among the
+    // bank-selecting ones.  Raw buffer (8-byte reads, pairs kept together):
+    // lanes vary u0, u1, g0, g1; positions 1-3 are available.  Stage
+    // (4-byte writes of (u, component)): lanes vary u0-u3; positions 0-3.
+    auto assign = [&](const int *lanes, int nlanes, int first, unsigned short *h) {
+        bool used[4] = {};
+        for (int i = 0; i < nlanes; i++) {
+            if (lanes[i] >= first && lanes[i] < 4) {
+                used[lanes[i]] = true;
+            }
+        }
+        for (int i = 0; i < nlanes; i++) {
+            if (lanes[i] < 4) {
+                continue;
+            }
+            for (int s = first; s < 4; s++) {
+                if (!used[s]) {
+                    used[s] = true;
+                    h[lanes[i]] = static_cast<unsigned short>(1u << s);
+                    break;
+                }
+            }
+        }
+    };
+    const int raw_lanes[4] = {upos[0], upos[1], gpos[0], gpos[1]};
+    const int st_lanes[4] = {upos[0], upos[1], upos[2], upos[3]};
+    assign(raw_lanes, 4, 1, g.hraw);
+    assign(st_lanes, 4, 0, g.hst);
+    auto swz = [&](unsigned jj, const unsigned short *h) {
+        unsigned x = jj;
+        for (int q = 4; q < 12; q++) {
+            if ((jj >> q) & 1u) {
+                x ^= h[q];
+            }
+        }
+        return x;
+    };
+    for (unsigned v = 0; v < 64; v++) {
+        g.st_of_u[v] = static_cast<unsigned short>(swz(g.jj_of_u[v], g.hst));
+        g.st_of_g[v] = static_cast<unsigned short>(swz(g.jj_of_g[v], g.hst));
     }
     return true;
 }
@@ -457,10 +510,10 @@ float bf16_to_float(unsigned short b) {
 }
 } // namespace
 
-void tc_build_a_image(const cx<float> *U, unsigned short *img) {
+void tc_build_a_image(const cx<float> *U, const TcGeom &geom, unsigned short *img) {
     for (int m = 0; m < 128; m++) {
         for (int k = 0; k < 128; k++) {
-            const int r = m >> 1, c = k >> 1;
+            const int r = geom.mat_of_u[m >> 1], c = geom.mat_of_u[k >> 1];
             const cx<float> u = U[r * 64 + c];
             float v;
             if ((m & 1) == 0) {

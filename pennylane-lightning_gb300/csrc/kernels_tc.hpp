@@ -6,28 +6,38 @@
 
 namespace plgb {
 
-// Tile geometry of a 6-wire block on an n-qubit register: the 12 local bits
-// (block bits and the six lowest other bits) in ascending order, and for
-// each local index bit q which member bit (ibit) or group bit (gbit) it is.
+// Tile geometry of a 6-wire block on an n-qubit register.  The tile's 12
+// local bits (the block bits and the six lowest other bits) in ascending
+// order give the local index jj.  Member index u (the block's own index,
+// bit q = the q-th lowest block bit) and group index g (bit q = the q-th
+// lowest other local bit) are bit permutations of jj.  Two shared-memory
+// buffers are XOR-swizzled on jj (linear maps of jj's bits 4-11 into bits
+// 0-3) so that the accesses of a warp fall in distinct banks: the raw tile
+// (read per (u, g) in the split) and the output stage (written per tensor
+// memory lane).
 struct TcGeom {
-    signed char ibit[12];
-    signed char gbit[12];
     int lbit[12];
     int glob[64];
     int nglob;
     u64 ntiles;
-    unsigned short jj_of_i[64];
+    unsigned short jj_of_u[64];
     unsigned short jj_of_g[64];
+    unsigned short hraw[12]; // XOR mask of raw-buffer position per jj bit
+    unsigned short hst[12];  // XOR mask of stage position per jj bit
+    unsigned short st_of_u[64], st_of_g[64]; // swizzled stage positions of u and g alone
+    unsigned short mat_of_u[64];             // row of the caller's matrix for member u
 };
 
 // false when the register is too small (fewer than 12 qubits) or the bits
 // are not six distinct positions below n; bits6[0] = the matrix's most
 // significant local bit (its first wire)
 bool tc_geom_for(int n, const int *bits6, TcGeom &g);
-// the shared-memory image of a row-major 64 x 64 complex64 matrix: its real
-// form split into three BF16 parts (h, m, l) in the MMA operand layout
+// the shared-memory image of a row-major 64 x 64 complex64 matrix (first
+// wire = most significant bit) for the geometry: its real form, rows and
+// columns in member order, split into three BF16 parts (h, m, l) in the MMA
+// operand layout
 size_t tc_a_image_bytes();
-void tc_build_a_image(const cx<float> *U, unsigned short *img);
+void tc_build_a_image(const cx<float> *U, const TcGeom &geom, unsigned short *img);
 // sv <- U on every group of the six bits (img: device copy of the image;
 // err: device word set to 1 when a CTA gave up waiting for its MMAs)
 void launch_dense6_tc(cudaStream_t s, cx<float> *sv, const TcGeom &geom, const unsigned short *a_img, int *err);

@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference", "cpu-sample"])
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference", "cpu-sample", "cpu-configs"])
     ap.add_argument("--qubits", type=int, default=30)
     ap.add_argument("--cycles", type=int, default=20)
     ap.add_argument("--tile-bits", type=int, default=None,
@@ -56,11 +56,13 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-circuits leg (config 2)")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the autograd adjoint leg (config 3)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg (config 4)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the config-0 / config-3 GPU-and-host-cores comparison")
     ap.add_argument("--adjoint-qubits", type=int, default=28, help="config-3 register size (32: the 64 GiB variant)")
     ap.add_argument("--adjoint-layers", type=int, default=12, help="config-3 layers (6 for the 32-qubit variant)")
     ap.add_argument("--adjoint-fd", type=int, default=0,
                     help="also check this many sampled gradient entries by central finite differences")
-    ap.add_argument("--serve-seconds", type=float, default=2.0,
+    ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="length of the config-4 arrival window replayed by the serving leg")
     return ap.parse_args()
 
@@ -401,10 +403,50 @@ def gpu_arm(args) -> dict | None:
             timed_step(sv64, S64, s64, tb)
             t64[tb] = timed_step(sv64, S64, s64, tb)[0]
         b64 = min(t64, key=t64.get)
-        res["c64"] = {"value": updates / (t64[b64] / 1e3) / 1e9, "unit": UNIT,
-                      "ms_per_step": t64[b64], "tile_bits": b64,
-                      "tuning_ms_per_step": {str(k): round(v, 1) for k, v in sorted(t64.items())}}
+        # dense-block fusion, fusion widths k = 2..6 (complex64 blocks of 4-6
+        # wires on the tensor cores)
+        def timed_blocks(svb, S, st, k):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            nk = svb.applyOperationsBlocks(S, k)
+            b.record(st)
+            svb.synchronize()
+            return a.elapsed_time(b), nk
+        blk64 = {}
+        for k in (2, 3, 4, 5, 6):
+            timed_blocks(sv64, S64, s64, k)
+            ms, nk = timed_blocks(sv64, S64, s64, k)
+            blk64[k] = {"ms_per_step": ms, "kernels": nk, "value": updates / (ms / 1e3) / 1e9}
+        kb = min(blk64, key=lambda k: blk64[k]["ms_per_step"])
+        best = ("blocks", kb, blk64[kb]["ms_per_step"]) if blk64[kb]["ms_per_step"] < t64[b64] else \
+            ("tiles", b64, t64[b64])
+        res["c64"] = {"value": updates / (best[2] / 1e3) / 1e9, "unit": UNIT, "ms_per_step": best[2],
+                      "path": (f"dense blocks of up to {kb} wires (tensor cores for 4-6 wires)" if best[0] == "blocks"
+                               else f"fused tile passes, 2^{b64} amplitudes per tile"),
+                      "tile_passes_ms_per_step": {str(k): round(v, 1) for k, v in sorted(t64.items())},
+                      "fusion_width_sweep": {str(k): {"ms_per_step": round(v["ms_per_step"], 1),
+                                                      "kernels": v["kernels"],
+                                                      "value": v["value"]} for k, v in blk64.items()}}
         del sv64
+        # the same sweep in complex128 (dense FP64 blocks on the CUDA cores)
+        # at 26 qubits: a dense 2^k block costs 4 * 2^k FP64 multiply-adds per
+        # amplitude, so this is a reference point, not a fast path
+        n_sw = min(n, 26)
+        circ_sw, _ = config1_circuit(n_sw, cycles)
+        S_sw = ops.OpsStructC128([o.name for o in circ_sw], [o.params for o in circ_sw],
+                                 [o.wires for o in circ_sw], [False] * len(circ_sw),
+                                 [o.matrix for o in circ_sw])
+        sv_sw = ops.StateVectorC128(n_sw)
+        st_sw = torch.cuda.ExternalStream(sv_sw.cuda_stream())
+        sweep128 = {}
+        for k in (2, 3, 4, 5, 6):
+            timed_blocks(sv_sw, S_sw, st_sw, k)
+            ms, nk = timed_blocks(sv_sw, S_sw, st_sw, k)
+            sweep128[str(k)] = {"ms_per_step": round(ms, 1), "kernels": nk}
+        ms_t, p_t = timed_step(sv_sw, S_sw, st_sw, best_tb)
+        res["c128_fusion_width_sweep"] = {"qubits": n_sw, "blocks": sweep128,
+                                          "fused_tile_passes": {"ms_per_step": round(ms_t, 1), "passes": p_t}}
+        del sv_sw
     if rank == 0:
         if not args.no_batch:
             res["batched"] = {"c128": batched_leg(ops, 128), "c64": batched_leg(ops, 64)}
@@ -617,6 +659,94 @@ def cpu_description(n_cpu: int, ng: int) -> str:
             f"the host cores (no AVX kernels on this host)")
 
 
+def _median_time(f, reps=3):
+    f()  # warm-up
+    ts = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        f()
+        ts.append(time.perf_counter() - t)
+    return statistics.median(ts)
+
+
+CONFIG3_CPU_QUBITS = 22  # config-3 size timed on both the host cores and the GPU
+
+
+def cpu_configs_leg(orc) -> dict:
+    """Configs 0 and 3 on the host cores (the oracle: the reference's
+    algorithm with OpenMP): config 0 at its full size (20 qubits, 10 layers,
+    600 parameters) and config 3 at 22 qubits (12 layers, 792 parameters,
+    200-term Hamiltonian)."""
+    from lightning_gb300.workloads import config0, config3, sum_z
+    from oracle.pyoracle import pauli_sum_spec
+
+    out = {"cores": orc.num_threads(), "host": host_cpu()}
+    c0 = config0(20, 10, seed=1000)
+    spec0 = pauli_sum_spec(sum_z(20).terms())
+    sv = orc.sv(20, np.complex128)
+
+    def fwd():
+        sv.set_basis_state([0] * 20, list(range(20)))
+        for op in c0:
+            sv.apply(op.name, op.wires, False, op.params)
+        sv.state()
+
+    tp0 = list(range(sum(1 for o in c0 if o.params)))
+    out["config0"] = {"qubits": 20, "params": len(tp0), "forward_s": _median_time(fwd),
+                      "expval_s": _median_time(lambda: sv.expval_obs(spec0)),
+                      "adjoint_s": _median_time(lambda: orc.sv(20, np.complex128).adjoint(
+                          [o.as_dict() for o in c0], [spec0], tp0, apply_ops=True), reps=1)}
+    n3 = CONFIG3_CPU_QUBITS
+    c3, h3 = config3(n3, 12, seed=1003, nterms=200)
+    tp3 = list(range(sum(1 for o in c3 if o.params)))
+    out["config3"] = {"qubits": n3, "params": len(tp3), "terms": 200,
+                      "adjoint_s": _median_time(lambda: orc.sv(n3, np.complex128).adjoint(
+                          [o.as_dict() for o in c3], [pauli_sum_spec(h3.terms())], tp3, apply_ops=True), reps=1)}
+    return out
+
+
+def gpu_configs_leg(ops) -> dict:
+    """Configs 0 and 3 on the GPU through the binding, as lightning.qubit's
+    device calls it: one call per gate, then expval and the adjoint
+    Jacobian (complex128)."""
+    from lightning_gb300.workloads import config0, config3
+
+    out = {}
+    c0 = config0(20, 10, seed=1000)
+    H = ops.observables.HamiltonianC128([1.0] * 20, [ops.observables.NamedObsC128("PauliZ", [q]) for q in range(20)])
+    st = np.empty(1 << 20, np.complex128)
+    holder = {}
+
+    def fwd():
+        sv = ops.StateVectorC128(20)
+        for op in c0:
+            getattr(sv, op.name)(op.wires, False, op.params)
+        sv.getState(st)
+        holder["sv"] = sv
+
+    S0 = ops.OpsStructC128([o.name for o in c0], [o.params for o in c0], [o.wires for o in c0], [False] * len(c0),
+                           [None] * len(c0))
+    tp0 = list(range(sum(1 for o in c0 if o.params)))
+    fwd_s = _median_time(fwd)
+    m = ops.MeasurementsC128(holder["sv"])
+    out["config0"] = {"qubits": 20, "params": len(tp0), "forward_s": fwd_s,
+                      "expval_s": _median_time(lambda: m.expval(H)),
+                      "adjoint_s": _median_time(lambda: ops.AdjointJacobianC128()(ops.StateVectorC128(20), [H], S0,
+                                                                                    tp0, True))}
+    n3 = CONFIG3_CPU_QUBITS
+    c3, h3 = config3(n3, 12, seed=1003, nterms=200)
+    names = {"X": "PauliX", "Y": "PauliY", "Z": "PauliZ"}
+    H3 = ops.observables.HamiltonianC128(list(h3.coeffs), [ops.observables.TensorProdObsC128(
+        [ops.observables.NamedObsC128(names[c], [w]) for c, w in zip(wd, ws)]) for wd, ws in zip(h3.words, h3.wires)])
+    S3 = ops.OpsStructC128([o.name for o in c3], [o.params for o in c3], [o.wires for o in c3], [False] * len(c3),
+                           [None] * len(c3))
+    tp3 = list(range(sum(1 for o in c3 if o.params)))
+    out["config3"] = {"qubits": n3, "params": len(tp3), "terms": 200,
+                      "adjoint_s": _median_time(lambda: ops.AdjointJacobianC128()(ops.StateVectorC128(n3), [H3], S3,
+                                                                                    tp3, True))}
+    return out
+
+
 def reference_arm(args) -> None:
     ws, rank, _ = dist_info()
     if rank != 0:
@@ -665,6 +795,9 @@ def main():
         reference_arm(args)
         return
     ws, rank, _ = dist_info()
+    if args.impl == "cpu-configs":
+        print(json.dumps(cpu_configs_leg(cpu_setup())))
+        return
     if args.impl == "cpu-sample":
         # child process of the CPU baseline: OpenMP thread binding stays out
         # of the GPU process (its host threads compile circuits in parallel)
@@ -681,9 +814,23 @@ def main():
                               str(args.qubits), "--cycles", str(args.cycles)], capture_output=True, text=True,
                              check=True)
         cpu = json.loads(out.stdout.strip().splitlines()[-1])
+    cpu_cfg = None
+    if rank == 0 and not args.no_cpu and not args.no_configs:
+        out = subprocess.run([sys.executable, str(Path(__file__).resolve()), "--impl", "cpu-configs"],
+                             capture_output=True, text=True, check=True)
+        cpu_cfg = json.loads(out.stdout.strip().splitlines()[-1])
     res = gpu_arm(args)
     if rank == 0 and res is not None:
         res["cpu_baseline"] = cpu
+        if not args.no_configs:
+            from lightning_gb300 import lightning_gb300_ops as ops
+
+            g = gpu_configs_leg(ops)
+            cmp = {"gpu": g, "cpu": cpu_cfg}
+            if cpu_cfg is not None:
+                cmp["speedup"] = {c: {k: cpu_cfg[c][k] / g[c][k] for k in g[c] if k.endswith("_s")}
+                                  for c in ("config0", "config3")}
+            res["configs_0_3"] = cmp
         print(json.dumps(res))
 
 

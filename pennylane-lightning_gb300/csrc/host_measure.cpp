@@ -474,20 +474,125 @@ double Measure<T>::var_sparse(StateVector<T> &sv, const int64_t *indptr, int64_t
     return var_obs(sv, o);
 }
 
+// <psi| sum_t c_t P_t |psi> by passes (launch_pauli_pass): the words are
+// packed, in order of their flip masks, into passes of at most kPassTerms
+// words whose flip bits together leave at least four of the tile's local
+// bits for the lowest index bits (coalesced tile loads); one read of the
+// state per pass.  Each word's sum is scaled by its coefficient on the host
+// and added in word order (deterministic).
+template <class T> double pauli_expval_passes(StateVector<T> &sv, const PauliSum &ps) {
+    const int n = sv.num_qubits();
+    const int t = std::min(n, kPassMaxTileBits);
+    struct W {
+        double coef;
+        const PauliSum::Term *term;
+    };
+    std::vector<W> words;
+    for (const auto &tm : ps.terms) {
+        const int par = __builtin_popcountll(tm.x & tm.yz) & 1;
+        const bool odd = (tm.ny4 & 1) != 0;
+        if (tm.x != 0 && par != (odd ? 1 : 0)) {
+            continue; // purely imaginary on every pair: no real part
+        }
+        double coef = tm.c;
+        if (tm.x != 0) {
+            coef = (tm.ny4 == 0 || tm.ny4 == 1) ? 2.0 * tm.c : -2.0 * tm.c;
+        } else if (tm.ny4 != 0) {
+            coef = tm.ny4 == 2 ? -tm.c : 0.0; // i^ny on a diagonal word: real part only
+        }
+        if (coef != 0.0) {
+            words.push_back({coef, &tm});
+        }
+    }
+    std::stable_sort(words.begin(), words.end(), [](const W &a, const W &b) { return a.term->x < b.term->x; });
+    std::vector<std::pair<size_t, size_t>> passes; // [begin, end) of words
+    {
+        size_t b = 0;
+        u64 U = 0;
+        for (size_t i = 0; i < words.size(); i++) {
+            const u64 nu = U | words[i].term->x;
+            const int lim = std::max(t - 4, __builtin_popcountll(words[i].term->x));
+            if (i > b && (i - b == static_cast<size_t>(kPassTerms) || __builtin_popcountll(nu) > lim)) {
+                passes.emplace_back(b, i);
+                b = i;
+                U = words[i].term->x;
+            } else {
+                U = nu;
+            }
+        }
+        if (b < words.size()) {
+            passes.emplace_back(b, words.size());
+        }
+    }
+    if (passes.empty()) {
+        return 0.0;
+    }
+    const u64 N = sv.length();
+    const size_t max_grid = static_cast<size_t>(LaunchGeom::sm_count()) * 8;
+    const auto bufs = sv.scratch().carve({max_grid * kPassTerms * sizeof(double),
+                                         passes.size() * kPassTerms * sizeof(double)});
+    double *partials = reinterpret_cast<double *>(bufs[0]);
+    double *outs = reinterpret_cast<double *>(bufs[1]);
+    for (size_t pi = 0; pi < passes.size(); pi++) {
+        PauliPass pp{};
+        pp.t = t;
+        u64 U = 0;
+        for (size_t i = passes[pi].first; i < passes[pi].second; i++) {
+            U |= words[i].term->x;
+        }
+        u64 L = U;
+        for (int b = 0; b < n && __builtin_popcountll(L) < t; b++) {
+            L |= u64{1} << b;
+        }
+        int nl = 0;
+        for (int b = 0; b < n; b++) {
+            if ((L >> b) & 1u) {
+                pp.lbit[nl++] = b;
+            } else {
+                pp.glob[pp.nglob++] = b;
+            }
+        }
+        pp.ntiles = N >> t;
+        auto gather = [&](u64 m) {
+            unsigned out = 0;
+            for (int q = 0; q < t; q++) {
+                if ((m >> pp.lbit[q]) & 1u) {
+                    out |= 1u << q;
+                }
+            }
+            return out;
+        };
+        pp.nterms = static_cast<int>(passes[pi].second - passes[pi].first);
+        for (int w = 0; w < pp.nterms; w++) {
+            const auto *tm = words[passes[pi].first + static_cast<size_t>(w)].term;
+            PauliPassTerm &pt = pp.term[w];
+            pt.yz = tm->yz;
+            pt.x = gather(tm->x);
+            pt.yzl = gather(tm->yz);
+            pt.hb = pt.x ? 31 - __builtin_clz(pt.x) : 0;
+            pt.im = (tm->ny4 & 1) != 0 ? 1 : 0;
+        }
+        const int grid = launch_pauli_pass<T>(sv.stream(), sv.data(), pp, partials);
+        launch_finalize_pass(sv.stream(), partials, grid, outs + pi * kPassTerms);
+    }
+    std::vector<double> h(passes.size() * kPassTerms);
+    cuda_check(cudaMemcpyAsync(h.data(), outs, h.size() * sizeof(double), cudaMemcpyDeviceToHost, sv.stream()),
+               "D2H");
+    sv.synchronize();
+    double total = 0.0;
+    for (size_t pi = 0; pi < passes.size(); pi++) {
+        for (size_t i = passes[pi].first; i < passes[pi].second; i++) {
+            total += words[i].coef * h[pi * kPassTerms + (i - passes[pi].first)];
+        }
+    }
+    return total;
+}
+
 template <class T> double Measure<T>::expval_obs(StateVector<T> &sv, const ObsNode &obs) {
     // MeasurementsLQubit.hpp:372-394
     PauliSum ps;
     if (compile_pauli(obs, sv.num_qubits(), ps)) {
-        double total = 0.0;
-        for (const auto &g : group_pauli(ps)) {
-            reduce_pauli_group<T>(sv.stream(), sv.data(), sv.length(), g, sv.scratch_red(),
-                                  sv.scratch_red() + 2 * kReduceBlocks);
-            cuda_check(cudaMemcpyAsync(sv.host_out(), sv.scratch_red() + 2 * kReduceBlocks, sizeof(double),
-                                       cudaMemcpyDeviceToHost, sv.stream()), "D2H");
-            sv.synchronize();
-            total += sv.host_out()[0];
-        }
-        return total;
+        return pauli_expval_passes(sv, ps);
     }
     if (obs.kind == ObsNode::Named && obs.wires.size() == 1 &&
         (obs.name == "Hadamard" || obs.name == "Identity")) {

@@ -103,6 +103,37 @@ template <class T>
 void launch_csr_apply(cudaStream_t s, const cx<T> *sv, cx<T> *out, u64 N, const long long *indptr,
                       const long long *indices, const cx<T> *vals);
 
+// Pauli-sum expectation values by passes (kernels_measure.cu): a pass
+// holds up to kPassTerms Pauli words whose flip bits all fit one tile of
+// 2^t amplitudes; the tile's local bits are those flip bits and the lowest
+// other bits.  One read of the state evaluates every word of the pass: per
+// word the kernel sums, over the amplitude pairs (j, j ^ x) of the tile
+// (j without x's top bit), (-1)^{|j & yz|} times Re or Im of
+// conj(psi_j) psi_{j^x} (the part the word's Y count selects), or for x = 0
+// (-1)^{|j & yz|} |psi_j|^2; the host applies each word's coefficient.
+constexpr int kPassTerms = 16;
+constexpr int kPassMaxTileBits = 12;
+struct PauliPassTerm {
+    u64 yz;          // Y|Z mask over the full index
+    unsigned x;      // flip mask over the local index (0: diagonal word)
+    unsigned yzl;    // Y|Z mask over the local index
+    int hb;          // highest set bit of x (local)
+    int im;          // 1: sum Im conj(psi_j) psi_{j^x}; 0: Re
+};
+struct PauliPass {
+    int t;                  // local bits per tile
+    int lbit[kPassMaxTileBits];
+    int nglob;
+    int glob[64];
+    u64 ntiles;
+    int nterms;             // <= kPassTerms
+    PauliPassTerm term[kPassTerms];
+};
+// per-block partial sums of the pass's words into partials[block * kPassTerms + w];
+// returns the grid size (the number of blocks to finalize)
+template <class T> int launch_pauli_pass(cudaStream_t s, const cx<T> *sv, const PauliPass &p, double *partials);
+void launch_finalize_pass(cudaStream_t s, const double *partials, int nblocks, double *out);
+
 // All flip-mask groups of a Pauli sum in one sweep (kernels_measure.cu):
 // out[j] (+)= sum_g sum_{t in g} c_t i^ny_t (-1)^{|k & yz_t|} psi[k], k = j ^ x_g,
 // in double-float arithmetic (coefficients split on the host).

@@ -248,6 +248,111 @@ void reduce_pauli_group(cudaStream_t s, const cx<T> *sv, u64 N, const PauliGroup
     finalize<1>(s, partials, grid, out);
 }
 
+// Pauli words by passes (kernels.hpp, PauliPass): the tile is staged in
+// shared memory as double-float pairs (each amplitude converted once), then
+// every word of the pass is evaluated from it.  Products and sums in
+// double-float arithmetic on the FP32 pipe.
+constexpr int kPassThreads = 256;
+template <class T>
+__global__ void __launch_bounds__(kPassThreads) k_pauli_pass(const cx<T> *__restrict__ a, const __grid_constant__ PauliPass d,
+                                                             double *partials) {
+    extern __shared__ float4 tl[]; // local amplitude jj: (re.hi, re.lo, im.hi, im.lo)
+    const unsigned tid = threadIdx.x;
+    const unsigned T_ = 1u << d.t;
+    // global offset of local index jj = r * 256 + tid: a thread part and a
+    // part per r (local bits 0-7 from tid, the rest from r)
+    u64 off_t = 0;
+    for (int q = 0; q < 8 && q < d.t; q++) {
+        off_t |= static_cast<u64>((tid >> q) & 1u) << d.lbit[q];
+    }
+    df acc[kPassTerms];
+#pragma unroll
+    for (int w = 0; w < kPassTerms; w++) {
+        acc[w] = df{0.f, 0.f};
+    }
+    for (u64 tile = blockIdx.x; tile < d.ntiles; tile += gridDim.x) {
+        u64 base = 0;
+        {
+            u64 tt = tile;
+            for (int q = 0; q < d.nglob; q++) {
+                base |= (tt & 1u) << d.glob[q];
+                tt >>= 1;
+            }
+        }
+        for (unsigned r = 0; r * kPassThreads < T_; r++) {
+            const unsigned jj = r * kPassThreads + tid;
+            if (jj >= T_) {
+                break;
+            }
+            u64 off = base | off_t;
+            for (int q = 8; q < d.t; q++) {
+                off |= static_cast<u64>((r >> (q - 8)) & 1u) << d.lbit[q];
+            }
+            const cx<T> v = a[off];
+            const df re = to_df<T>(v.x), im = to_df<T>(v.y);
+            tl[jj] = make_float4(re.hi, re.lo, im.hi, im.lo);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int w = 0; w < kPassTerms; w++) {
+            if (w >= d.nterms) {
+                break;
+            }
+            const PauliPassTerm &pt = d.term[w];
+            const unsigned tpar = static_cast<unsigned>(__popcll(base & pt.yz)) & 1u;
+            if (pt.x == 0) {
+                for (unsigned j = tid; j < T_; j += kPassThreads) {
+                    const float4 p = tl[j];
+                    const df pr{p.x, p.y}, pi{p.z, p.w};
+                    const df v = df_fma(pr * pr, pi, pi);
+                    const bool neg = ((static_cast<unsigned>(__popc(j & pt.yzl)) ^ tpar) & 1u) != 0;
+                    acc[w] = neg ? acc[w] - v : acc[w] + v;
+                }
+            } else {
+                const unsigned lo = (1u << pt.hb) - 1u;
+                for (unsigned k = tid; k < (T_ >> 1); k += kPassThreads) {
+                    const unsigned j = ((k >> pt.hb) << (pt.hb + 1)) | (k & lo);
+                    const float4 p = tl[j], q = tl[j ^ pt.x];
+                    const df pr{p.x, p.y}, pi{p.z, p.w}, qr{q.x, q.y}, qi{q.z, q.w};
+                    // conj(p) q = (pr qr + pi qi) + i (pr qi - pi qr)
+                    const df v = pt.im ? df_fma(pr * qi, -pi, qr) : df_fma(pr * qr, pi, qi);
+                    const bool neg = ((static_cast<unsigned>(__popc(j & pt.yzl)) ^ tpar) & 1u) != 0;
+                    acc[w] = neg ? acc[w] - v : acc[w] + v;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    double v[kPassTerms];
+#pragma unroll
+    for (int w = 0; w < kPassTerms; w++) {
+        v[w] = df_to_double(acc[w]);
+    }
+    block_reduce_store<kPassTerms>(v, partials);
+}
+template <class T> int launch_pauli_pass(cudaStream_t s, const cx<T> *sv, const PauliPass &p, double *partials) {
+    const size_t smem = sizeof(float4) << p.t;
+    static bool attr = false;
+    if (!attr) {
+        cuda_check(cudaFuncSetAttribute(k_pauli_pass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        static_cast<int>(sizeof(float4) << kPassMaxTileBits)),
+                   "k_pauli_pass smem attribute");
+        attr = true;
+    }
+    int per_sm = 0;
+    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pauli_pass<T>, kPassThreads, smem),
+               "k_pauli_pass occupancy");
+    const u64 cap = static_cast<u64>(LaunchGeom::sm_count()) * static_cast<u64>(per_sm < 1 ? 1 : per_sm);
+    const int grid = static_cast<int>(p.ntiles < cap ? p.ntiles : cap);
+    k_pauli_pass<T><<<grid, kPassThreads, smem, s>>>(sv, p, partials);
+    cuda_check(cudaGetLastError(), "k_pauli_pass launch");
+    note_launch();
+    return grid;
+}
+void launch_finalize_pass(cudaStream_t s, const double *partials, int nblocks, double *out) {
+    finalize<kPassTerms>(s, partials, nblocks, out);
+}
+
 // <a| Pi P |b> where Pi projects on (j & pmask) == pval (row index j):
 // sum_j conj(a_j) i^ny (-1)^{|(j^x) & yz|} b_{j^x}.
 template <class T>
@@ -514,7 +619,8 @@ template <class T> void launch_probs_marginal_serial(cudaStream_t s, const cx<T>
     template void launch_pauli_apply<T>(cudaStream_t, const cx<T> *, cx<T> *, u64, const PauliGroupHdr *, int,    \
                                         const PauliTermDF *, int, bool);                                          \
     template void launch_probs_all<T>(cudaStream_t, const cx<T> *, u64, T *);                                    \
-    template void launch_probs_marginal_serial<T>(cudaStream_t, const cx<T> *, const MarginalGeom &, T *);
+    template void launch_probs_marginal_serial<T>(cudaStream_t, const cx<T> *, const MarginalGeom &, T *);     \
+    template int launch_pauli_pass<T>(cudaStream_t, const cx<T> *, const PauliPass &, double *);
 
 PLGB_INST_MEAS(float)
 PLGB_INST_MEAS(double)

@@ -50,9 +50,16 @@ namespace plgb {
 
 namespace {
 
-constexpr int kTcThreads = 256;
+// 256 threads (8 warps).  The index maps below also hold for 512 threads
+// (kTcThreadBits = 9), which measured slower on a GB300 (0.61 against
+// 0.54 ms for a 2^26-amplitude gate): the phases of a tile are separated by
+// barriers, and more warps per phase do not shorten the chain.
+constexpr int kTcThreadBits = 8;
+constexpr int kTcThreads = 1 << kTcThreadBits;
+constexpr int kTcWarps = kTcThreads / 32;
+constexpr int kTcCols = 64 / (kTcWarps / 4);     // accumulator columns a warp reads back
 constexpr int kTcTileBits = 12;                  // 4096 amplitudes per tile
-constexpr int kTcPerThread = (1 << kTcTileBits) / kTcThreads; // 16
+constexpr int kTcPerThread = (1 << kTcTileBits) / kTcThreads; // amplitudes per thread and tile
 constexpr unsigned kTcASplitBytes = 128u * 128u * 2u;         // one BF16 split of A: 32 KiB
 constexpr unsigned kTcBSplitBytes = 64u * 128u * 2u;          // one split of B: 16 KiB
 constexpr unsigned kTcRawBytes = 4096u * 8u;                 // one tile of complex64: 32 KiB
@@ -122,8 +129,24 @@ __device__ __forceinline__ void tc_commit(unsigned bar) {
                  : "memory");
 }
 
+// 16 consecutive FP32 columns of this thread's tensor-memory lane
+[[maybe_unused]] __device__ __forceinline__ void tc_ld(unsigned taddr, float (&v)[16]) {
+    unsigned r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                 "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                   "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int c = 0; c < 16; c++) {
+        v[c] = __uint_as_float(r[c]);
+    }
+}
 // 32 consecutive FP32 columns of this thread's tensor-memory lane
-__device__ __forceinline__ void tc_ld32(unsigned taddr, float (&v)[32]) {
+__device__ __forceinline__ void tc_ld(unsigned taddr, float (&v)[32]) {
     unsigned r[32];
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
                  "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
@@ -227,11 +250,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         return x;
     };
-    // store phase: local index jj = r * 256 + tid, read from the swizzled
-    // stage, written to global memory (consecutive threads, consecutive
-    // addresses)
+    // store phase: local index jj = r * kTcThreads + tid, read from the
+    // swizzled stage, written to global memory (consecutive threads,
+    // consecutive addresses)
     u64 off_t = 0;
-    for (int q = 0; q < 8; q++) {
+    for (int q = 0; q < kTcThreadBits; q++) {
         off_t |= static_cast<u64>((tid >> q) & 1u) << geom.lbit[q];
     }
     const unsigned st_t = swz(tid, geom.hst);
@@ -239,24 +262,28 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     u64 off_r[kTcPerThread];
 #pragma unroll
     for (int r = 0; r < kTcPerThread; r++) {
-        st_r[r] = swz(static_cast<unsigned>(r) << 8, geom.hst);
+        st_r[r] = swz(static_cast<unsigned>(r) << kTcThreadBits, geom.hst);
         u64 o = 0;
-        for (int q = 0; q < 4; q++) {
-            o |= static_cast<u64>((r >> q) & 1) << geom.lbit[8 + q];
+        for (int q = 0; q < kTcTileBits - kTcThreadBits; q++) {
+            o |= static_cast<u64>((r >> q) & 1) << geom.lbit[kTcThreadBits + q];
         }
         off_r[r] = o;
     }
-    // split phase: this thread handles member u = (lane & 3) | (r << 2) of
-    // group g = (lane >> 2) | (warp << 3), so a warp's B stores are 32
-    // consecutive words; the raw tile is read at its swizzled position
-    const unsigned g_me = (lane >> 2) | (warp << 3);
-    const unsigned raw_t = swz(geom.jj_of_u[lane & 3u] | geom.jj_of_g[g_me], geom.hraw);
+    // split phase: this thread handles group g = (lane >> 2) | ((warp & 7)
+    // << 3) and member u = (lane & 3) | (uh << 2), uh = (warp >> 3) | (r <<
+    // (threads bits - 8)), so a warp's B stores are 32 consecutive words;
+    // the raw tile is read at its swizzled position
+    constexpr int kUs = kTcThreadBits - 8; // member bits from the warp index
+    const unsigned g_me = (lane >> 2) | ((warp & 7u) << 3);
+    const unsigned raw_t =
+        swz(geom.jj_of_u[(lane & 3u) | ((warp >> 3) << 2)] | geom.jj_of_g[g_me], geom.hraw);
     unsigned raw_r[kTcPerThread];
 #pragma unroll
     for (int r = 0; r < kTcPerThread; r++) {
-        raw_r[r] = swz(geom.jj_of_u[static_cast<unsigned>(r) << 2], geom.hraw);
+        raw_r[r] = swz(geom.jj_of_u[static_cast<unsigned>(r) << (2 + kUs)], geom.hraw);
     }
-    const unsigned b_t = (warp * 16u) * 128u + lane * 4u; // kmajor_off(g, 2u) for r = 0
+    // kmajor_off(g, 2u) for r = 0
+    const unsigned b_t = ((warp & 7u) * 16u + (warp >> 3)) * 128u + lane * 4u;
     // global offsets and swizzled raw positions of this thread's copy
     // chunks: local index 2c with c = r * 256 + tid
     u64 coff[kTcChunksPerThread];
@@ -275,7 +302,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // u = m / 2, component m % 2
     const unsigned row = 32u * (warp & 3u) + lane;
     const unsigned st_u = geom.st_of_u[row >> 1];
-    const unsigned col0 = 32u * (warp >> 2);
+    const unsigned col0 = static_cast<unsigned>(kTcCols) * (warp >> 2);
 
     const unsigned a0 = smem_u32(A0), b0 = smem_u32(B0), r0 = smem_u32(R0);
     const unsigned bar = smem_u32(mbar);
@@ -301,7 +328,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
         for (int r = 0; r < kTcPerThread; r++) {
             const float2 v = raw[raw_t ^ raw_r[r]];
-            const unsigned o = b_t + static_cast<unsigned>(r) * 128u; // (re, im) adjacent: k = 2u, 2u + 1
+            const unsigned o = b_t + (static_cast<unsigned>(r) << kUs) * 128u; // (re, im) adjacent: k = 2u, 2u + 1
             unsigned short xh, xm, xl, yh, ym, yl;
             split3(v.x, xh, xm, xl);
             split3(v.y, yh, ym, yl);
@@ -356,16 +383,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         phase ^= 1u;
         tc_fence_after();
-        // D row m = 32 (warp % 4) + lane; warps 0-3 read columns 0-31, warps
-        // 4-7 columns 32-63.  The MMAs have consumed B, so the stage (over
+        // D row m = 32 (warp % 4) + lane; warp w reads kTcCols columns from
+        // kTcCols * (w / 4).  The MMAs have consumed B, so the stage (over
         // the B splits) may be written.
         {
-            float d[32];
-            tc_ld32(tmem + ((32u * (warp & 3u)) << 16) + col0, d);
+            float d[kTcCols];
+            tc_ld(tmem + ((32u * (warp & 3u)) << 16) + col0, d);
             float *st = reinterpret_cast<float *>(stage);
             const unsigned comp = row & 1u;
 #pragma unroll
-            for (int c = 0; c < 32; c++) {
+            for (int c = 0; c < kTcCols; c++) {
                 st[2u * (st_u ^ geom.st_of_g[col0 + static_cast<unsigned>(c)]) + comp] = d[c];
             }
         }

@@ -499,9 +499,29 @@ def batched_leg(ops, prec: int, plain_every: int = 32) -> dict:
     eng = BatchEngine(prec)
     eng.run(packed)  # warm-up: tile-size autotuning, device arenas and pinned staging at full size
     t = time.perf_counter()
-    eng.run(packed)
+    vals = eng.run(packed)
     dt = time.perf_counter() - t
     st = eng.stats()
+    df_leg = None
+    if prec == 128:
+        # the opt-in double-float passes on the same batch: throughput and the
+        # largest deviation of its expectation values from the FP64 run's,
+        # relative to each observable's sum |c| (the bound of |<O>|)
+        prev = ops.set_c128_fp64_passes(False)
+        try:
+            eng_df = BatchEngine(prec)
+            eng_df.run(packed)
+            t = time.perf_counter()
+            vals_df = eng_df.run(packed)
+            dt_df = time.perf_counter() - t
+        finally:
+            ops.set_c128_fp64_passes(prev)
+        to = np.asarray(packed.term_offsets, np.int64)
+        norm = np.add.reduceat(np.abs(np.asarray(packed.term_coeffs, np.float64)), to[:-1])
+        dev = np.abs(np.asarray(vals_df) - np.asarray(vals)) / norm
+        df_leg = {"value": packed.num_circuits / dt_df, "unit": "circuits/s", "seconds": dt_df,
+                  "arithmetic": "double-float passes (opt-in, set_c128_fp64_passes(False))",
+                  "max_dev_vs_fp64_rel_sum_abs_c": float(dev.max()), "observables": int(dev.size)}
     lat = np.asarray(st["wave_done_ms"])[np.asarray(st["wave_of"], int)]
     sample = list(range(0, packed.num_circuits, plain_every))
     # warm-up of both per-call paths on the widest sampled circuit (first
@@ -521,6 +541,10 @@ def batched_leg(ops, prec: int, plain_every: int = 32) -> dict:
     for r in sample:
         _plain_circuit(ops, packed, r, names, prec, lazy=True)
     plain_lazy = len(sample) / (time.perf_counter() - t)
+    extra = {}
+    if df_leg is not None:
+        df_leg["speedup_vs_plain"] = df_leg["value"] / plain
+        extra["double_float"] = df_leg
     return {"metric": "config2 circuits/s", "value": packed.num_circuits / dt, "unit": "circuits/s",
             "circuits": packed.num_circuits, "seconds": dt, "p50_ms": float(np.percentile(lat, 50)),
             "p99_ms": float(np.percentile(lat, 99)), "compile_ms": st["compile_ms"], "device_ms": st["device_ms"],
@@ -531,7 +555,7 @@ def batched_leg(ops, prec: int, plain_every: int = 32) -> dict:
             "plain_lazy_fusion": {"value": plain_lazy, "unit": "circuits/s",
                                   "note": "the same per-gate calls, queued and fused by the binding"},
             "speedup_vs_plain": packed.num_circuits / dt / plain,
-            "speedup_vs_plain_lazy_fusion": packed.num_circuits / dt / plain_lazy}
+            "speedup_vs_plain_lazy_fusion": packed.num_circuits / dt / plain_lazy, **extra}
 
 
 def adjoint_leg(n: int = 28, layers: int = 12, fd: int = 0) -> dict:
@@ -585,6 +609,17 @@ def serve_leg(seconds: float) -> dict:
     res = srv.run(packed, arrival, adjoint)
     out = {"metric": "config4 requests/s", **res.summary(), "window_s": seconds,
            "offered_per_s": packed.num_circuits / seconds}
+    # the same stream with admission control: requests whose predicted wait
+    # exceeds 1 s are refused at arrival
+    slo = 1.0
+    srv_adm = Server(128, slo_s=slo)
+    srv_adm.run(packed.select(w), arrival[w] - arrival[0], adjoint[w])  # warm-up
+    ra = srv_adm.run(packed, arrival, adjoint).summary()
+    out["admission_control"] = {"slo_s": slo, "offered_per_s": packed.num_circuits / seconds,
+                                "admitted": ra["requests"], "refused": ra["refused"],
+                                "admitted_fraction": ra["requests"] / max(1, ra["offered"]),
+                                "goodput_per_s": ra["throughput_per_s"], "p50_ms": ra["p50_ms"],
+                                "p99_ms": ra["p99_ms"], "lanes": ra["lanes"]}
     # the same stream shape offered below capacity: latency without a backlog
     cap = out["throughput_per_s"]
     if cap > 0:

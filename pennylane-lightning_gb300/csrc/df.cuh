@@ -13,9 +13,10 @@
 // passes of one program; only its first pass reads doubles and only its last
 // pass writes them.
 //
-// Range: |value| < 2^127.  Values below 2^-126 in magnitude become 0, and
+// Range: |value| < 2^128.  Values below 2^-126 in magnitude become 0, and
 // the low part is dropped below 2^-74 (absolute errors far below the
-// tolerance of normalised states).
+// tolerance of normalised states); larger magnitudes and infinities become
+// +-infinity, and NaN stays NaN.
 #pragma once
 
 #include "plgb_common.cuh"
@@ -90,6 +91,10 @@ __device__ __forceinline__ df df_from_bits(double x) {
     const int e = static_cast<int>((hw >> 20) & 0x7ffu);
     if (e < 897) { // below the float normal range (or zero)
         return df{0.f, 0.f};
+    }
+    if (e > 1150) { // |x| >= 2^128 (beyond the float range), infinity or NaN
+        const bool nan = e == 2047 && ((hw & 0xfffffu) | lw) != 0u;
+        return df{__int_as_float(static_cast<int>(nan ? 0x7fc00000u : (sign | 0x7f800000u))), 0.f};
     }
     // hi: the top 24 significant bits, truncated
     const unsigned m23 = ((hw & 0xfffffu) << 3) | (lw >> 29);

@@ -241,119 +241,112 @@ struct PassPlan {
     u64 local{0};
 };
 
-// Order the primitives of one pass as dependency layers (see the comment
-// inside); returns them in execution order with, per position, its level.
+// Order the primitives of one pass for execution; per position, levels_out
+// gets the merge group of a diagonal (diagonals of one group run as one
+// merged op) and the dependency depth of any other primitive.
+//
+// Dependencies, in program order: two non-diagonal primitives that share a
+// touched bit; a diagonal and a non-diagonal primitive that changes one of
+// its bits (tmask: touched minus control bits; a diagonal commutes with an op
+// that only uses its bits as controls).  Diagonals commute with each other.
+// The order is a list schedule that postpones diagonals: every ready
+// non-diagonal primitive is emitted first (lowest dependency depth, then
+// program order); only when none is left are all ready diagonals emitted as
+// one group.  A diagonal thus waits until a primitive needs it, and every
+// diagonal ready by then joins it: in a layer of one-wire rotations followed
+// by a CNOT chain, the diagonal halves of the rotations merge into one group
+// before the chain and one after it, where depth levels would stagger them
+// along the chain.
 std::vector<size_t> order_by_levels(const std::vector<size_t> &prims, const std::vector<u64> &touch,
                                     const std::vector<u64> &tmask, const std::vector<char> &diag,
                                     std::vector<int> *levels_out) {
-    // Order the pass as dependency layers.  Non-diagonal ops go to the
-    // first level after everything they depend on.  A diagonal may sit at
-    // any level from its last non-diagonal predecessor up to just before
-    // the next non-diagonal op on its bits; diagonals on two or more
-    // bits also hold later non-diagonal ops on their bits behind them,
-    // which keeps every such range non-empty.  Only the bits an op acts on
-    // (tmask: touched minus control bits) order it against diagonals: a
-    // diagonal commutes with an op that only uses its bits as controls.
-    // The diagonals are then
-    // packed onto as few levels as possible (interval point cover,
-    // greedy by right end); all diagonals of one level merge into one
-    // op placed after that level's non-diagonal ops.
     const size_t np = prims.size();
-    std::vector<int> level(np, 0), dlo(np, 0), dhi(np, 0);
-    int maxlv = 0;
+    // dependency depth of the non-diagonal primitives (emission priority)
+    std::vector<int> depth(np, 0);
     {
-        int ndl[64] = {0}, ndl_t[64] = {0}, floor_lv[64] = {0};
+        int ndl[64] = {0};
         for (size_t k = 0; k < np; k++) {
             const size_t pi = prims[k];
-            const u64 tb = touch[pi];
+            if (diag[pi]) {
+                continue;
+            }
             int lv = 0;
-            if (diag[pi]) {
-                for (u64 r = tb; r; r &= r - 1) {
-                    lv = std::max(lv, ndl_t[__builtin_ctzll(r)]);
-                }
-                dlo[k] = lv;
-                if (__builtin_popcountll(tb) >= 2) {
-                    for (u64 r = tb; r; r &= r - 1) {
-                        const int b = __builtin_ctzll(r);
-                        floor_lv[b] = std::max(floor_lv[b], lv);
-                    }
-                }
-            } else {
-                for (u64 r = tb; r; r &= r - 1) {
-                    lv = std::max(lv, ndl[__builtin_ctzll(r)]);
-                }
-                for (u64 r = tmask[pi]; r; r &= r - 1) {
-                    lv = std::max(lv, floor_lv[__builtin_ctzll(r)]);
-                }
-                lv += 1;
-                for (u64 r = tb; r; r &= r - 1) {
-                    ndl[__builtin_ctzll(r)] = lv;
-                }
-                for (u64 r = tmask[pi]; r; r &= r - 1) {
-                    ndl_t[__builtin_ctzll(r)] = lv;
-                }
-                level[k] = lv;
-                maxlv = std::max(maxlv, lv);
+            for (u64 r = touch[pi]; r; r &= r - 1) {
+                lv = std::max(lv, ndl[__builtin_ctzll(r)]);
             }
-        }
-        int next_lv[64];
-        std::fill(next_lv, next_lv + 64, maxlv + 1);
-        for (size_t k = np; k-- > 0;) {
-            const size_t pi = prims[k];
-            const u64 tb = touch[pi];
-            if (diag[pi]) {
-                int h = maxlv;
-                for (u64 r = tb; r; r &= r - 1) {
-                    h = std::min(h, next_lv[__builtin_ctzll(r)] - 1);
-                }
-                dhi[k] = h;
-            } else {
-                for (u64 r = tmask[pi]; r; r &= r - 1) {
-                    next_lv[__builtin_ctzll(r)] = level[k];
-                }
+            lv += 1;
+            for (u64 r = touch[pi]; r; r &= r - 1) {
+                ndl[__builtin_ctzll(r)] = lv;
             }
-        }
-        std::vector<size_t> dk;
-        for (size_t k = 0; k < np; k++) {
-            if (diag[prims[k]]) {
-                dk.push_back(k);
-            }
-        }
-        std::stable_sort(dk.begin(), dk.end(), [&](size_t a, size_t b) { return dhi[a] < dhi[b]; });
-        int point = -1;
-        for (size_t k : dk) {
-            if (point < dlo[k]) {
-                point = dhi[k];
-            }
-            level[k] = point;
+            depth[k] = lv;
         }
     }
-    // bucket by (level, non-diagonal first), keeping program order inside
+    auto depends = [&](size_t a, size_t b) { // a before b in program order
+        const size_t pa = prims[a], pb = prims[b];
+        if (diag[pa] && diag[pb]) {
+            return false;
+        }
+        if (diag[pa]) {
+            return (touch[pa] & tmask[pb]) != 0;
+        }
+        if (diag[pb]) {
+            return (tmask[pa] & touch[pb]) != 0;
+        }
+        return (touch[pa] & touch[pb]) != 0;
+    };
+    std::vector<int> npred(np, 0);
+    std::vector<std::vector<size_t>> succ(np);
+    for (size_t b = 0; b < np; b++) {
+        for (size_t a = 0; a < b; a++) {
+            if (depends(a, b)) {
+                npred[b]++;
+                succ[a].push_back(b);
+            }
+        }
+    }
     std::vector<size_t> ordered;
     ordered.reserve(np);
-    {
-        std::vector<size_t> cnt(2 * static_cast<size_t>(maxlv + 1) + 1, 0);
-        auto key = [&](size_t k) { return 2 * static_cast<size_t>(level[k]) + (diag[prims[k]] ? 1 : 0); };
+    std::vector<int> lv_of(np, 0);
+    std::vector<char> emitted(np, 0);
+    auto emit = [&](size_t k, int lv) {
+        emitted[k] = 1;
+        ordered.push_back(prims[k]);
+        lv_of[ordered.size() - 1] = lv;
+        for (size_t q : succ[k]) {
+            npred[q]--;
+        }
+    };
+    int group = 0;
+    while (ordered.size() < np) {
+        // the ready non-diagonal primitive of lowest depth, else a group of
+        // every ready diagonal
+        size_t best = np;
         for (size_t k = 0; k < np; k++) {
-            cnt[key(k) + 1]++;
+            if (!emitted[k] && npred[k] == 0 && !diag[prims[k]] && (best == np || depth[k] < depth[best])) {
+                best = k;
+            }
         }
-        for (size_t q = 1; q < cnt.size(); q++) {
-            cnt[q] += cnt[q - 1];
+        if (best != np) {
+            emit(best, depth[best]);
+            continue;
         }
-        ordered.resize(np);
+        std::vector<size_t> ready;
         for (size_t k = 0; k < np; k++) {
-            ordered[cnt[key(k)]++] = prims[k];
+            if (!emitted[k] && npred[k] == 0) {
+                ready.push_back(k); // diagonals only: no non-diagonal one is ready
+            }
         }
+        if (ready.empty()) {
+            // not reachable: program order is a topological order
+            throw PLError("fusion plan: cyclic dependencies in a pass");
+        }
+        for (size_t k : ready) {
+            emit(k, group);
+        }
+        group++;
     }
     if (levels_out) {
-        levels_out->clear();
-        std::vector<int> lv_of(touch.size(), 0);
-        for (size_t k = 0; k < np; k++) {
-            lv_of[prims[k]] = level[k];
-        }
-        for (size_t pi : ordered) {
-            levels_out->push_back(lv_of[pi]);
-        }
+        levels_out->assign(lv_of.begin(), lv_of.end());
     }
     return ordered;
 }

@@ -18,6 +18,14 @@ queues independently, so work of different lanes overlaps on the device:
   streams and buffer pool (fused forward pass, <H>, in-place adjoint
   sweep).
 
+Admission control (`slo_s`): a request is refused at arrival when the
+work queued ahead of it on its lane, at the lane's measured rate, would take
+longer than `slo_s` (the lane's rate is learned from its completed batches:
+cost units, gates x 2^n, x 4 for an adjoint, per second).  Under a load
+beyond the device's capacity the admitted requests then keep a bounded
+latency instead of all waiting on an ever longer queue; the refused ones
+are reported.  Without `slo_s` every request is admitted.
+
 Results of a request do not depend on what else is in flight: a forward
 request's value is bit-identical to running it alone in a batch engine with
 the same tile size, and an adjoint request runs exactly as it would alone.
@@ -60,6 +68,37 @@ class MemoryBudget:
             self.cv.notify_all()
 
 
+class Admission:
+    """Admission control by predicted wait.  Per lane kind: the cost queued
+    or in flight, and the kind's completion rate (cost units per second over
+    all its `parallel` lanes, an average of the completed batches weighted
+    0.2 towards the newest).  A request is refused when the cost ahead of it
+    plus its own, at that rate, exceeds `slo_s`; before a kind's first batch
+    completes there is no rate yet and every request is admitted."""
+
+    def __init__(self, slo_s: float | None, parallel):
+        self.slo_s = None if slo_s is None else float(slo_s)
+        self.parallel = [float(x) for x in parallel]
+        self.backlog = [0.0] * len(self.parallel)
+        self.rate = [None] * len(self.parallel)
+        self.lock = threading.Lock()
+
+    def offer(self, kind: int, cost: float) -> bool:
+        with self.lock:
+            r = self.rate[kind]
+            if self.slo_s is not None and r is not None and (self.backlog[kind] + cost) / r > self.slo_s:
+                return False
+            self.backlog[kind] += cost
+            return True
+
+    def completed(self, kind: int, cost: float, seconds: float) -> None:
+        with self.lock:
+            self.backlog[kind] -= cost
+            thr = cost / max(seconds, 1e-4) * self.parallel[kind]
+            r = self.rate[kind]
+            self.rate[kind] = thr if r is None else 0.8 * r + 0.2 * thr
+
+
 @dataclass
 class ServeResult:
     values: np.ndarray   # <H> per request
@@ -69,25 +108,41 @@ class ServeResult:
     done: np.ndarray     # seconds from the start when its result was ready
     lane: np.ndarray     # lane index that served it
     batches: list = field(default_factory=list)  # (lane, size, seconds) per batch
+    refused: np.ndarray = None  # requests refused by admission control
 
     @property
     def latency(self) -> np.ndarray:
-        return self.done - self.arrival
+        """Arrival to result, admitted requests only."""
+        ok = self.admitted
+        return self.done[ok] - self.arrival[ok]
+
+    @property
+    def admitted(self) -> np.ndarray:
+        return ~self.refused if self.refused is not None else np.ones(self.done.size, bool)
 
     def summary(self) -> dict:
         lat = self.latency
-        span = float(self.done.max() - self.arrival.min()) if lat.size else 0.0
-        return {"requests": int(lat.size), "throughput_per_s": lat.size / span if span > 0 else 0.0,
+        ok = self.admitted
+        span = float(self.done[ok].max() - self.arrival.min()) if lat.size else 0.0
+        busy = {}
+        for li, size, sec in self.batches:
+            k = "forward" if li < 2 else "adjoint"
+            b = busy.setdefault(k, {"batches": 0, "requests": 0, "lane_seconds": 0.0})
+            b["batches"] += 1
+            b["requests"] += int(size)
+            b["lane_seconds"] += float(sec)
+        return {"requests": int(lat.size), "offered": int(self.done.size), "refused": int((~ok).sum()),
+                "throughput_per_s": lat.size / span if span > 0 else 0.0,
                 "p50_ms": float(np.percentile(lat, 50) * 1e3) if lat.size else None,
                 "p99_ms": float(np.percentile(lat, 99) * 1e3) if lat.size else None,
                 "mean_batch": float(np.mean([b[1] for b in self.batches])) if self.batches else 0.0,
-                "batches": len(self.batches), "span_s": span}
+                "batches": len(self.batches), "span_s": span, "lanes": busy}
 
 
 class Server:
     def __init__(self, precision: int = 128, budget_bytes: float = 150e9, big_qubits: int = 20,
                  adjoint_lanes: int = 8, max_batch: int = 4096, tile_bits: int = 11, adjoint_share: float = 0.4,
-                 adjoint_take: int = 1):
+                 adjoint_take: int = 1, slo_s: float | None = None):
         self.precision = int(precision)
         self.S = 16 if self.precision == 128 else 8
         # forward and adjoint lanes draw on separate shares of the budget, so
@@ -99,6 +154,7 @@ class Server:
         self.tile_bits = int(tile_bits)
         self.adjoint_lanes = int(adjoint_lanes)
         self.adjoint_take = int(adjoint_take)
+        self.slo_s = None if slo_s is None else float(slo_s)
         # forward lanes keep their engines (device arenas, tuned tile sizes)
         self.engines = [BatchEngine(self.precision, wave_bytes=int(budget_bytes)),
                         BatchEngine(self.precision, wave_bytes=int(budget_bytes))]
@@ -113,6 +169,13 @@ class Server:
     def _bytes(self, r: int) -> int:
         n = max(int(self.packed.num_qubits[r]), 9)
         return (1 << n) * self.S * (3 if self.adjoint[r] else 1)
+
+    def _costs(self) -> np.ndarray:
+        """Cost units per request: gates x 2^n, x 4 for an adjoint request."""
+        p = self.packed
+        ngates = np.diff(np.asarray(p.op_offsets, np.int64)).astype(np.float64)
+        c = ngates * np.exp2(np.asarray(p.num_qubits, np.float64))
+        return c * np.where(self.adjoint, 4.0, 1.0)
 
     def _ops_struct(self, r: int):
         p = self.packed
@@ -158,8 +221,14 @@ class Server:
         start = np.zeros(R)
         done = np.zeros(R)
         lane_of = np.zeros(R, np.int32)
+        refused = np.zeros(R, bool)
         batches: list = []
         lock = threading.Lock()
+        cost = self._costs()
+        adm = Admission(self.slo_s, [1, 1, self.adjoint_lanes])
+
+        def completed(li, got, seconds):
+            adm.completed(li, float(cost[got].sum()), seconds)
         nl = 3  # two forward lanes; one queue shared by the adjoint lanes
         queues = [collections.deque() for _ in range(nl)]
         cvs = [threading.Condition() for _ in range(nl)]
@@ -207,6 +276,7 @@ class Server:
                     fin = eng.done_ms()
                     for r in got:
                         self.budget.release(self._bytes(r))
+                    completed(li, got, te - ts)
                     with lock:
                         for k, r in enumerate(got):
                             values[r] = vals[k]
@@ -230,6 +300,7 @@ class Server:
                     fin = eng.done_ms()
                     for r in got:
                         self.adj_budget.release(self._bytes(r))
+                    completed(2, got, te - ts)
                     with lock:
                         for k, r in enumerate(got):
                             values[r], jacs[r] = vals[k], js[k][0]
@@ -256,13 +327,18 @@ class Server:
                 li = 2
             else:
                 li = 1 if packed.num_qubits[r] >= self.big else 0
+            if not adm.offer(li, float(cost[r])):
+                refused[r] = True
+                with lock:
+                    done[r] = now()
+                continue
             with cvs[li]:
                 queues[li].append(r)
                 cvs[li].notify()
         # drain
         while not errors:
             with lock:
-                finished = int(np.count_nonzero(done > 0))
+                finished = int(np.count_nonzero((done > 0) | refused))
             if finished == R:
                 break
             time.sleep(0.01)
@@ -271,7 +347,7 @@ class Server:
             th.join()
         if errors:
             raise errors[0]
-        return ServeResult(values, jacs, np.asarray(arrival, float) / speed, start, done, lane_of, batches)
+        return ServeResult(values, jacs, np.asarray(arrival, float) / speed, start, done, lane_of, batches, refused)
 
 
 _ONE_PARAM = {"PhaseShift", "RX", "RY", "RZ", "IsingXX", "IsingXY", "IsingYY", "IsingZZ", "ControlledPhaseShift",

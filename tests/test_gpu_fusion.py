@@ -153,6 +153,33 @@ def test_c128_double_float_passes_match_fp64(ops_module):
     assert not np.array_equal(outs[False], outs[True])  # the two arithmetics did run
 
 
+def test_double_float_range(ops_module, oracle):
+    # the double-float passes hold magnitudes below 2^128: a larger amplitude
+    # becomes infinite (and NaN stays NaN) instead of a wrapped exponent; the
+    # amplitudes it does not touch are unaffected
+    n = 12
+    rng = np.random.default_rng(seed_of("df-range"))
+    st = rand_state(rng, n)
+    st[5], st[9] = 1e300 + 0j, complex(np.nan, 0.0)
+    ops = [dict(name="RZ", wires=[0], params=[0.7]), dict(name="RX", wires=[3], params=[0.4]),
+           dict(name="PhaseShift", wires=[1], params=[1.1])]
+    prev = ops_module.set_c128_fp64_passes(False)
+    try:
+        sv = ops_module.StateVectorC128(n)
+        sv.updateData(st)
+        sv.applyOperations(ops_struct(ops_module, np.complex128, ops), 11)
+        out = sv.state()
+    finally:
+        ops_module.set_c128_fp64_passes(prev)
+    hit = [5, 5 ^ 256, 9, 9 ^ 256]  # RX on wire 3 mixes amplitude bit 8
+    assert not np.isfinite(out[hit]).any()
+    rest = np.setdiff1d(np.arange(1 << n), hit)
+    st_ok = st.copy()
+    st_ok[hit] = 0.0
+    ref = oracle_apply(oracle, n, np.complex128, st_ok, ops)
+    assert np.max(np.abs(out[rest] - ref[rest])) <= 1e-10 * np.max(np.abs(ref))
+
+
 @pytest.mark.parametrize("dt", DTYPES)
 @pytest.mark.parametrize("fp64", [False, True])
 def test_wide_local_diagonals_fused(ops_module, oracle, dt, fp64):

@@ -488,7 +488,12 @@ template <class T> double pauli_expval_passes(StateVector<T> &sv, const PauliSum
         const PauliSum::Term *term;
     };
     std::vector<W> words;
+    PauliSum wide; // words with more flip bits than a tile holds: one sweep per flip mask
     for (const auto &tm : ps.terms) {
+        if (__builtin_popcountll(tm.x) > t) {
+            wide.terms.push_back(tm);
+            continue;
+        }
         const int par = __builtin_popcountll(tm.x & tm.yz) & 1;
         const bool odd = (tm.ny4 & 1) != 0;
         if (tm.x != 0 && par != (odd ? 1 : 0)) {
@@ -504,15 +509,66 @@ template <class T> double pauli_expval_passes(StateVector<T> &sv, const PauliSum
             words.push_back({coef, &tm});
         }
     }
-    std::stable_sort(words.begin(), words.end(), [](const W &a, const W &b) { return a.term->x < b.term->x; });
+    // Passes: groups of at most kPassTerms words whose flip bits together
+    // leave the tile at least its 2 lowest other bits (4 consecutive
+    // amplitudes per group of copies, whole 32-byte sectors).  Up to 512 words: each pass starts from
+    // the open word with the most flip bits and adds the words that widen its
+    // flip set least (diagonal words widen nothing); larger sums are grouped
+    // in flip-mask order.
     std::vector<std::pair<size_t, size_t>> passes; // [begin, end) of words
-    {
+    const int lim = std::max(1, t - 2);
+    if (words.size() <= 512) {
+        std::vector<W> ordered;
+        ordered.reserve(words.size());
+        std::vector<char> used(words.size(), 0);
+        size_t left = words.size();
+        while (left > 0) {
+            size_t seed = words.size();
+            for (size_t i = 0; i < words.size(); i++) {
+                if (!used[i] && (seed == words.size() || __builtin_popcountll(words[i].term->x) >
+                                                             __builtin_popcountll(words[seed].term->x))) {
+                    seed = i;
+                }
+            }
+            const size_t b0 = ordered.size();
+            u64 U = words[seed].term->x;
+            const int cap = std::max(lim, __builtin_popcountll(U));
+            used[seed] = 1;
+            ordered.push_back(words[seed]);
+            left--;
+            while (left > 0 && ordered.size() - b0 < static_cast<size_t>(kPassTerms)) {
+                size_t best = words.size();
+                int best_add = 64;
+                for (size_t i = 0; i < words.size(); i++) {
+                    if (used[i]) {
+                        continue;
+                    }
+                    const u64 nu = U | words[i].term->x;
+                    const int add = __builtin_popcountll(nu) - __builtin_popcountll(U);
+                    if (__builtin_popcountll(nu) <= cap && add < best_add) {
+                        best = i;
+                        best_add = add;
+                    }
+                }
+                if (best == words.size()) {
+                    break;
+                }
+                used[best] = 1;
+                U |= words[best].term->x;
+                ordered.push_back(words[best]);
+                left--;
+            }
+            passes.emplace_back(b0, ordered.size());
+        }
+        words.swap(ordered);
+    } else {
+        std::stable_sort(words.begin(), words.end(), [](const W &a, const W &b) { return a.term->x < b.term->x; });
         size_t b = 0;
         u64 U = 0;
         for (size_t i = 0; i < words.size(); i++) {
             const u64 nu = U | words[i].term->x;
-            const int lim = std::max(t - 4, __builtin_popcountll(words[i].term->x));
-            if (i > b && (i - b == static_cast<size_t>(kPassTerms) || __builtin_popcountll(nu) > lim)) {
+            const int cap = std::max(lim, __builtin_popcountll(words[i].term->x));
+            if (i > b && (i - b == static_cast<size_t>(kPassTerms) || __builtin_popcountll(nu) > cap)) {
                 passes.emplace_back(b, i);
                 b = i;
                 U = words[i].term->x;
@@ -524,13 +580,15 @@ template <class T> double pauli_expval_passes(StateVector<T> &sv, const PauliSum
             passes.emplace_back(b, words.size());
         }
     }
-    if (passes.empty()) {
+    const std::vector<PauliGroup> wide_groups = group_pauli(wide);
+    if (passes.empty() && wide_groups.empty()) {
         return 0.0;
     }
     const u64 N = sv.length();
     const size_t max_grid = static_cast<size_t>(LaunchGeom::sm_count()) * 8;
-    const auto bufs = sv.scratch().carve({max_grid * kPassTerms * sizeof(double),
-                                         passes.size() * kPassTerms * sizeof(double)});
+    const size_t nout = passes.size() * kPassTerms + wide_groups.size();
+    const auto bufs = sv.scratch().carve({std::max<size_t>(max_grid * kPassTerms, kReduceBlocks) * sizeof(double),
+                                         nout * sizeof(double)});
     double *partials = reinterpret_cast<double *>(bufs[0]);
     double *outs = reinterpret_cast<double *>(bufs[1]);
     for (size_t pi = 0; pi < passes.size(); pi++) {
@@ -571,11 +629,27 @@ template <class T> double pauli_expval_passes(StateVector<T> &sv, const PauliSum
             pt.yzl = gather(tm->yz);
             pt.hb = pt.x ? 31 - __builtin_clz(pt.x) : 0;
             pt.im = (tm->ny4 & 1) != 0 ? 1 : 0;
+            if (t == kPassMaxTileBits) {
+                const unsigned lo = (1u << pt.hb) - 1u;
+                pt.srm = 0;
+                for (unsigned r = 0; r < (pt.x ? 4u : 8u); r++) {
+                    const unsigned k = r << 9;
+                    const unsigned j = pt.x ? (((k >> pt.hb) << (pt.hb + 1)) | (k & lo)) : k;
+                    if (pt.x) {
+                        pt.jr[r] = static_cast<unsigned short>(j);
+                    }
+                    pt.srm |= (static_cast<unsigned>(__builtin_popcount(j & pt.yzl)) & 1u) << r;
+                }
+            }
         }
         const int grid = launch_pauli_pass<T>(sv.stream(), sv.data(), pp, partials);
         launch_finalize_pass(sv.stream(), partials, grid, outs + pi * kPassTerms);
     }
-    std::vector<double> h(passes.size() * kPassTerms);
+    for (size_t g = 0; g < wide_groups.size(); g++) {
+        reduce_pauli_group<T>(sv.stream(), sv.data(), N, wide_groups[g], partials,
+                              outs + passes.size() * kPassTerms + g);
+    }
+    std::vector<double> h(nout);
     cuda_check(cudaMemcpyAsync(h.data(), outs, h.size() * sizeof(double), cudaMemcpyDeviceToHost, sv.stream()),
                "D2H");
     sv.synchronize();
@@ -584,6 +658,9 @@ template <class T> double pauli_expval_passes(StateVector<T> &sv, const PauliSum
         for (size_t i = passes[pi].first; i < passes[pi].second; i++) {
             total += words[i].coef * h[pi * kPassTerms + (i - passes[pi].first)];
         }
+    }
+    for (size_t g = 0; g < wide_groups.size(); g++) {
+        total += h[passes.size() * kPassTerms + g]; // coefficients applied in the sweep
     }
     return total;
 }

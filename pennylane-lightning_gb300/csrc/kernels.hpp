@@ -119,6 +119,11 @@ struct PauliPassTerm {
     unsigned yzl;    // Y|Z mask over the local index
     int hb;          // highest set bit of x (local)
     int im;          // 1: sum Im conj(psi_j) psi_{j^x}; 0: Re
+    // tiles of 2^12 amplitudes, 512 threads: pair k = r * 512 + tid, r < 4,
+    // has j = jt(tid) | jr[r] (k with a zero inserted at bit hb); srm bit r =
+    // parity of jr[r] & yzl (x = 0: of (r << 9) & yzl, r < 8)
+    unsigned short jr[4];
+    unsigned srm;
 };
 struct PauliPass {
     int t;                  // local bits per tile

@@ -12,10 +12,14 @@
 #include "df.cuh"
 #include "kernels.hpp"
 
+#include <type_traits>
+
 namespace plgb {
 
-template <int NOUT> __device__ __forceinline__ void block_reduce_store(double (&v)[NOUT], double *partials) {
-    __shared__ double sh[NOUT][kReduceThreads / 32];
+template <int NOUT, int THREADS = kReduceThreads>
+__device__ __forceinline__ void block_reduce_store(double (&v)[NOUT], double *partials) {
+    static_assert(THREADS % 32 == 0 && THREADS <= 1024, "whole warps, at most 32");
+    __shared__ double sh[NOUT][THREADS / 32];
 #pragma unroll
     for (int o = 0; o < NOUT; o++) {
         double x = v[o];
@@ -31,7 +35,7 @@ template <int NOUT> __device__ __forceinline__ void block_reduce_store(double (&
     if (threadIdx.x < 32) {
 #pragma unroll
         for (int o = 0; o < NOUT; o++) {
-            double x = threadIdx.x < (kReduceThreads / 32) ? sh[o][threadIdx.x] : 0.0;
+            double x = threadIdx.x < (THREADS / 32) ? sh[o][threadIdx.x] : 0.0;
 #pragma unroll
             for (int d = 16; d > 0; d >>= 1) {
                 x += __shfl_down_sync(0xffffffffu, x, d);
@@ -330,21 +334,237 @@ __global__ void __launch_bounds__(kPassThreads) k_pauli_pass(const cx<T> *__rest
     }
     block_reduce_store<kPassTerms>(v, partials);
 }
+// Tiles of 2^12 amplitudes (registers of 12 or more qubits): the same sums
+// with less index and sign work per pair, and the loads of the next tile in
+// flight while the current one is evaluated.  One 512-thread CTA per SM;
+// tiles arrive by 16-byte (complex64: 8-byte) asynchronous copies into two
+// raw buffers; a complex128 tile is converted in place to double-float
+// pairs (16 bytes either way) by the thread that copied each amplitude.
+// Thread tid takes pairs k = r * 512 + tid (r < 4) of a non-diagonal word;
+// j (k with a zero at the word's top flip bit) is a thread part computed
+// once per word and tile OR the host's part jr[r], and the sign
+// (-1)^{|j & yz|} splits the same way (thread part, tile part from the
+// global bits, srm bit r).  A pair's value keeps the products' rounding
+// errors (TwoProd by FMA, TwoSum); each word's sum is a float pair (A, L):
+// A accumulates by TwoSum, L collects the low parts.  The pairs of the 16
+// words live in shared memory behind the buffers (one float2 per word and
+// thread), read and written once per word and tile.
+struct PassAcc {
+    float a, l;
+};
+// s + c = (ah + al)(bh + bl) + (ch + cl)(dh + dl), without the lo x lo terms
+__device__ __forceinline__ void pass_dot2(float ah, float al, float bh, float bl, float ch, float cl, float dh,
+                                          float dl, float &s, float &c) {
+    const float h1 = __fmul_rn(ah, bh);
+    const float e1 = __fmaf_rn(ah, bh, -h1);
+    const float h2 = __fmul_rn(ch, dh);
+    const float e2 = __fmaf_rn(ch, dh, -h2);
+    s = __fadd_rn(h1, h2);
+    const float bb = __fsub_rn(s, h1);
+    const float es = __fadd_rn(__fsub_rn(h1, __fsub_rn(s, bb)), __fsub_rn(h2, bb));
+    float t = __fmaf_rn(ah, bl, e1);
+    t = __fmaf_rn(al, bh, t);
+    t = __fmaf_rn(ch, dl, t);
+    t = __fmaf_rn(cl, dh, t);
+    c = __fadd_rn(t, __fadd_rn(e2, es));
+}
+// s + c = a b + c d for floats (exact)
+__device__ __forceinline__ void pass_dot2f(float a, float b, float c_, float d, float &s, float &c) {
+    const float h1 = __fmul_rn(a, b);
+    const float e1 = __fmaf_rn(a, b, -h1);
+    const float h2 = __fmul_rn(c_, d);
+    const float e2 = __fmaf_rn(c_, d, -h2);
+    s = __fadd_rn(h1, h2);
+    const float bb = __fsub_rn(s, h1);
+    const float es = __fadd_rn(__fsub_rn(h1, __fsub_rn(s, bb)), __fsub_rn(h2, bb));
+    c = __fadd_rn(e1, __fadd_rn(e2, es));
+}
+// acc += sg * (s + c), sg = +-1 (sg * s is exact)
+__device__ __forceinline__ void pass_accumulate(PassAcc &acc, float sg, float s, float c) {
+    const float b = __fmul_rn(sg, s);
+    const float a1 = __fadd_rn(acc.a, b);
+    const float bb = __fsub_rn(a1, acc.a);
+    const float ea = __fadd_rn(__fsub_rn(acc.a, __fsub_rn(a1, bb)), __fsub_rn(b, bb));
+    acc.l = __fadd_rn(acc.l, __fmaf_rn(sg, c, ea));
+    acc.a = a1;
+}
+__device__ __forceinline__ float pass_sign(unsigned bit) { return bit ? -1.f : 1.f; }
+
+__device__ __forceinline__ void pass_cp_async(unsigned dst, const void *src, int bytes) {
+    if (bytes == 16) {
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+    } else {
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+    }
+}
+
+constexpr int kPass12Threads = 512;
+template <class T> constexpr size_t pass12_smem() {
+    return 2 * (sizeof(cx<T>) << 12) + sizeof(float2) * kPassTerms * kPass12Threads;
+}
+template <class T>
+__global__ void __launch_bounds__(kPass12Threads, 1)
+    k_pauli_pass12(const cx<T> *__restrict__ a, const __grid_constant__ PauliPass d, double *partials) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr bool kDF = sizeof(T) == 8; // complex128: double-float pairs
+    constexpr unsigned kT = 1u << 12;
+    constexpr unsigned kAmp = sizeof(cx<T>);
+    constexpr unsigned kTileBytes = kAmp * kT;
+    constexpr int kRows = kT / kPass12Threads; // amplitudes per thread and tile (8)
+    float2 *sums = reinterpret_cast<float2 *>(smem + 2 * kTileBytes); // [word][thread]
+    const unsigned tid = threadIdx.x;
+    const unsigned s0 = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    u64 off_t = 0;
+    for (int q = 0; q < 9; q++) {
+        off_t |= static_cast<u64>((tid >> q) & 1u) << d.lbit[q];
+    }
+    u64 off_r[kRows];
+#pragma unroll
+    for (int r = 0; r < kRows; r++) {
+        u64 o = 0;
+        for (int q = 0; q < 3; q++) {
+            o |= static_cast<u64>((r >> q) & 1) << d.lbit[9 + q];
+        }
+        off_r[r] = o;
+    }
+    for (int w = 0; w < kPassTerms; w++) {
+        sums[w * kPass12Threads + tid] = make_float2(0.f, 0.f);
+    }
+    auto tile_base = [&](u64 tt) {
+        u64 base = 0;
+        for (int q = 0; q < d.nglob; q++) {
+            base |= (tt & 1u) << d.glob[q];
+            tt >>= 1;
+        }
+        return base;
+    };
+    // local amplitude jj = r * 512 + tid of a tile, copied by thread tid
+    auto fetch = [&](u64 tt, unsigned buf) {
+        const u64 base = tile_base(tt) | off_t;
+#pragma unroll
+        for (int r = 0; r < kRows; r++) {
+            pass_cp_async(s0 + buf * kTileBytes + (static_cast<unsigned>(r) * kPass12Threads + tid) * kAmp,
+                          a + (base | off_r[r]), static_cast<int>(kAmp));
+        }
+    };
+    const u64 stride = gridDim.x;
+    u64 tile = blockIdx.x;
+    if (tile < d.ntiles) {
+        fetch(tile, 0);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    for (unsigned buf = 0; tile < d.ntiles; tile += stride, buf ^= 1u) {
+        if (tile + stride < d.ntiles) {
+            fetch(tile + stride, buf ^ 1u);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_group 1;" ::: "memory"); // this thread's copies of the tile
+        unsigned char *tb = smem + buf * kTileBytes;
+        if constexpr (kDF) { // in place: the copying thread converts its own amplitudes
+            const double2 *raw = reinterpret_cast<const double2 *>(tb);
+            float4 *tl = reinterpret_cast<float4 *>(tb);
+#pragma unroll
+            for (int r = 0; r < kRows; r++) {
+                const unsigned jj = static_cast<unsigned>(r) * kPass12Threads + tid;
+                const double2 v = raw[jj];
+                const df re = df_from_bits(v.x), im = df_from_bits(v.y);
+                tl[jj] = make_float4(re.hi, re.lo, im.hi, im.lo);
+            }
+        }
+        __syncthreads();
+        const u64 base = tile_base(tile);
+#pragma unroll 1
+        for (int w = 0; w < d.nterms; w++) {
+            const PauliPassTerm &pt = d.term[w];
+            const unsigned tpar = static_cast<unsigned>(__popcll(base & pt.yz)) & 1u;
+            const float2 sw = sums[w * kPass12Threads + tid];
+            PassAcc ac{sw.x, sw.y};
+            if (pt.x == 0) {
+                const unsigned st = (static_cast<unsigned>(__popc(tid & pt.yzl)) ^ tpar) & 1u;
+#pragma unroll
+                for (int r = 0; r < kRows; r++) {
+                    const unsigned j = static_cast<unsigned>(r) * kPass12Threads + tid;
+                    float sv, cv;
+                    if constexpr (kDF) {
+                        const float4 p = reinterpret_cast<const float4 *>(tb)[j];
+                        pass_dot2(p.x, p.y, p.x, p.y, p.z, p.w, p.z, p.w, sv, cv);
+                    } else {
+                        const float2 p = reinterpret_cast<const float2 *>(tb)[j];
+                        pass_dot2f(p.x, p.x, p.y, p.y, sv, cv);
+                    }
+                    pass_accumulate(ac, pass_sign(st ^ ((pt.srm >> r) & 1u)), sv, cv);
+                }
+            } else {
+                const unsigned hb = static_cast<unsigned>(pt.hb);
+                const unsigned jt = ((tid >> hb) << (hb + 1)) | (tid & ((1u << hb) - 1u));
+                const unsigned st = (static_cast<unsigned>(__popc(jt & pt.yzl)) ^ tpar) & 1u;
+                // Re conj(p) q = pr qr + pi qi; Im conj(p) q = pr qi - pi qr (one
+                // loop per part: a branch inside would evaluate both)
+                auto pairs = [&](auto im) {
+#pragma unroll
+                    for (int r = 0; r < kRows / 2; r++) {
+                        const unsigned j = jt | pt.jr[r];
+                        float sv, cv;
+                        if constexpr (kDF) {
+                            const float4 p = reinterpret_cast<const float4 *>(tb)[j];
+                            const float4 q = reinterpret_cast<const float4 *>(tb)[j ^ pt.x];
+                            if constexpr (decltype(im)::value) {
+                                pass_dot2(p.x, p.y, q.z, q.w, -p.z, -p.w, q.x, q.y, sv, cv);
+                            } else {
+                                pass_dot2(p.x, p.y, q.x, q.y, p.z, p.w, q.z, q.w, sv, cv);
+                            }
+                        } else {
+                            const float2 p = reinterpret_cast<const float2 *>(tb)[j];
+                            const float2 q = reinterpret_cast<const float2 *>(tb)[j ^ pt.x];
+                            if constexpr (decltype(im)::value) {
+                                pass_dot2f(p.x, q.y, -p.y, q.x, sv, cv);
+                            } else {
+                                pass_dot2f(p.x, q.x, p.y, q.y, sv, cv);
+                            }
+                        }
+                        pass_accumulate(ac, pass_sign(st ^ ((pt.srm >> r) & 1u)), sv, cv);
+                    }
+                };
+                if (pt.im) {
+                    pairs(std::true_type{});
+                } else {
+                    pairs(std::false_type{});
+                }
+            }
+            sums[w * kPass12Threads + tid] = make_float2(ac.a, ac.l);
+        }
+        __syncthreads(); // the buffer is refilled two tiles on
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    double v[kPassTerms];
+#pragma unroll
+    for (int w = 0; w < kPassTerms; w++) {
+        const float2 sw = sums[w * kPass12Threads + tid];
+        v[w] = __dadd_rn(static_cast<double>(sw.x), static_cast<double>(sw.y));
+    }
+    block_reduce_store<kPassTerms, kPass12Threads>(v, partials);
+}
+
 template <class T> int launch_pauli_pass(cudaStream_t s, const cx<T> *sv, const PauliPass &p, double *partials) {
-    const size_t smem = sizeof(float4) << p.t;
+    const bool fast = p.t == kPassMaxTileBits;
+    const size_t smem = fast ? pass12_smem<T>() : sizeof(float4) << p.t;
+    auto *kern = fast ? k_pauli_pass12<T> : k_pauli_pass<T>;
+    const int threads = fast ? kPass12Threads : kPassThreads;
     static bool attr = false;
     if (!attr) {
+        cuda_check(cudaFuncSetAttribute(k_pauli_pass12<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        static_cast<int>(pass12_smem<T>())),
+                   "k_pauli_pass12 smem attribute");
         cuda_check(cudaFuncSetAttribute(k_pauli_pass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         static_cast<int>(sizeof(float4) << kPassMaxTileBits)),
                    "k_pauli_pass smem attribute");
         attr = true;
     }
     int per_sm = 0;
-    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pauli_pass<T>, kPassThreads, smem),
-               "k_pauli_pass occupancy");
+    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem), "k_pauli_pass occupancy");
     const u64 cap = static_cast<u64>(LaunchGeom::sm_count()) * static_cast<u64>(per_sm < 1 ? 1 : per_sm);
     const int grid = static_cast<int>(p.ntiles < cap ? p.ntiles : cap);
-    k_pauli_pass<T><<<grid, kPassThreads, smem, s>>>(sv, p, partials);
+    kern<<<grid, threads, smem, s>>>(sv, p, partials);
     cuda_check(cudaGetLastError(), "k_pauli_pass launch");
     note_launch();
     return grid;

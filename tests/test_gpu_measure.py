@@ -97,6 +97,27 @@ def test_expval_pauli_hamiltonian(ops_module, oracle, dt):
 
 
 @pytest.mark.parametrize("dt", DTYPES)
+@pytest.mark.parametrize("n", [12, 15])
+def test_expval_pauli_hamiltonian_tiles(ops_module, oracle, dt, n):
+    # registers of 12 or more qubits: words evaluated in passes over tiles of
+    # 2^12 amplitudes (the pipelined pass kernel) -- diagonal words, Re and
+    # Im words (even / odd Y count), repeated flip masks, words of high weight
+    # -- and words with more flip bits than a tile holds (one sweep per mask)
+    from oracle.pyoracle import pauli_sum_spec
+
+    rng, sv, m, o = _setup(ops_module, oracle, n, dt, seed_of("ham-tiles", dt.__name__, n))
+    terms = _pauli_terms(rng, n, 48) + _pauli_terms(rng, n, 16, maxw=8)
+    terms += [(0.5, "XZ", [1, 4]), (-0.25, "XZ", [1, 7]), (0.75, "YY", [2, 3]), (0.1, "XX", [2, 3]),
+              (0.3, "Y", [n - 1]), (-0.6, "ZZ", [0, n - 1]), (0.2, "Z", [5])]
+    wide = list(range(n - 1))  # 11 or 14 flip bits
+    terms += [(0.4, ("XY" * n)[: len(wide)], wide), (-0.35, ("YYX" * n)[: len(wide)] + "Z", wide + [n - 1])]
+    H = _ham_obs(ops_module, dt, terms)
+    spec = pauli_sum_spec(terms)
+    c1 = sum(abs(t[0]) for t in terms)
+    assert_scalar(m.expval(H), o.expval_obs(spec), dt, mag=c1, what=f"E ham {n}q")
+
+
+@pytest.mark.parametrize("dt", DTYPES)
 def test_expval_mixed_observables(ops_module, oracle, dt):
     from oracle.pyoracle import ObsData
 

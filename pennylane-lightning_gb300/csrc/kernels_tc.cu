@@ -40,7 +40,6 @@
 // memory and returns; the host reads the word after the launch.
 #include "kernels_tc.hpp"
 
-#include <cuda_bf16.h>
 
 #include <atomic>
 #include <cstring>
@@ -67,6 +66,12 @@ constexpr int kTcChunksPerThread = 4096 * 8 / 16 / kTcThreads; // 16-byte copies
 constexpr unsigned kTcSmemBytes = 3 * kTcASplitBytes + 3 * kTcBSplitBytes + 2 * kTcRawBytes + 64;
 constexpr unsigned kTcTmemCols = 64;             // the 128 x 64 FP32 accumulator
 constexpr long long kTcWaitLimit = 1ll << 22;    // mbarrier polls before giving up
+// split of A and of B in each of the six products (0 = h, 1 = m, 2 = l)
+__host__ __device__ constexpr unsigned tc_pa(int p) { return p == 0 ? 2u : (p == 2 || p == 3) ? 1u : 0u; }
+__host__ __device__ constexpr unsigned tc_pb(int p) { return p == 1 ? 2u : (p == 2 || p == 4) ? 1u : 0u; }
+static_assert(tc_pa(0) == 2 && tc_pb(0) == 0 && tc_pa(1) == 0 && tc_pb(1) == 2 && tc_pa(2) == 1 && tc_pb(2) == 1 &&
+                  tc_pa(3) == 1 && tc_pb(3) == 0 && tc_pa(4) == 0 && tc_pb(4) == 1 && tc_pa(5) == 0 && tc_pb(5) == 0,
+              "products l.h, h.l, m.m, m.h, h.m, h.h");
 
 // byte offset of element (row, k) in a no-swizzle K-major operand with 128
 // K elements of 2 bytes: core matrix (row / 8, k / 8) of 8 rows x 16 bytes;
@@ -165,17 +170,15 @@ __device__ __forceinline__ void tc_ld(unsigned taddr, float (&v)[32]) {
     }
 }
 
-// x = h + m + l, three BF16 values rounded to nearest (exact for FP32 x);
-// returned as the bit patterns of the three
-__device__ __forceinline__ void split3(float x, unsigned short &h, unsigned short &m, unsigned short &l) {
-    const __nv_bfloat16 bh = __float2bfloat16_rn(x);
-    const float r1 = x - __bfloat162float(bh);
-    const __nv_bfloat16 bm = __float2bfloat16_rn(r1);
-    const float r2 = r1 - __bfloat162float(bm);
-    const __nv_bfloat16 bl = __float2bfloat16_rn(r2);
-    h = __bfloat16_as_ushort(bh);
-    m = __bfloat16_as_ushort(bm);
-    l = __bfloat16_as_ushort(bl);
+// x = h + m + l for the two floats x, y at once: three BF16 values each,
+// rounded to nearest (exact for FP32 inputs), returned as packed pairs
+// (x in the low half, y in the high half: a B-operand word (re, im))
+__device__ __forceinline__ void split3x2(float x, float y, unsigned &h, unsigned &m, unsigned &l) {
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(y), "f"(x));
+    const float rx = __fsub_rn(x, __uint_as_float(h << 16)), ry = __fsub_rn(y, __uint_as_float(h & 0xffff0000u));
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(m) : "f"(ry), "f"(rx));
+    const float sx = __fsub_rn(rx, __uint_as_float(m << 16)), sy = __fsub_rn(ry, __uint_as_float(m & 0xffff0000u));
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(l) : "f"(sy), "f"(sx));
 }
 
 __device__ __forceinline__ void cp_async16(unsigned dst, const void *src) {
@@ -305,6 +308,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const unsigned col0 = static_cast<unsigned>(kTcCols) * (warp >> 2);
 
     const unsigned a0 = smem_u32(A0), b0 = smem_u32(B0), r0 = smem_u32(R0);
+    // the address field of a descriptor is 14 bits of bytes >> 4: every
+    // operand address (below 228 KiB) fits, so offsets add without carry
+    const unsigned long long adesc0 = smem_desc(a0, kLbo, kSbo), bdesc0 = smem_desc(b0, kLbo, kSbo);
     const unsigned bar = smem_u32(mbar);
     unsigned phase = 0;
     bool failed = false;
@@ -329,14 +335,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         for (int r = 0; r < kTcPerThread; r++) {
             const float2 v = raw[raw_t ^ raw_r[r]];
             const unsigned o = b_t + (static_cast<unsigned>(r) << kUs) * 128u; // (re, im) adjacent: k = 2u, 2u + 1
-            unsigned short xh, xm, xl, yh, ym, yl;
-            split3(v.x, xh, xm, xl);
-            split3(v.y, yh, ym, yl);
-            *reinterpret_cast<unsigned *>(B0 + o) = static_cast<unsigned>(xh) | (static_cast<unsigned>(yh) << 16);
-            *reinterpret_cast<unsigned *>(B0 + kTcBSplitBytes + o) =
-                static_cast<unsigned>(xm) | (static_cast<unsigned>(ym) << 16);
-            *reinterpret_cast<unsigned *>(B0 + 2 * kTcBSplitBytes + o) =
-                static_cast<unsigned>(xl) | (static_cast<unsigned>(yl) << 16);
+            unsigned h, m, l;
+            split3x2(v.x, v.y, h, m, l);
+            *reinterpret_cast<unsigned *>(B0 + o) = h;
+            *reinterpret_cast<unsigned *>(B0 + kTcBSplitBytes + o) = m;
+            *reinterpret_cast<unsigned *>(B0 + 2 * kTcBSplitBytes + o) = l;
         }
         proxy_fence_smem();
         tc_fence_before();
@@ -351,17 +354,19 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         if (tid == 0) {
             tc_fence_after();
-            unsigned acc = 0;
-            // split pairs (A, B), smallest products first: l.h, h.l, m.m, m.h, h.m, h.h
-            const unsigned pa[6] = {2, 0, 1, 1, 0, 0}, pb[6] = {0, 2, 1, 0, 1, 0};
-            for (int p = 0; p < 6; p++) {
-                const unsigned as = a0 + pa[p] * kTcASplitBytes, bs = b0 + pb[p] * kTcBSplitBytes;
+            // split pairs (A, B), smallest products first: l.h, h.l, m.m, m.h,
+            // h.m, h.h.  The 48 descriptors are the two base descriptors plus
+            // compile-time offsets in the address field (bytes >> 4): a split
+            // stride, and 256 bytes (two 16-byte core columns, K = 16) per step.
 #pragma unroll
-                for (int ks = 0; ks < 8; ks++) { // K = 16 per instruction: two 16-byte core columns
-                    const unsigned long long ad = smem_desc(as + ks * 256u, kLbo, kSbo);
-                    const unsigned long long bd = smem_desc(bs + ks * 256u, kLbo, kSbo);
-                    tc_mma_bf16(tmem, ad, bd, acc);
-                    acc = 1;
+            for (int p = 0; p < 6; p++) {
+#pragma unroll
+                for (int ks = 0; ks < 8; ks++) {
+                    const unsigned long long ad =
+                        adesc0 + ((tc_pa(p) * kTcASplitBytes + static_cast<unsigned>(ks) * 256u) >> 4);
+                    const unsigned long long bd =
+                        bdesc0 + ((tc_pb(p) * kTcBSplitBytes + static_cast<unsigned>(ks) * 256u) >> 4);
+                    tc_mma_bf16(tmem, ad, bd, (p | ks) != 0 ? 1u : 0u);
                 }
             }
             tc_commit(bar);

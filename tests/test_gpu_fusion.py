@@ -211,3 +211,29 @@ def test_wide_local_diagonals_fused(ops_module, oracle, dt, fp64):
         ops_module.set_c128_fp64_passes(prev)
     ref = oracle_apply(oracle, n, dt, st, ops)
     assert_close(sv.state(), ref, dt, what=f"wide diagonals fp64={fp64}")
+
+
+def test_fp64_passes_keep_tiny_amplitudes(ops_module, oracle):
+    # the default complex128 passes compute in FP64: amplitudes far below the
+    # float range (1e-200) keep their relative accuracy, like the reference's
+    # f64 kernels; the opt-in double-float passes flush them to zero
+    n = 13
+    rng = np.random.default_rng(seed_of("tiny-amps"))
+    st = rand_state(rng, n) * 1e-200
+    ops = [dict(name=str(rng.choice(["RX", "RY", "RZ"])), wires=[int(w)], params=[float(rng.uniform(0, 6))])
+           for w in rng.integers(0, n, size=60)]
+    ops += [dict(name="CNOT", wires=[0, 7]), dict(name="CZ", wires=[3, 12]), dict(name="RY", wires=[5], params=[0.3])]
+    S = ops_struct(ops_module, np.complex128, ops)
+    sv = ops_module.StateVectorC128(n)
+    sv.updateData(st)
+    assert sv.applyOperations(S, 11) >= 1
+    ref = oracle_apply(oracle, n, np.complex128, st, ops)
+    assert_close(sv.state(), ref, np.complex128, what="1e-200 amplitudes, FP64 passes")
+    prev = ops_module.set_c128_fp64_passes(False)
+    try:
+        sv2 = ops_module.StateVectorC128(n)
+        sv2.updateData(st)
+        sv2.applyOperations(S, 11)
+        assert not np.any(sv2.state())
+    finally:
+        ops_module.set_c128_fp64_passes(prev)

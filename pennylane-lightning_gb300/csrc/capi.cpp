@@ -41,8 +41,8 @@ struct plgb_ops {
     std::map<std::tuple<int, int, int>, std::shared_ptr<FusedProgram<float>>> prog_f;
     std::map<std::tuple<int, int, int>, std::shared_ptr<FusedProgram<double>>> prog_d;
     // dense-block programs, keyed by (num_qubits, precision, block width)
-    std::map<std::tuple<int, int, int>, std::shared_ptr<const std::vector<Prim<float>>>> blk_f;
-    std::map<std::tuple<int, int, int>, std::shared_ptr<const std::vector<Prim<double>>>> blk_d;
+    std::map<std::tuple<int, int, int>, std::shared_ptr<const BlockProgram<float>>> blk_f;
+    std::map<std::tuple<int, int, int>, std::shared_ptr<const BlockProgram<double>>> blk_d;
     std::mutex mu;
 };
 
@@ -885,7 +885,7 @@ int plgb_sv_apply_operations_blocks(plgb_sv *sv, plgb_ops *ops, int block_wires,
         need(ops, "ops");
         using T = decltype(s.data()->x);
         PLGB_REQUIRE(block_wires >= 1 && block_wires <= 6, "block_wires must be in 1..6");
-        std::shared_ptr<const std::vector<Prim<T>>> prog;
+        std::shared_ptr<const BlockProgram<T>> prog;
         {
             std::lock_guard<std::mutex> lk(ops->mu);
             const auto key = std::make_tuple(s.num_qubits(), static_cast<int>(sizeof(T)), block_wires);
@@ -903,17 +903,15 @@ int plgb_sv_apply_operations_blocks(plgb_sv *sv, plgb_ops *ops, int block_wires,
                     auto p = s.lower_op(op, op.inverse);
                     prims.insert(prims.end(), std::make_move_iterator(p.begin()), std::make_move_iterator(p.end()));
                 }
-                auto blocks = std::make_shared<const std::vector<Prim<T>>>(
-                    fuse_dense_blocks<T>(prims, s.num_qubits(), block_wires));
+                auto blocks = prepare_blocks<T>(fuse_dense_blocks<T>(prims, s.num_qubits(), block_wires),
+                                                s.num_qubits());
                 it = cache.emplace(key, std::move(blocks)).first;
             }
             prog = it->second;
         }
-        for (const auto &p : *prog) {
-            s.run_prim(p);
-        }
+        run_blocks<T>(s, *prog);
         if (blocks_out) {
-            *blocks_out = static_cast<int>(prog->size());
+            *blocks_out = static_cast<int>(prog->prims.size());
         }
     });
 }

@@ -6,6 +6,7 @@
 #pragma once
 
 #include "kernels.hpp"
+#include "kernels_tc.hpp"
 
 #include <complex>
 #include <cstdint>
@@ -120,7 +121,9 @@ struct DeviceScratch {
     double *host_out{nullptr};  // pinned
     void *mat{nullptr};         // matrices / diagonals / offsets
     size_t mat_bytes{0};
+    int *flag{nullptr};         // error word of the tensor-core kernel (allocated on first use)
     void ensure_mat(size_t bytes);
+    int *ensure_flag();
     // Carve consecutive sub-buffers of the given byte sizes out of `mat`,
     // each starting on a 256-byte boundary (16-byte vector loads of
     // complex128 need at least 16).
@@ -287,6 +290,22 @@ void run_fused_adjoint(StateVector<T> &lam, StateVector<T> &hlam, const FusedPro
 // blocks on at most kmax bits (Pair / Dense2 / DenseK primitives; others
 // pass through)
 template <class T> std::vector<Prim<T>> fuse_dense_blocks(const std::vector<Prim<T>> &prims, int n, int kmax);
+// A dense-block program prepared for one register size: complex64 blocks on
+// six wires carry their tensor-core geometry, and their matrix images are
+// uploaded to the device once, so an application launches one kernel per
+// block and checks the tensor-core error word once at the end.
+template <class T> struct BlockProgram {
+    std::vector<Prim<T>> prims;
+    std::vector<int> tc;      // per primitive: its tensor-core block, -1 = the CUDA-core kernels
+    std::vector<TcGeom> geom; // per tensor-core block
+    void *images{nullptr};    // device: one image of tc_a_image_bytes() per tensor-core block
+    BlockProgram() = default;
+    BlockProgram(const BlockProgram &) = delete;
+    BlockProgram &operator=(const BlockProgram &) = delete;
+    ~BlockProgram() { dev_free(images); }
+};
+template <class T> std::shared_ptr<const BlockProgram<T>> prepare_blocks(std::vector<Prim<T>> prims, int n);
+template <class T> void run_blocks(StateVector<T> &sv, const BlockProgram<T> &prog);
 struct FusedStats {
     size_t passes, unfused, prims;
 };

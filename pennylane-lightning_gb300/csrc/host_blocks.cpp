@@ -390,4 +390,64 @@ template <class T> std::vector<Prim<T>> fuse_dense_blocks(const std::vector<Prim
 template std::vector<Prim<float>> fuse_dense_blocks<float>(const std::vector<Prim<float>> &, int, int);
 template std::vector<Prim<double>> fuse_dense_blocks<double>(const std::vector<Prim<double>> &, int, int);
 
+
+template <class T> std::shared_ptr<const BlockProgram<T>> prepare_blocks(std::vector<Prim<T>> prims, int n) {
+    auto prog = std::make_shared<BlockProgram<T>>();
+    prog->tc.assign(prims.size(), -1);
+    if constexpr (std::is_same_v<T, float>) {
+        std::vector<unsigned short> host;
+        const size_t words = tc_a_image_bytes() / sizeof(unsigned short);
+        for (size_t i = 0; i < prims.size(); i++) {
+            const Prim<T> &p = prims[i];
+            TcGeom g{};
+            if (p.kind == Prim<T>::DenseK && p.tbits.size() == 6 && p.cmask == 0 && tc_geom_for(n, p.tbits.data(), g)) {
+                prog->tc[i] = static_cast<int>(prog->geom.size());
+                prog->geom.push_back(g);
+                host.resize(host.size() + words);
+                tc_build_a_image(p.m.data(), g, host.data() + host.size() - words);
+            }
+        }
+        if (!prog->geom.empty()) {
+            prog->images = dev_alloc(host.size() * sizeof(unsigned short));
+            cuda_check(cudaMemcpy(prog->images, host.data(), host.size() * sizeof(unsigned short),
+                                  cudaMemcpyHostToDevice),
+                       "H2D block matrix images");
+        }
+    }
+    prog->prims = std::move(prims);
+    return prog;
+}
+
+template <class T> void run_blocks(StateVector<T> &sv, const BlockProgram<T> &prog) {
+    bool any_tc = false;
+    int *derr = nullptr;
+    for (size_t i = 0; i < prog.prims.size(); i++) {
+        if constexpr (std::is_same_v<T, float>) {
+            if (prog.tc[i] >= 0 && tc_dense_enabled()) {
+                if (!any_tc) {
+                    derr = sv.scratch().ensure_flag();
+                    cuda_check(cudaMemsetAsync(derr, 0, sizeof(int), sv.stream()), "clear error word");
+                    any_tc = true;
+                }
+                const auto *img = static_cast<const unsigned short *>(prog.images) +
+                                  static_cast<size_t>(prog.tc[i]) * (tc_a_image_bytes() / sizeof(unsigned short));
+                launch_dense6_tc(sv.stream(), sv.data(), prog.geom[static_cast<size_t>(prog.tc[i])], img, derr);
+                continue;
+            }
+        }
+        sv.run_prim(prog.prims[i]);
+    }
+    if (any_tc) {
+        int herr = 0;
+        cuda_check(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, sv.stream()), "D2H error word");
+        sv.synchronize();
+        PLGB_REQUIRE(herr == 0, "tensor-core dense block: a CTA timed out waiting for its MMAs");
+    }
+}
+
+template std::shared_ptr<const BlockProgram<float>> prepare_blocks<float>(std::vector<Prim<float>>, int);
+template std::shared_ptr<const BlockProgram<double>> prepare_blocks<double>(std::vector<Prim<double>>, int);
+template void run_blocks<float>(StateVector<float> &, const BlockProgram<float> &);
+template void run_blocks<double>(StateVector<double> &, const BlockProgram<double> &);
+
 } // namespace plgb

@@ -158,10 +158,17 @@ std::vector<char *> DeviceScratch::carve(std::initializer_list<size_t> sizes) {
     return out;
 }
 
+int *DeviceScratch::ensure_flag() {
+    if (!flag) {
+        flag = static_cast<int *>(dev_alloc(sizeof(int)));
+    }
+    return flag;
+}
 DeviceScratch::~DeviceScratch() {
     dev_free(red);
     pinned_free(host_out);
     dev_free(mat);
+    dev_free(flag);
 }
 
 static const char *kGateNames[] = {
@@ -518,8 +525,8 @@ template <class T> void StateVector<T>::run_prim(const Prim<T> &p) {
             if (k == 6 && p.cmask == 0 && tc_dense_enabled() && tc_geom_for(n_, p.tbits.data(), tg)) {
                 std::vector<unsigned short> img(tc_a_image_bytes() / sizeof(unsigned short));
                 tc_build_a_image(p.m.data(), tg, img.data());
-                const auto bufs = scratch_.carve({tc_a_image_bytes(), sizeof(int)});
-                int *derr = reinterpret_cast<int *>(bufs[1]);
+                const auto bufs = scratch_.carve({tc_a_image_bytes()});
+                int *derr = scratch_.ensure_flag();
                 cuda_check(cudaMemcpyAsync(bufs[0], img.data(), tc_a_image_bytes(), cudaMemcpyHostToDevice, s_),
                            "H2D matrix image");
                 cuda_check(cudaMemsetAsync(derr, 0, sizeof(int), s_), "clear error word");

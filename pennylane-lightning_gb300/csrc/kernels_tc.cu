@@ -16,28 +16,27 @@
 // h.m, h.h, smallest first); the three omitted ones are below 2^-24 of the
 // result, so a block is as accurate as an FP32 matrix product.
 //
-// Per CTA (256 threads, one per SM): the three splits of A (32 KiB each)
-// stay in shared memory for every tile.  Tiles arrive by 16-byte
-// asynchronous copies (cp.async) into two raw buffers, two tiles ahead, so
-// the loads of the next tiles overlap this tile's work.  Per tile the 4096
-// amplitudes are split and written to the three B operands in the
-// canonical no-swizzle K-major layout (8 x 16-byte core matrices), one
-// thread issues the 48 MMAs and commits them to an mbarrier, all threads
-// read D back from tensor memory (tcgen05.ld), stage the tile in shared
-// memory in global order and store it coalesced.
+// Per CTA (one per SM, warp-specialized, see k_dense6_tc): the three splits
+// of A (32 KiB each) stay in shared memory for every tile; B (three splits,
+// canonical no-swizzle K-major layout of 8 x 16-byte core matrices) and the
+// tensor-memory accumulator are double-buffered, so the split of one tile,
+// the MMAs of the next and the read-back and store of the previous one run
+// at the same time.
 //
 // Tile geometry: the tile's 12 local bits are the six block bits and the
 // six lowest other bits; local index jj enumerates them in ascending global
-// position, so consecutive threads touch consecutive addresses.  The member
-// index u (row of A in member order: bit q = the q-th lowest block bit) and
-// group index g are bit permutations of jj.  The split reads the raw tile
-// per (u, g) so that a warp writes 32 consecutive words of B; the raw
-// buffer and the output stage are XOR-swizzled (TcGeom) so that those reads
-// and the stage writes per tensor-memory lane are free of bank conflicts.
+// position.  The member index u (row of A in member order: bit q = the q-th
+// lowest block bit) and group index g are bit permutations of jj.  The split
+// threads read the amplitudes of (u, g) straight from global memory (in
+// whole 32-byte sectors: a warp covers two or three of the lowest index
+// bits) so that a warp writes 32 consecutive words of B; the output stage is
+// XOR-swizzled (TcGeom) so that the writes per tensor-memory lane are free of
+// bank conflicts, and its reads in global order give coalesced stores.
 //
 // Every wait is bounded: an mbarrier that does not complete within the
-// limit sets the error word, and the CTA stops issuing, frees its tensor
-// memory and returns; the host reads the word after the launch.
+// limit sets the error word and the CTA's abort flag; every role then
+// leaves its loop, the MMA thread waits for the MMAs it issued, and the
+// tensor memory is freed; the host reads the word after the launch.
 #include "kernels_tc.hpp"
 
 
@@ -49,23 +48,10 @@ namespace plgb {
 
 namespace {
 
-// 256 threads (8 warps).  The index maps below also hold for 512 threads
-// (kTcThreadBits = 9), which measured slower on a GB300 (0.61 against
-// 0.54 ms for a 2^26-amplitude gate): the phases of a tile are separated by
-// barriers, and more warps per phase do not shorten the chain.
-constexpr int kTcThreadBits = 8;
-constexpr int kTcThreads = 1 << kTcThreadBits;
-constexpr int kTcWarps = kTcThreads / 32;
-constexpr int kTcCols = 64 / (kTcWarps / 4);     // accumulator columns a warp reads back
-constexpr int kTcTileBits = 12;                  // 4096 amplitudes per tile
-constexpr int kTcPerThread = (1 << kTcTileBits) / kTcThreads; // amplitudes per thread and tile
-constexpr unsigned kTcASplitBytes = 128u * 128u * 2u;         // one BF16 split of A: 32 KiB
-constexpr unsigned kTcBSplitBytes = 64u * 128u * 2u;          // one split of B: 16 KiB
-constexpr unsigned kTcRawBytes = 4096u * 8u;                 // one tile of complex64: 32 KiB
-constexpr int kTcChunksPerThread = 4096 * 8 / 16 / kTcThreads; // 16-byte copies per thread and tile
-constexpr unsigned kTcSmemBytes = 3 * kTcASplitBytes + 3 * kTcBSplitBytes + 2 * kTcRawBytes + 64;
-constexpr unsigned kTcTmemCols = 64;             // the 128 x 64 FP32 accumulator
-constexpr long long kTcWaitLimit = 1ll << 22;    // mbarrier polls before giving up
+constexpr int kTcTileBits = 12;                          // 4096 amplitudes per tile
+constexpr unsigned kTcASplitBytes = 128u * 128u * 2u;   // one BF16 split of A: 32 KiB
+constexpr unsigned kTcBSplitBytes = 64u * 128u * 2u;    // one split of B: 16 KiB
+constexpr long long kTcWaitLimit = 1ll << 22;           // mbarrier polls before giving up
 // split of A and of B in each of the six products (0 = h, 1 = m, 2 = l)
 __host__ __device__ constexpr unsigned tc_pa(int p) { return p == 0 ? 2u : (p == 2 || p == 3) ? 1u : 0u; }
 __host__ __device__ constexpr unsigned tc_pb(int p) { return p == 1 ? 2u : (p == 2 || p == 4) ? 1u : 0u; }
@@ -134,22 +120,6 @@ __device__ __forceinline__ void tc_commit(unsigned bar) {
                  : "memory");
 }
 
-// 16 consecutive FP32 columns of this thread's tensor-memory lane
-[[maybe_unused]] __device__ __forceinline__ void tc_ld(unsigned taddr, float (&v)[16]) {
-    unsigned r[16];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-                 "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                   "=r"(r[14]), "=r"(r[15])
-                 : "r"(taddr)
-                 : "memory");
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int c = 0; c < 16; c++) {
-        v[c] = __uint_as_float(r[c]);
-    }
-}
 // 32 consecutive FP32 columns of this thread's tensor-memory lane
 __device__ __forceinline__ void tc_ld(unsigned taddr, float (&v)[32]) {
     unsigned r[32];
@@ -181,12 +151,6 @@ __device__ __forceinline__ void split3x2(float x, float y, unsigned &h, unsigned
     asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(l) : "f"(sy), "f"(sx));
 }
 
-__device__ __forceinline__ void cp_async16(unsigned dst, const void *src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // the tile number deposited into the non-local bits
 __device__ __forceinline__ u64 tile_base(const TcGeom &geom, u64 tile) {
@@ -198,44 +162,109 @@ __device__ __forceinline__ u64 tile_base(const TcGeom &geom, u64 tile) {
     return base;
 }
 
-// Copy one tile (4096 amplitudes) into a raw buffer with 16-byte
-// asynchronous copies: chunk c holds amplitudes 2c and 2c + 1 of the local
-// order, adjacent in memory (local bit 0 is index bit 0), placed at their
-// swizzled position.
-__device__ __forceinline__ void fetch_tile(const float2 *sv, u64 base, const u64 *coff, const unsigned *cdst,
-                                           unsigned raw) {
-#pragma unroll
-    for (int r = 0; r < kTcChunksPerThread; r++) {
-        cp_async16(raw + cdst[r], sv + (base | coff[r]));
+// Warp roles (288 threads, one CTA per SM):
+//   split warps 0-3: load a tile's amplitudes straight from global memory
+//     (the next tile's loads are in flight in registers while the current
+//     one is split), split them into the B operand of buffer t % 2;
+//   warp 8, one elected thread: issues the 48 MMAs of tile t into tensor
+//     memory columns 64 (t % 2) .. + 63 and commits them to an mbarrier;
+//   epilogue warps 4-7 (one per tensor-memory lane quarter): read tile t's
+//     accumulator, stage it in shared memory over B of buffer t % 2 (its
+//     MMAs are complete) and store it coalesced.
+// B and the accumulator are double-buffered, so the split of tile t + 1, the
+// MMAs of tile t and the epilogue of tile t - 1 overlap.  Every hand-off is
+// an mbarrier (B full, MMAs done, accumulator free, B free, stage written);
+// every wait is bounded, and a wait that runs out sets the CTA's abort flag
+// and the error word: all roles then leave their loops, the MMA thread waits
+// (bounded) for the MMAs it issued, and tensor memory is freed.
+constexpr int kWsSplitThreads = 128;
+constexpr int kWsEpiThreads = 128;
+constexpr int kWsThreads = kWsSplitThreads + kWsEpiThreads + 32;
+constexpr int kWsRows = 4096 / kWsSplitThreads; // amplitudes per split / epilogue thread and tile (32)
+constexpr unsigned kWsBBytes = 3 * kTcBSplitBytes;  // one B buffer (three splits): 48 KiB
+constexpr unsigned kWsTmemCols = 128;               // two 128 x 64 FP32 accumulators
+enum WsBar { kBFull = 0, kMDone = 2, kTFree = 4, kBFree = 6, kEStage = 8, kNumWsBars = 9 };
+constexpr unsigned kWsTableBytes = 32 * 8 * 2 + 32 * 4 + 16;
+constexpr unsigned kWsSmemBytes = 3 * kTcASplitBytes + 2 * kWsBBytes + kWsTableBytes + kNumWsBars * 8 + 32;
+
+// bounded wait for the phase of `bar` with parity `phase`; false when the
+// CTA aborted or the wait ran out (which aborts the CTA)
+__device__ __forceinline__ bool ws_wait(unsigned bar, unsigned phase, volatile int *abort_flag, int *err) {
+    long long polls = 0;
+    while (!mbar_try_wait(bar, phase)) {
+        if (*abort_flag) {
+            return false;
+        }
+        if (++polls > kTcWaitLimit) {
+            *abort_flag = 1;
+            atomicExch(err, 1);
+            return false;
+        }
     }
+    return true;
+}
+__device__ __forceinline__ void mbar_arrive(unsigned bar) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(bar) : "memory");
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __launch_bounds__(kWsThreads, 1)
     k_dense6_tc(float2 *__restrict__ sv, TcGeom geom, const uint4 *__restrict__ a_img, int *__restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    // A splits h, m, l | B splits h, m, l | two raw tile buffers | mbarrier |
-    // tensor-memory address
+    // A splits h, m, l | B buffers 0, 1 (each splits h, m, l) | offset tables
+    // | mbarriers | tensor-memory address | abort flag
     unsigned char *A0 = smem;
-    unsigned char *B0 = smem + 3 * kTcASplitBytes;
-    unsigned char *R0 = B0 + 3 * kTcBSplitBytes;
-    unsigned long long *mbar = reinterpret_cast<unsigned long long *>(R0 + 2 * kTcRawBytes);
-    unsigned *tslot = reinterpret_cast<unsigned *>(R0 + 2 * kTcRawBytes + 16);
-    float2 *stage = reinterpret_cast<float2 *>(B0); // the tile in local order, after the MMAs (32 of 48 KiB)
+    unsigned char *Bbuf = smem + 3 * kTcASplitBytes;
+    u64 *soff_r = reinterpret_cast<u64 *>(Bbuf + 2 * kWsBBytes);  // split: per-row global offsets
+    u64 *eoff_r = soff_r + 32;                                     // epilogue: per-row global offsets
+    unsigned *est_r = reinterpret_cast<unsigned *>(eoff_r + 32);   // epilogue: per-row stage positions
+    unsigned long long *bars = reinterpret_cast<unsigned long long *>(Bbuf + 2 * kWsBBytes + kWsTableBytes);
+    unsigned *tslot = reinterpret_cast<unsigned *>(bars + kNumWsBars);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tslot + 1);
 
     const unsigned tid = threadIdx.x;
     const unsigned warp = tid >> 5, lane = tid & 31u;
+    auto dep = [&](unsigned jj) { // local index -> offset of its bits in the full index
+        u64 o = 0;
+        for (int q = 0; q < kTcTileBits; q++) {
+            o |= static_cast<u64>((jj >> q) & 1u) << geom.lbit[q];
+        }
+        return o;
+    };
+    auto swz = [&](unsigned jj) { // stage position of a local index
+        unsigned x = jj;
+#pragma unroll
+        for (int q = 4; q < 12; q++) {
+            x ^= ((jj >> q) & 1u) ? geom.hst[q] : 0u;
+        }
+        return x;
+    };
 
-    for (unsigned i = tid; i < 3 * kTcASplitBytes / 16; i += kTcThreads) {
+    for (unsigned i = tid; i < 3 * kTcASplitBytes / 16; i += kWsThreads) {
         reinterpret_cast<uint4 *>(smem)[i] = a_img[i];
+    }
+    if (tid < 32) {
+        // split thread (warp w, lane l) row r: g = (l >> 2) | (w << 3) | ((r & 1) << 5),
+        // u = (l & 3) | ((r >> 1) << 2); the row part of its local index
+        soff_r[tid] = dep(geom.jj_of_u[(tid >> 1) << 2] | geom.jj_of_g[(tid & 1u) << 5]);
+        // epilogue thread e row r: local index jj = r * 128 + e
+        eoff_r[tid] = dep(tid << 7);
+        est_r[tid] = swz(tid << 7);
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
-                     "r"(kTcTmemCols)
+                     "r"(kWsTmemCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        mbar_init(smem_u32(mbar), 1);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(smem_u32(&bars[kBFull + b]), kWsSplitThreads);
+            mbar_init(smem_u32(&bars[kMDone + b]), 1);
+            mbar_init(smem_u32(&bars[kTFree + b]), kWsEpiThreads);
+            mbar_init(smem_u32(&bars[kBFree + b]), kWsEpiThreads);
+        }
+        mbar_init(smem_u32(&bars[kEStage]), kWsEpiThreads);
+        *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     proxy_fence_smem(); // A written by the generic proxy, read by the MMAs
@@ -243,121 +272,116 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __syncthreads();
     tc_fence_after();
     const unsigned tmem = *tslot;
-
-    // XOR swizzle of a local index (linear in its bits 4-11)
-    auto swz = [&](unsigned jj, const unsigned short *h) {
-        unsigned x = jj;
-#pragma unroll
-        for (int q = 4; q < 12; q++) {
-            x ^= ((jj >> q) & 1u) ? h[q] : 0u;
-        }
-        return x;
-    };
-    // store phase: local index jj = r * kTcThreads + tid, read from the
-    // swizzled stage, written to global memory (consecutive threads,
-    // consecutive addresses)
-    u64 off_t = 0;
-    for (int q = 0; q < kTcThreadBits; q++) {
-        off_t |= static_cast<u64>((tid >> q) & 1u) << geom.lbit[q];
-    }
-    const unsigned st_t = swz(tid, geom.hst);
-    unsigned st_r[kTcPerThread];
-    u64 off_r[kTcPerThread];
-#pragma unroll
-    for (int r = 0; r < kTcPerThread; r++) {
-        st_r[r] = swz(static_cast<unsigned>(r) << kTcThreadBits, geom.hst);
-        u64 o = 0;
-        for (int q = 0; q < kTcTileBits - kTcThreadBits; q++) {
-            o |= static_cast<u64>((r >> q) & 1) << geom.lbit[kTcThreadBits + q];
-        }
-        off_r[r] = o;
-    }
-    // split phase: this thread handles group g = (lane >> 2) | ((warp & 7)
-    // << 3) and member u = (lane & 3) | (uh << 2), uh = (warp >> 3) | (r <<
-    // (threads bits - 8)), so a warp's B stores are 32 consecutive words;
-    // the raw tile is read at its swizzled position
-    constexpr int kUs = kTcThreadBits - 8; // member bits from the warp index
-    const unsigned g_me = (lane >> 2) | ((warp & 7u) << 3);
-    const unsigned raw_t =
-        swz(geom.jj_of_u[(lane & 3u) | ((warp >> 3) << 2)] | geom.jj_of_g[g_me], geom.hraw);
-    unsigned raw_r[kTcPerThread];
-#pragma unroll
-    for (int r = 0; r < kTcPerThread; r++) {
-        raw_r[r] = swz(geom.jj_of_u[static_cast<unsigned>(r) << (2 + kUs)], geom.hraw);
-    }
-    // kmajor_off(g, 2u) for r = 0
-    const unsigned b_t = ((warp & 7u) * 16u + (warp >> 3)) * 128u + lane * 4u;
-    // global offsets and swizzled raw positions of this thread's copy
-    // chunks: local index 2c with c = r * 256 + tid
-    u64 coff[kTcChunksPerThread];
-    unsigned cdst[kTcChunksPerThread];
-#pragma unroll
-    for (int r = 0; r < kTcChunksPerThread; r++) {
-        const unsigned c = static_cast<unsigned>(r) * kTcThreads + tid;
-        u64 o = 0;
-        for (int q = 0; q < 11; q++) {
-            o |= static_cast<u64>((c >> q) & 1u) << geom.lbit[q + 1];
-        }
-        coff[r] = o;
-        cdst[r] = swz(2u * c, geom.hraw) * 8u; // byte offset of the pair (bit 0 is never swizzled)
-    }
-    // stage writes: tensor-memory lane m = 32 (warp % 4) + lane is member
-    // u = m / 2, component m % 2
-    const unsigned row = 32u * (warp & 3u) + lane;
-    const unsigned st_u = geom.st_of_u[row >> 1];
-    const unsigned col0 = static_cast<unsigned>(kTcCols) * (warp >> 2);
-
-    const unsigned a0 = smem_u32(A0), b0 = smem_u32(B0), r0 = smem_u32(R0);
-    // the address field of a descriptor is 14 bits of bytes >> 4: every
-    // operand address (below 228 KiB) fits, so offsets add without carry
-    const unsigned long long adesc0 = smem_desc(a0, kLbo, kSbo), bdesc0 = smem_desc(b0, kLbo, kSbo);
-    const unsigned bar = smem_u32(mbar);
-    unsigned phase = 0;
-    bool failed = false;
-
-    // prefetch the first two tiles (one commit group each, empty when absent)
     const u64 stride = gridDim.x;
-    u64 tile = blockIdx.x;
-    for (int k = 0; k < 2; k++) {
-        const u64 t = tile + static_cast<u64>(k) * stride;
-        if (t < geom.ntiles) {
-            fetch_tile(sv, tile_base(geom, t), coff, cdst, r0 + static_cast<unsigned>(k) * kTcRawBytes);
-        }
-        cp_async_commit();
-    }
-    for (unsigned buf = 0; tile < geom.ntiles && !failed; tile += stride, buf ^= 1u) {
-        const u64 base = tile_base(geom, tile);
-        cp_async_wait1(); // this tile's group has landed (the next one may be in flight)
-        __syncthreads();
-        // split the tile into the B operands
-        const float2 *raw = reinterpret_cast<const float2 *>(R0 + buf * kTcRawBytes);
+
+    if (warp < 4) {
+        // ---------------------------------------------------------------- split
+        const unsigned g0 = (lane >> 2) | (warp << 3);
+        const u64 off_t = dep(geom.jj_of_u[lane & 3u] | geom.jj_of_g[g0]);
+        const unsigned b_t = (warp * 16u) * 128u + lane * 4u; // kmajor_off(g0, 2 (lane & 3))
+        float2 cur[kWsRows], nxt[kWsRows];
+        auto load = [&](float2 (&dst)[kWsRows], u64 tt) {
+            const u64 base = tile_base(geom, tt) | off_t;
 #pragma unroll
-        for (int r = 0; r < kTcPerThread; r++) {
-            const float2 v = raw[raw_t ^ raw_r[r]];
-            const unsigned o = b_t + (static_cast<unsigned>(r) << kUs) * 128u; // (re, im) adjacent: k = 2u, 2u + 1
-            unsigned h, m, l;
-            split3x2(v.x, v.y, h, m, l);
-            *reinterpret_cast<unsigned *>(B0 + o) = h;
-            *reinterpret_cast<unsigned *>(B0 + kTcBSplitBytes + o) = m;
-            *reinterpret_cast<unsigned *>(B0 + 2 * kTcBSplitBytes + o) = l;
-        }
-        proxy_fence_smem();
-        tc_fence_before();
-        __syncthreads();
-        // the raw buffer is consumed: fetch the tile after next into it
-        {
-            const u64 t = tile + 2 * stride;
-            if (t < geom.ntiles) {
-                fetch_tile(sv, tile_base(geom, t), coff, cdst, r0 + buf * kTcRawBytes);
+            for (int r = 0; r < kWsRows; r++) {
+                dst[r] = __ldcs(&sv[base | soff_r[r]]);
             }
-            cp_async_commit();
+        };
+        u64 tile = blockIdx.x;
+        if (tile < geom.ntiles) {
+            load(cur, tile);
         }
-        if (tid == 0) {
+        auto step = [&](float2 (&now)[kWsRows], float2 (&next)[kWsRows], unsigned t) -> bool {
+            const unsigned b = t & 1u, k = t >> 1;
+            if (tile + stride < geom.ntiles) {
+                load(next, tile + stride);
+            }
+            if (t >= 2 && !ws_wait(smem_u32(&bars[kBFree + b]), (k - 1) & 1u, abort_flag, err)) {
+                return false;
+            }
+            unsigned char *B0 = Bbuf + b * kWsBBytes;
+#pragma unroll
+            for (int r = 0; r < kWsRows; r++) {
+                // (re, im) adjacent: k = 2u, 2u + 1 of group g
+                const unsigned o = b_t + ((static_cast<unsigned>(r & 1) * 64u + static_cast<unsigned>(r >> 1)) * 128u);
+                unsigned h, m, l;
+                split3x2(now[r].x, now[r].y, h, m, l);
+                *reinterpret_cast<unsigned *>(B0 + o) = h;
+                *reinterpret_cast<unsigned *>(B0 + kTcBSplitBytes + o) = m;
+                *reinterpret_cast<unsigned *>(B0 + 2 * kTcBSplitBytes + o) = l;
+            }
+            proxy_fence_smem();
+            mbar_arrive(smem_u32(&bars[kBFull + b]));
+            return true;
+        };
+        for (unsigned t = 0; tile < geom.ntiles && !*abort_flag; t += 2) {
+            if (!step(cur, nxt, t)) {
+                break;
+            }
+            tile += stride;
+            if (tile >= geom.ntiles || *abort_flag) {
+                break;
+            }
+            if (!step(nxt, cur, t + 1)) {
+                break;
+            }
+            tile += stride;
+        }
+    } else if (warp < 8) {
+        // ------------------------------------------------------------- epilogue
+        const unsigned ew = warp - 4, e = tid - kWsSplitThreads;
+        const unsigned row = 32u * ew + lane; // accumulator row m: member m / 2, component m % 2
+        const unsigned st_u = geom.st_of_u[row >> 1], comp = row & 1u;
+        const u64 off_e = dep(e);
+        const unsigned st_e = swz(e);
+        unsigned t = 0;
+        for (u64 tile = blockIdx.x; tile < geom.ntiles && !*abort_flag; tile += stride, t++) {
+            const unsigned b = t & 1u, k = t >> 1;
+            if (!ws_wait(smem_u32(&bars[kMDone + b]), k & 1u, abort_flag, err)) {
+                break;
+            }
             tc_fence_after();
-            // split pairs (A, B), smallest products first: l.h, h.l, m.m, m.h,
-            // h.m, h.h.  The 48 descriptors are the two base descriptors plus
-            // compile-time offsets in the address field (bytes >> 4): a split
-            // stride, and 256 bytes (two 16-byte core columns, K = 16) per step.
+            float d0[32], d1[32];
+            tc_ld(tmem + ((32u * ew) << 16) + 64u * b, d0);
+            tc_ld(tmem + ((32u * ew) << 16) + 64u * b + 32u, d1);
+            tc_fence_before();
+            mbar_arrive(smem_u32(&bars[kTFree + b])); // the accumulator may be overwritten
+            // stage over B of this buffer (its MMAs are complete)
+            float *st = reinterpret_cast<float *>(Bbuf + b * kWsBBytes);
+#pragma unroll
+            for (int c = 0; c < 32; c++) {
+                st[2u * (st_u ^ geom.st_of_g[c]) + comp] = d0[c];
+                st[2u * (st_u ^ geom.st_of_g[32 + c]) + comp] = d1[c];
+            }
+            mbar_arrive(smem_u32(&bars[kEStage]));
+            if (!ws_wait(smem_u32(&bars[kEStage]), t & 1u, abort_flag, err)) {
+                break;
+            }
+            const float2 *stage = reinterpret_cast<const float2 *>(st);
+            const u64 base = tile_base(geom, tile) | off_e;
+#pragma unroll 8
+            for (int r = 0; r < kWsRows; r++) {
+                __stcs(&sv[base | eoff_r[r]], stage[st_e ^ est_r[r]]);
+            }
+            mbar_arrive(smem_u32(&bars[kBFree + b])); // the stage has been read
+        }
+    } else if (lane == 0) {
+        // ------------------------------------------------------------------ MMA
+        const unsigned a0 = smem_u32(A0);
+        const unsigned long long adesc0 = smem_desc(a0, kLbo, kSbo);
+        unsigned t = 0;
+        bool issued = false;
+        unsigned last_b = 0, last_k = 0;
+        for (u64 tile = blockIdx.x; tile < geom.ntiles && !*abort_flag; tile += stride, t++) {
+            const unsigned b = t & 1u, k = t >> 1;
+            if (t >= 2 && !ws_wait(smem_u32(&bars[kTFree + b]), (k - 1) & 1u, abort_flag, err)) {
+                break;
+            }
+            if (!ws_wait(smem_u32(&bars[kBFull + b]), k & 1u, abort_flag, err)) {
+                break;
+            }
+            tc_fence_after();
+            const unsigned long long bdesc0 = smem_desc(smem_u32(Bbuf + b * kWsBBytes), kLbo, kSbo);
 #pragma unroll
             for (int p = 0; p < 6; p++) {
 #pragma unroll
@@ -366,53 +390,25 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                         adesc0 + ((tc_pa(p) * kTcASplitBytes + static_cast<unsigned>(ks) * 256u) >> 4);
                     const unsigned long long bd =
                         bdesc0 + ((tc_pb(p) * kTcBSplitBytes + static_cast<unsigned>(ks) * 256u) >> 4);
-                    tc_mma_bf16(tmem, ad, bd, (p | ks) != 0 ? 1u : 0u);
+                    tc_mma_bf16(tmem + 64u * b, ad, bd, (p | ks) != 0 ? 1u : 0u);
                 }
             }
-            tc_commit(bar);
+            tc_commit(smem_u32(&bars[kMDone + b]));
+            issued = true;
+            last_b = b;
+            last_k = k;
         }
-        // wait for the MMAs (bounded)
-        long long polls = 0;
-        while (!mbar_try_wait(bar, phase)) {
-            if (++polls > kTcWaitLimit) {
-                failed = true;
-                break;
+        // no MMA may be in flight when the tensor memory is freed
+        if (issued) {
+            long long polls = 0;
+            while (!mbar_try_wait(smem_u32(&bars[kMDone + last_b]), last_k & 1u) && ++polls <= kTcWaitLimit) {
             }
         }
-        failed = __syncthreads_or(failed) != 0;
-        if (failed) {
-            if (tid == 0) {
-                atomicExch(err, 1);
-            }
-            break;
-        }
-        phase ^= 1u;
-        tc_fence_after();
-        // D row m = 32 (warp % 4) + lane; warp w reads kTcCols columns from
-        // kTcCols * (w / 4).  The MMAs have consumed B, so the stage (over
-        // the B splits) may be written.
-        {
-            float d[kTcCols];
-            tc_ld(tmem + ((32u * (warp & 3u)) << 16) + col0, d);
-            float *st = reinterpret_cast<float *>(stage);
-            const unsigned comp = row & 1u;
-#pragma unroll
-            for (int c = 0; c < kTcCols; c++) {
-                st[2u * (st_u ^ geom.st_of_g[col0 + static_cast<unsigned>(c)]) + comp] = d[c];
-            }
-        }
-        tc_fence_before();
-        __syncthreads();
-#pragma unroll
-        for (int r = 0; r < kTcPerThread; r++) {
-            __stcs(&sv[base | off_t | off_r[r]], stage[st_t ^ st_r[r]]);
-        }
-        __syncthreads(); // the stage is read before the next tile's B writes
     }
-    cp_async_wait0(); // no copy into shared memory outlives the CTA
     __syncthreads();
     if (warp == 0) {
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols)
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kWsTmemCols)
                      : "memory");
     }
 }
@@ -455,9 +451,6 @@ bool tc_geom_for(int n, const int *bits6, TcGeom &g) {
             g.glob[g.nglob++] = b;
         }
     }
-    if (g.lbit[0] != 0) { // the 16-byte copies need adjacent amplitude pairs
-        return false;
-    }
     g.ntiles = u64{1} << (n - kTcTileBits);
     int upos[6], gpos[6];
     for (int q = 0; q < 6; q++) {
@@ -481,11 +474,9 @@ bool tc_geom_for(int n, const int *bits6, TcGeom &g) {
         g.jj_of_g[v] = static_cast<unsigned short>(jg);
         g.mat_of_u[v] = static_cast<unsigned short>(mi);
     }
-    // Swizzles: the jj bits that vary across the lanes of a half-warp at
-    // positions 4 and up are mapped onto the free positions among the
-    // bank-selecting ones.  Raw buffer (8-byte reads, pairs kept together):
-    // lanes vary u0, u1, g0, g1; positions 1-3 are available.  Stage
-    // (4-byte writes of (u, component)): lanes vary u0-u3; positions 0-3.
+    // Stage swizzle: the jj bits that vary across the lanes of a warp's
+    // 4-byte writes of (u, component) -- u0-u3 -- at positions 4 and up are
+    // mapped onto the free positions among the bank-selecting ones 0-3.
     auto assign = [&](const int *lanes, int nlanes, int first, unsigned short *h) {
         bool used[4] = {};
         for (int i = 0; i < nlanes; i++) {
@@ -506,9 +497,7 @@ bool tc_geom_for(int n, const int *bits6, TcGeom &g) {
             }
         }
     };
-    const int raw_lanes[4] = {upos[0], upos[1], gpos[0], gpos[1]};
     const int st_lanes[4] = {upos[0], upos[1], upos[2], upos[3]};
-    assign(raw_lanes, 4, 1, g.hraw);
     assign(st_lanes, 4, 0, g.hst);
     auto swz = [&](unsigned jj, const unsigned short *h) {
         unsigned x = jj;
@@ -577,15 +566,15 @@ bool set_tc_dense_enabled(bool on) { return g_tc_dense.exchange(on); }
 void launch_dense6_tc(cudaStream_t s, cx<float> *sv, const TcGeom &geom, const unsigned short *a_img, int *err) {
     static bool attr_set = false;
     if (!attr_set) {
-        cuda_check(cudaFuncSetAttribute(k_dense6_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemBytes),
+        cuda_check(cudaFuncSetAttribute(k_dense6_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kWsSmemBytes),
                    "cudaFuncSetAttribute(k_dense6_tc)");
         attr_set = true;
     }
     const u64 want = geom.ntiles;
     const u64 cap = static_cast<u64>(LaunchGeom::sm_count());
     const unsigned grid = static_cast<unsigned>(want < cap ? want : cap);
-    k_dense6_tc<<<grid, kTcThreads, kTcSmemBytes, s>>>(reinterpret_cast<float2 *>(sv), geom,
-                                                        reinterpret_cast<const uint4 *>(a_img), err);
+    k_dense6_tc<<<grid, kWsThreads, kWsSmemBytes, s>>>(reinterpret_cast<float2 *>(sv), geom,
+                                                       reinterpret_cast<const uint4 *>(a_img), err);
     cuda_check(cudaGetLastError(), "k_dense6_tc launch");
     note_launch();
 }

@@ -10,11 +10,10 @@ namespace plgb {
 // local bits (the block bits and the six lowest other bits) in ascending
 // order give the local index jj.  Member index u (the block's own index,
 // bit q = the q-th lowest block bit) and group index g (bit q = the q-th
-// lowest other local bit) are bit permutations of jj.  Two shared-memory
-// buffers are XOR-swizzled on jj (linear maps of jj's bits 4-11 into bits
-// 0-3) so that the accesses of a warp fall in distinct banks: the raw tile
-// (read per (u, g) in the split) and the output stage (written per tensor
-// memory lane).
+// lowest other local bit) are bit permutations of jj.  The output stage in
+// shared memory is XOR-swizzled on jj (a linear map of jj's bits 4-11 into
+// bits 0-3) so that its writes per tensor-memory lane fall in distinct
+// banks.
 struct TcGeom {
     int lbit[12];
     int glob[64];
@@ -22,7 +21,6 @@ struct TcGeom {
     u64 ntiles;
     unsigned short jj_of_u[64];
     unsigned short jj_of_g[64];
-    unsigned short hraw[12]; // XOR mask of raw-buffer position per jj bit
     unsigned short hst[12];  // XOR mask of stage position per jj bit
     unsigned short st_of_u[64], st_of_g[64]; // swizzled stage positions of u and g alone
     unsigned short mat_of_u[64];             // row of the caller's matrix for member u

@@ -42,6 +42,7 @@
 
 #include <atomic>
 #include <cstring>
+#include <string>
 #include <vector>
 
 namespace plgb {
@@ -172,7 +173,10 @@ __device__ __forceinline__ u64 tile_base(const TcGeom &geom, u64 tile) {
 //     accumulator, stage it in shared memory over B of buffer t % 2 (its
 //     MMAs are complete) and store it coalesced.
 // B and the accumulator are double-buffered, so the split of tile t + 1, the
-// MMAs of tile t and the epilogue of tile t - 1 overlap.  Every hand-off is
+// MMAs of tile t and the epilogue of tile t - 1 overlap.  (Eight split warps
+// with two tiles of loads in flight measured slower: 0.29-0.30 against
+// 0.27-0.29 ms for a 2^26-amplitude gate, the register budget of 416
+// threads forcing spills.)  Every hand-off is
 // an mbarrier (B full, MMAs done, accumulator free, B free, stage written);
 // every wait is bounded, and a wait that runs out sets the CTA's abort flag
 // and the error word: all roles then leave their loops, the MMA thread waits
@@ -575,7 +579,15 @@ void launch_dense6_tc(cudaStream_t s, cx<float> *sv, const TcGeom &geom, const u
     const unsigned grid = static_cast<unsigned>(want < cap ? want : cap);
     k_dense6_tc<<<grid, kWsThreads, kWsSmemBytes, s>>>(reinterpret_cast<float2 *>(sv), geom,
                                                        reinterpret_cast<const uint4 *>(a_img), err);
-    cuda_check(cudaGetLastError(), "k_dense6_tc launch");
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) {
+        cudaFuncAttributes fa{};
+        cudaFuncGetAttributes(&fa, k_dense6_tc);
+        cuda_check(le, ("k_dense6_tc launch (" + std::to_string(kWsThreads) + " threads, " +
+                        std::to_string(fa.numRegs) + " registers, max " + std::to_string(fa.maxThreadsPerBlock) +
+                        " threads per block, " + std::to_string(kWsSmemBytes) + " B dynamic shared memory)")
+                           .c_str());
+    }
     note_launch();
 }
 

@@ -399,9 +399,15 @@ def gpu_arm(args) -> dict | None:
         sv64 = ops.StateVectorC64(n)
         s64 = torch.cuda.ExternalStream(sv64.cuda_stream())
         t64 = {}
-        for tb in ((11, 12) if args.tile_bits is None else (args.tile_bits,)):
-            timed_step(sv64, S64, s64, tb)
-            t64[tb] = timed_step(sv64, S64, s64, tb)[0]
+        # tile passes: complex64 registers of 22 qubits and more run
+        # applyOperations as dense blocks while the tensor cores are on
+        prev_tc = ops.set_tc_dense(False)
+        try:
+            for tb in ((11, 12) if args.tile_bits is None else (args.tile_bits,)):
+                timed_step(sv64, S64, s64, tb)
+                t64[tb] = timed_step(sv64, S64, s64, tb)[0]
+        finally:
+            ops.set_tc_dense(prev_tc)
         b64 = min(t64, key=t64.get)
         # dense-block fusion, fusion widths k = 2..6 (complex64 blocks of 4-6
         # wires on the tensor cores)

@@ -185,8 +185,11 @@ int plgb_ops_num_par_ops(const plgb_ops *ops, int *out);
  * 127-175): apply every operation of `ops` (each with its own inverse flag).
  * tile_bits = 0 launches one kernel per gate; tile_bits = t > 0 fuses the
  * list into shared-memory tile passes of up to 2^t amplitudes (the compiled
- * passes are cached on `ops` per register size, precision and t).
- * *passes_out (optional) receives the number of kernel passes per call. */
+ * passes are cached on `ops` per register size, precision and t); complex64
+ * registers of 22 qubits and more instead run it as dense blocks of up to six
+ * wires (as plgb_sv_apply_operations_blocks with 6) while the tensor cores are
+ * on (plgb_set_tc_dense).  *passes_out (optional) receives the number of
+ * kernel passes (or blocks) per call. */
 int plgb_sv_apply_operations(plgb_sv *sv, plgb_ops *ops, int tile_bits, int *passes_out);
 /* Dense-block fusion (no counterpart in the reference): the operations of
  * `ops` merged, in order, into dense blocks on at most block_wires (1..6)

@@ -93,13 +93,57 @@ void need(const void *p, const char *what) {
 std::atomic<int> g_lazy_fusion{1};
 std::atomic<int> g_lazy_min_qubits{17};
 constexpr size_t kLazyFuseMin = 16;
+// Complex64 registers from 22 qubits on run fused gate lists as dense blocks
+// of up to six wires (six-wire blocks on the tensor cores) instead of tile
+// passes: measured faster on the config-0, -1 and -3 circuits at 22, 26 and
+// 29 qubits (1.2-1.7x).  Switched off with the tensor cores
+// (plgb_set_tc_dense(0)).
+constexpr int kC64BlocksMinQubits = 22;
+template <class T> bool blocks_preferred(const StateVector<T> &s) {
+    return std::is_same_v<T, float> && s.num_qubits() >= kC64BlocksMinQubits && tc_dense_enabled();
+}
+
+// the operation list as dense blocks of at most block_wires wires, the block
+// program cached on the ops object per (register size, precision, width);
+// returns the number of blocks
+template <class T> int apply_ops_blocks(StateVector<T> &s, plgb_ops *ops, int block_wires) {
+    std::shared_ptr<const BlockProgram<T>> prog;
+    {
+        std::lock_guard<std::mutex> lk(ops->mu);
+        const auto key = std::make_tuple(s.num_qubits(), static_cast<int>(sizeof(T)), block_wires);
+        auto &cache = [&]() -> auto & {
+            if constexpr (std::is_same_v<T, double>) {
+                return ops->blk_d;
+            } else {
+                return ops->blk_f;
+            }
+        }();
+        auto it = cache.find(key);
+        if (it == cache.end()) {
+            std::vector<Prim<T>> prims;
+            for (const auto &op : ops->list.ops) {
+                auto p = s.lower_op(op, op.inverse);
+                prims.insert(prims.end(), std::make_move_iterator(p.begin()), std::make_move_iterator(p.end()));
+            }
+            auto blocks =
+                prepare_blocks<T>(fuse_dense_blocks<T>(prims, s.num_qubits(), block_wires), s.num_qubits());
+            it = cache.emplace(key, std::move(blocks)).first;
+        }
+        prog = it->second;
+    }
+    run_blocks<T>(s, *prog);
+    return static_cast<int>(prog->prims.size());
+}
+
 template <class T> void run_pending(StateVector<T> &s, std::vector<Prim<T>> &pend) {
     if (pend.empty()) {
         return;
     }
     std::vector<Prim<T>> prims;
     prims.swap(pend); // the queue is empty whatever happens next
-    if (s.num_qubits() >= kMinRegTileBits && prims.size() >= kLazyFuseMin) {
+    if (blocks_preferred(s) && prims.size() >= kLazyFuseMin) {
+        run_blocks<T>(s, *prepare_blocks<T>(fuse_dense_blocks<T>(prims, s.num_qubits(), 6), s.num_qubits()));
+    } else if (s.num_qubits() >= kMinRegTileBits && prims.size() >= kLazyFuseMin) {
         s.apply_prims_fused(prims, sizeof(T) == 8 ? 11 : 12);
     } else {
         for (const auto &p : prims) {
@@ -840,6 +884,14 @@ int plgb_sv_apply_operations(plgb_sv *sv, plgb_ops *ops, int tile_bits, int *pas
     return with_sv(sv, [&](auto &s) {
         need(ops, "ops");
         using T = decltype(s.data()->x);
+        if (tile_bits > 0 && blocks_preferred(s)) {
+            PLGB_REQUIRE(tile_bits <= 14, "tile_bits must be in 1..14");
+            const int nb = apply_ops_blocks<T>(s, ops, 6);
+            if (passes_out) {
+                *passes_out = nb;
+            }
+            return;
+        }
         if (tile_bits <= 0) {
             for (const auto &op : ops->list.ops) {
                 s.apply_op(op, op.inverse);
@@ -885,33 +937,9 @@ int plgb_sv_apply_operations_blocks(plgb_sv *sv, plgb_ops *ops, int block_wires,
         need(ops, "ops");
         using T = decltype(s.data()->x);
         PLGB_REQUIRE(block_wires >= 1 && block_wires <= 6, "block_wires must be in 1..6");
-        std::shared_ptr<const BlockProgram<T>> prog;
-        {
-            std::lock_guard<std::mutex> lk(ops->mu);
-            const auto key = std::make_tuple(s.num_qubits(), static_cast<int>(sizeof(T)), block_wires);
-            auto &cache = [&]() -> auto & {
-                if constexpr (std::is_same_v<T, double>) {
-                    return ops->blk_d;
-                } else {
-                    return ops->blk_f;
-                }
-            }();
-            auto it = cache.find(key);
-            if (it == cache.end()) {
-                std::vector<Prim<T>> prims;
-                for (const auto &op : ops->list.ops) {
-                    auto p = s.lower_op(op, op.inverse);
-                    prims.insert(prims.end(), std::make_move_iterator(p.begin()), std::make_move_iterator(p.end()));
-                }
-                auto blocks = prepare_blocks<T>(fuse_dense_blocks<T>(prims, s.num_qubits(), block_wires),
-                                                s.num_qubits());
-                it = cache.emplace(key, std::move(blocks)).first;
-            }
-            prog = it->second;
-        }
-        run_blocks<T>(s, *prog);
+        const int nb = apply_ops_blocks<T>(s, ops, block_wires);
         if (blocks_out) {
-            *blocks_out = static_cast<int>(prog->prims.size());
+            *blocks_out = nb;
         }
     });
 }

@@ -283,8 +283,10 @@ class _StateVectorBase:
         """Apply an OpsStruct list (StateVectorBase::applyOperations).
 
         tile_bits = 0 runs one kernel per gate; tile_bits = t > 0 fuses the
-        list into shared-memory tile passes of 2^t amplitudes.  Returns the
-        number of kernel passes the call issued."""
+        list into shared-memory tile passes of 2^t amplitudes (complex64
+        registers of 22 qubits and more: dense blocks of up to six wires on
+        the tensor cores while set_tc_dense is on).  Returns the number of
+        kernel passes the call issued."""
         passes = C.c_int()
         call("plgb_sv_apply_operations", self._h, ops._h, int(tile_bits), C.byref(passes))
         return passes.value

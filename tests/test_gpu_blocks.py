@@ -43,3 +43,40 @@ def test_config1_blocks(ops_module, oracle, dt, k):
     sv.resetStateVector()
     sv.applyOperationsBlocks(S, k)
     assert_state(sv.state(), ref, dt, what=f"config-1 blocks k={k}, cached")
+
+
+def test_c64_large_registers_run_blocks_by_default(ops_module, oracle):
+    # complex64 registers of 22 qubits and more run applyOperations and the
+    # lazy per-gate queue as dense blocks (six-wire blocks on the tensor
+    # cores); with the tensor cores off they take the tile passes.  All
+    # three agree with the oracle's complex128 state at the complex64
+    # tolerance.
+    from lightning_gb300.workloads import config0
+
+    n = 22
+    circuit = config0(n, 3, seed=1000)
+    ops = [op.as_dict() for op in circuit]
+    S = ops_module.OpsStructC64([o["name"] for o in ops], [o.get("params", []) for o in ops],
+                                [o["wires"] for o in ops], [False] * len(ops), [None] * len(ops))
+    st0 = np.zeros(1 << n, np.complex128)
+    st0[0] = 1
+    o = oracle.sv(n, np.complex128)
+    o.set_state(st0)
+    for op in ops:
+        o.apply(op["name"], op["wires"], False, op.get("params", ()))
+    ref = o.state()
+    sv = ops_module.StateVectorC64(n)
+    nk = sv.applyOperations(S, 12)
+    assert nk == len(S.block_plan(n, 6, False))  # the blocks path ran
+    assert_state(sv.state(), ref, np.complex64, what="c64 blocks by default")
+    lazy = ops_module.StateVectorC64(n)
+    for op in ops:
+        getattr(lazy, op["name"])(op["wires"], False, op.get("params", []))
+    assert_state(lazy.state(), ref, np.complex64, what="c64 lazy queue as blocks")
+    prev = ops_module.set_tc_dense(False)
+    try:
+        tiles = ops_module.StateVectorC64(n)
+        assert tiles.applyOperations(S, 12) != nk  # tile passes
+        assert_state(tiles.state(), ref, np.complex64, what="c64 tile passes")
+    finally:
+        ops_module.set_tc_dense(prev)

@@ -163,32 +163,29 @@ __device__ __forceinline__ u64 tile_base(const TcGeom &geom, u64 tile) {
     return base;
 }
 
-// Warp roles (288 threads, one CTA per SM):
-//   split warps 0-3: load a tile's amplitudes straight from global memory
+// Warp roles (544 threads, one CTA per SM):
+//   split warps 0-7: load a tile's amplitudes straight from global memory
 //     (the next tile's loads are in flight in registers while the current
 //     one is split), split them into the B operand of buffer t % 2;
-//   warp 8, one elected thread: issues the 48 MMAs of tile t into tensor
+//   warp 16, one elected thread: issues the 48 MMAs of tile t into tensor
 //     memory columns 64 (t % 2) .. + 63 and commits them to an mbarrier;
-//   epilogue warps 4-7 (one per tensor-memory lane quarter): read tile t's
-//     accumulator, stage it in shared memory over B of buffer t % 2 (its
-//     MMAs are complete) and store it coalesced.
+//   epilogue warps 8-15 (two per tensor-memory lane quarter, 32 columns
+//     each): read tile t's accumulator, stage it in shared memory over B of
+//     buffer t % 2 (its MMAs are complete) and store it coalesced.
 // B and the accumulator are double-buffered, so the split of tile t + 1, the
-// MMAs of tile t and the epilogue of tile t - 1 overlap.  (Eight split warps
-// with two tiles of loads in flight measured slower: 0.29-0.30 against
-// 0.27-0.29 ms for a 2^26-amplitude gate, the register budget of 416
-// threads forcing spills.)  Every hand-off is
+// MMAs of tile t and the epilogue of tile t - 1 overlap.  Every hand-off is
 // an mbarrier (B full, MMAs done, accumulator free, B free, stage written);
 // every wait is bounded, and a wait that runs out sets the CTA's abort flag
 // and the error word: all roles then leave their loops, the MMA thread waits
 // (bounded) for the MMAs it issued, and tensor memory is freed.
-constexpr int kWsSplitThreads = 128;
-constexpr int kWsEpiThreads = 128;
+constexpr int kWsSplitThreads = 256;
+constexpr int kWsEpiThreads = 256;
 constexpr int kWsThreads = kWsSplitThreads + kWsEpiThreads + 32;
-constexpr int kWsRows = 4096 / kWsSplitThreads; // amplitudes per split / epilogue thread and tile (32)
+constexpr int kWsRows = 4096 / kWsSplitThreads; // amplitudes per split / epilogue thread and tile (16)
 constexpr unsigned kWsBBytes = 3 * kTcBSplitBytes;  // one B buffer (three splits): 48 KiB
 constexpr unsigned kWsTmemCols = 128;               // two 128 x 64 FP32 accumulators
 enum WsBar { kBFull = 0, kMDone = 2, kTFree = 4, kBFree = 6, kEStage = 8, kNumWsBars = 9 };
-constexpr unsigned kWsTableBytes = 32 * 8 * 2 + 32 * 4 + 16;
+constexpr unsigned kWsTableBytes = 16;
 constexpr unsigned kWsSmemBytes = 3 * kTcASplitBytes + 2 * kWsBBytes + kWsTableBytes + kNumWsBars * 8 + 32;
 
 // bounded wait for the phase of `bar` with parity `phase`; false when the
@@ -218,9 +215,6 @@ __global__ void __launch_bounds__(kWsThreads, 1)
     // | mbarriers | tensor-memory address | abort flag
     unsigned char *A0 = smem;
     unsigned char *Bbuf = smem + 3 * kTcASplitBytes;
-    u64 *soff_r = reinterpret_cast<u64 *>(Bbuf + 2 * kWsBBytes);  // split: per-row global offsets
-    u64 *eoff_r = soff_r + 32;                                     // epilogue: per-row global offsets
-    unsigned *est_r = reinterpret_cast<unsigned *>(eoff_r + 32);   // epilogue: per-row stage positions
     unsigned long long *bars = reinterpret_cast<unsigned long long *>(Bbuf + 2 * kWsBBytes + kWsTableBytes);
     unsigned *tslot = reinterpret_cast<unsigned *>(bars + kNumWsBars);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tslot + 1);
@@ -246,14 +240,6 @@ __global__ void __launch_bounds__(kWsThreads, 1)
     for (unsigned i = tid; i < 3 * kTcASplitBytes / 16; i += kWsThreads) {
         reinterpret_cast<uint4 *>(smem)[i] = a_img[i];
     }
-    if (tid < 32) {
-        // split thread (warp w, lane l) row r: g = (l >> 2) | (w << 3) | ((r & 1) << 5),
-        // u = (l & 3) | ((r >> 1) << 2); the row part of its local index
-        soff_r[tid] = dep(geom.jj_of_u[(tid >> 1) << 2] | geom.jj_of_g[(tid & 1u) << 5]);
-        // epilogue thread e row r: local index jj = r * 128 + e
-        eoff_r[tid] = dep(tid << 7);
-        est_r[tid] = swz(tid << 7);
-    }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
                      "r"(kWsTmemCols)
@@ -278,17 +264,19 @@ __global__ void __launch_bounds__(kWsThreads, 1)
     const unsigned tmem = *tslot;
     const u64 stride = gridDim.x;
 
-    if (warp < 4) {
+    if (warp < kWsSplitThreads / 32) {
         // ---------------------------------------------------------------- split
+        // thread (warp w, lane l) row r: group g = (l >> 2) | (w << 3),
+        // member u = (l & 3) | (r << 2)
         const unsigned g0 = (lane >> 2) | (warp << 3);
         const u64 off_t = dep(geom.jj_of_u[lane & 3u] | geom.jj_of_g[g0]);
-        const unsigned b_t = (warp * 16u) * 128u + lane * 4u; // kmajor_off(g0, 2 (lane & 3))
+        const unsigned b_t = (warp * 16u) * 128u + lane * 4u; // kmajor_off(g, 2 (lane & 3)); row r adds r * 128
         float2 cur[kWsRows], nxt[kWsRows];
         auto load = [&](float2 (&dst)[kWsRows], u64 tt) {
             const u64 base = tile_base(geom, tt) | off_t;
 #pragma unroll
             for (int r = 0; r < kWsRows; r++) {
-                dst[r] = __ldcs(&sv[base | soff_r[r]]);
+                dst[r] = __ldcs(&sv[base | geom.split_row_off[r]]);
             }
         };
         u64 tile = blockIdx.x;
@@ -307,7 +295,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 #pragma unroll
             for (int r = 0; r < kWsRows; r++) {
                 // (re, im) adjacent: k = 2u, 2u + 1 of group g
-                const unsigned o = b_t + ((static_cast<unsigned>(r & 1) * 64u + static_cast<unsigned>(r >> 1)) * 128u);
+                const unsigned o = b_t + static_cast<unsigned>(r) * 128u;
                 unsigned h, m, l;
                 split3x2(now[r].x, now[r].y, h, m, l);
                 *reinterpret_cast<unsigned *>(B0 + o) = h;
@@ -331,9 +319,11 @@ __global__ void __launch_bounds__(kWsThreads, 1)
             }
             tile += stride;
         }
-    } else if (warp < 8) {
+    } else if (warp < (kWsSplitThreads + kWsEpiThreads) / 32) {
         // ------------------------------------------------------------- epilogue
-        const unsigned ew = warp - 4, e = tid - kWsSplitThreads;
+        // two warps per tensor-memory lane quarter (warp % 4), each reading
+        // 32 of the 64 accumulator columns
+        const unsigned ew = warp % 4u, half = (warp - kWsSplitThreads / 32) / 4u, e = tid - kWsSplitThreads;
         const unsigned row = 32u * ew + lane; // accumulator row m: member m / 2, component m % 2
         const unsigned st_u = geom.st_of_u[row >> 1], comp = row & 1u;
         const u64 off_e = dep(e);
@@ -345,17 +335,15 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                 break;
             }
             tc_fence_after();
-            float d0[32], d1[32];
-            tc_ld(tmem + ((32u * ew) << 16) + 64u * b, d0);
-            tc_ld(tmem + ((32u * ew) << 16) + 64u * b + 32u, d1);
+            float d0[32];
+            tc_ld(tmem + ((32u * ew) << 16) + 64u * b + 32u * half, d0);
             tc_fence_before();
             mbar_arrive(smem_u32(&bars[kTFree + b])); // the accumulator may be overwritten
             // stage over B of this buffer (its MMAs are complete)
             float *st = reinterpret_cast<float *>(Bbuf + b * kWsBBytes);
 #pragma unroll
             for (int c = 0; c < 32; c++) {
-                st[2u * (st_u ^ geom.st_of_g[c]) + comp] = d0[c];
-                st[2u * (st_u ^ geom.st_of_g[32 + c]) + comp] = d1[c];
+                st[2u * (st_u ^ geom.st_of_g[32u * half + c]) + comp] = d0[c];
             }
             mbar_arrive(smem_u32(&bars[kEStage]));
             if (!ws_wait(smem_u32(&bars[kEStage]), t & 1u, abort_flag, err)) {
@@ -363,9 +351,9 @@ __global__ void __launch_bounds__(kWsThreads, 1)
             }
             const float2 *stage = reinterpret_cast<const float2 *>(st);
             const u64 base = tile_base(geom, tile) | off_e;
-#pragma unroll 8
+#pragma unroll
             for (int r = 0; r < kWsRows; r++) {
-                __stcs(&sv[base | eoff_r[r]], stage[st_e ^ est_r[r]]);
+                __stcs(&sv[base | geom.epi_row_off[r]], stage[st_e ^ geom.epi_row_st[r]]);
             }
             mbar_arrive(smem_u32(&bars[kBFree + b])); // the stage has been read
         }
@@ -515,6 +503,18 @@ bool tc_geom_for(int n, const int *bits6, TcGeom &g) {
     for (unsigned v = 0; v < 64; v++) {
         g.st_of_u[v] = static_cast<unsigned short>(swz(g.jj_of_u[v], g.hst));
         g.st_of_g[v] = static_cast<unsigned short>(swz(g.jj_of_g[v], g.hst));
+    }
+    auto dep = [&](unsigned jj) {
+        u64 o = 0;
+        for (int q = 0; q < kTcTileBits; q++) {
+            o |= static_cast<u64>((jj >> q) & 1u) << g.lbit[q];
+        }
+        return o;
+    };
+    for (unsigned r = 0; r < 16; r++) {
+        g.split_row_off[r] = dep(g.jj_of_u[r << 2]);
+        g.epi_row_off[r] = dep(r << 8);
+        g.epi_row_st[r] = static_cast<unsigned short>(swz(r << 8, g.hst));
     }
     return true;
 }

@@ -24,6 +24,13 @@ struct TcGeom {
     unsigned short hst[12];  // XOR mask of stage position per jj bit
     unsigned short st_of_u[64], st_of_g[64]; // swizzled stage positions of u and g alone
     unsigned short mat_of_u[64];             // row of the caller's matrix for member u
+    // per-row parts of the kernel's thread maps (256 split and 256 epilogue
+    // threads, 16 rows each): the full-index offsets of local index
+    // jj_of_u[r << 2] (split row r) and of r << 8 (epilogue row r), and the
+    // stage position of r << 8
+    u64 split_row_off[16];
+    u64 epi_row_off[16];
+    unsigned short epi_row_st[16];
 };
 
 // false when the register is too small (fewer than 12 qubits) or the bits

@@ -10,7 +10,8 @@ helpers.assert_state / assert_scalar, no multipliers).
 * the same circuit in the opt-in double-float passes, whose accuracy figure
   is printed and bounded separately;
 * config 3 (Rot + CNOT-range layers) at 20 qubits with its 200-term
-  Hamiltonian: the full adjoint Jacobian;
+  Hamiltonian: the full adjoint Jacobian (complex128; complex64 against the
+  complex128 oracle at the complex64 tolerance);
 * samples at 20 qubits, all wires and a wire subset: exactly the oracle's
   integers for the same seed.
 
@@ -144,6 +145,31 @@ def test_config3_20q_adjoint_jacobian(ops_module, oracle):
     nr, pr = rel_errors(jac, ref, np.complex128)
     print(f"config-3 {N3}q Jacobian ({len(tp)} params, 200 terms): norm-rel {nr:.3e}, per-entry {pr:.3e}")
     assert_state(np.ravel(jac), np.ravel(ref), np.complex128, what="config-3 Jacobian")
+
+
+def test_config3_20q_adjoint_jacobian_c64(ops_module, oracle):
+    # the complex64 sweep against the oracle's complex128 Jacobian, at the
+    # complex64 tolerance
+    from oracle.pyoracle import pauli_sum_spec
+
+    circuit, ham = config3(N3, 12, seed=1003, nterms=200)
+    S = ops_module.OpsStructC64([o.name for o in circuit], [o.params for o in circuit], [o.wires for o in circuit],
+                                [False] * len(circuit), [None] * len(circuit))
+    tp = list(range(sum(1 for o in circuit if o.params)))
+    H = _ham_obs(ops_module, np.complex64, ham)
+    jac = np.asarray(ops_module.AdjointJacobianC64()(ops_module.StateVectorC64(N3), [H], S, tp, True))
+    spec = [pauli_sum_spec(ham.terms())]
+    ops = [o.as_dict() for o in circuit]
+    ref = oracle.sv(N3, np.complex128).adjoint(ops, spec, tp, apply_ops=True)[0]
+    ref64 = oracle.sv(N3, np.complex64).adjoint(ops, spec, tp, apply_ops=True)[0]
+    nr, pr = rel_errors(jac, ref, np.complex64)
+    o_nr, o_pr = rel_errors(ref64, ref, np.complex64)
+    print(f"config-3 {N3}q complex64 Jacobian vs the complex128 one: GPU {nr:.3e} / {pr:.3e}, "
+          f"oracle complex64 {o_nr:.3e} / {o_pr:.3e}")
+    # as for config 1: within the tolerance norm-wise, and per entry no less
+    # accurate than the reference algorithm's own complex64 result
+    assert nr <= 1e-5
+    assert pr <= max(1e-5, 2.0 * o_pr)
 
 
 @pytest.mark.parametrize("dt", [np.complex128, np.complex64])

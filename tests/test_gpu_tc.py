@@ -1,7 +1,7 @@
-"""Dense complex64 gates on six wires on the tensor cores (tcgen05, split-TF32
-operands) against the oracle and against the CUDA-core kernel: wires on
-low, high and mixed index bits, registers of 12 to 18 qubits, inverse
-matrices, and a run of several blocks."""
+"""Dense complex64 gates on six wires on the tensor cores (tcgen05, FP32
+operands split into three BF16 parts) against the oracle and against the
+CUDA-core kernel: wires on low, high and mixed index bits, registers of 12
+to 24 qubits, inverse matrices, and a run of several blocks."""
 import numpy as np
 import pytest
 
@@ -50,4 +50,27 @@ def test_dense6_tensor_cores_vs_cuda_cores(ops_module):
         finally:
             ops_module.set_tc_dense(prev)
     assert_state(out[True], out[False], np.complex64, what="tensor cores vs CUDA cores")
+    assert not np.array_equal(out[True], out[False])
+
+
+@pytest.mark.parametrize("wires", [[18, 19, 20, 21, 22, 23], [0, 1, 2, 3, 4, 5], [23, 0, 11, 5, 17, 2]])
+def test_dense6_tensor_cores_24_qubits(ops_module, wires):
+    # 4096 tiles (many per CTA, every pipeline stage of the kernel in steady
+    # state): the tensor-core result equals the CUDA-core kernel's within the
+    # complex64 tolerance
+    n = 24
+    rng = np.random.default_rng(seed_of("tc6-24", tuple(wires)))
+    st = rand_state(rng, n, np.complex64)
+    U = rand_unitary(rng, 6)
+    out = {}
+    for tc in (True, False):
+        prev = ops_module.set_tc_dense(tc)
+        try:
+            sv = ops_module.StateVectorC64(n)
+            sv.updateData(st)
+            sv.applyMatrix(U, wires, False)
+            out[tc] = sv.state()
+        finally:
+            ops_module.set_tc_dense(prev)
+    assert_state(out[True], out[False], np.complex64, what=f"24 qubits wires={wires}")
     assert not np.array_equal(out[True], out[False])

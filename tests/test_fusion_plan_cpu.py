@@ -65,3 +65,18 @@ def test_wide_dense_matrix_runs_unfused(ops_module):
     unfused = [p for p in plan if not p["tile"]]
     assert len(unfused) == 1
     assert plan[0]["tile"] and plan[-1]["tile"]
+
+
+def test_diagonals_merge_across_a_cnot_chain(ops_module):
+    # the list schedule postpones diagonals until a gate needs them: in the
+    # config-0 ansatz (RX RY RZ per qubit, then a CNOT ring) the diagonal
+    # halves of a layer's rotations merge into about two groups per layer
+    # and pass, where per-level placement staggered them along the chain
+    # (the 22-qubit config-2 circuits went from 110 to 66 merged diagonals)
+    n, layers = 14, 8
+    circuit = [op.as_dict() for op in config0(n, layers, seed=7)]
+    plan = struct(ops_module, circuit).fusion_plan(n, 11)
+    rotations = sum(p["rotations"] for p in plan)
+    diagonals = sum(p["diagonals"] for p in plan)
+    assert rotations == n * layers  # RX RY RZ merge into one rotation per qubit and layer
+    assert diagonals <= 2 * layers + 2 * len(plan), (diagonals, len(plan))

@@ -80,3 +80,19 @@ def test_diagonals_merge_across_a_cnot_chain(ops_module):
     diagonals = sum(p["diagonals"] for p in plan)
     assert rotations == n * layers  # RX RY RZ merge into one rotation per qubit and layer
     assert diagonals <= 2 * layers + 2 * len(plan), (diagonals, len(plan))
+
+
+@pytest.mark.parametrize("n", [10, 11, 12])
+def test_register_of_one_tile_runs_on_chip(ops_module, n):
+    # a register no wider than its tile keeps every gate tile-local: each
+    # pass is one register-kernel launch over the whole register, and the
+    # pass count is set only by the 192 op records a pass stages
+    from lightning_gb300.workloads import config2
+    circuits = [c for c in config2(256, seed=1002) if c.n == n][:8]
+    assert circuits
+    for c in circuits:
+        ops = [op.as_dict() for op in c.ops]
+        plan = struct(ops_module, ops).fusion_plan(n, n)
+        assert all(p["tile"] and p["register_kernel"] and p["t"] == n for p in plan)
+        assert 1 <= len(plan) <= 3
+        assert sum(p["ops"] for p in plan) <= 192 * len(plan)

@@ -34,10 +34,13 @@
 #ifndef PL_GB300_HPP
 #define PL_GB300_HPP
 
+#include <algorithm>
+#include <cmath>
 #include <complex>
 #include <cstddef>
 #include <cstdint>
 #include <exception>
+#include <numeric>
 #include <memory>
 #include <optional>
 #include <random>
@@ -95,6 +98,97 @@ inline bool has_gate_op(const std::string &name) {
         return s;
     }();
     return names.count(name) != 0;
+}
+
+/* Eigen-decomposition of a Hermitian matrix (row-major, dim x dim) by the
+ * cyclic Jacobi method (Golub and Van Loan, Matrix Computations, 4th ed.,
+ * section 8.5), carried to complex Hermitian matrices by a phase that makes
+ * each pivot real: with a_pq = r e^{i phi}, G = diag(1, e^{-i phi}) J(c, s)
+ * zeroes a_pq in G^H A G, (c, s) the real symmetric Jacobi rotation of
+ * [[a_pp, r], [r, a_qq]].  Returns the eigenvalues ascending in w and the
+ * matching orthonormal eigenvectors as the columns of v (row-major).  Used for
+ * the shot-based measurement of Hermitian observables, whose matrices span a
+ * few wires. */
+inline void hermitian_eigh(std::vector<std::complex<double>> a, std::size_t dim, std::vector<double> &w,
+                           std::vector<std::complex<double>> &v) {
+    using C = std::complex<double>;
+    if (a.size() != dim * dim) {
+        throw LightningException("hermitian_eigh: the matrix must be dim x dim");
+    }
+    std::vector<C> vv(dim * dim, C{0.0, 0.0});
+    for (std::size_t i = 0; i < dim; i++) {
+        vv[i * dim + i] = 1.0;
+    }
+    double total = 0.0;
+    for (const C &x : a) {
+        total += std::norm(x);
+    }
+    auto off_diagonal = [&] {
+        double s = 0.0;
+        for (std::size_t i = 0; i < dim; i++) {
+            for (std::size_t j = 0; j < dim; j++) {
+                s += i != j ? std::norm(a[i * dim + j]) : 0.0;
+            }
+        }
+        return s;
+    };
+    for (int sweep = 0; sweep < 64 && total > 0.0 && off_diagonal() > 1e-32 * total; sweep++) {
+        for (std::size_t p = 0; p + 1 < dim; p++) {
+            for (std::size_t q = p + 1; q < dim; q++) {
+                const C apq = a[p * dim + q];
+                const double r = std::abs(apq);
+                if (r <= 1e-300) {
+                    continue;
+                }
+                const C ph = apq / r;
+                const double tau = (a[q * dim + q].real() - a[p * dim + p].real()) / (2.0 * r);
+                const double t = (tau >= 0.0 ? 1.0 : -1.0) / (std::abs(tau) + std::sqrt(1.0 + tau * tau));
+                const double c = 1.0 / std::sqrt(1.0 + t * t), s = t * c;
+                const C g_qp = -s * std::conj(ph), g_qq = c * std::conj(ph); // G: (p,p) c, (p,q) s
+                for (std::size_t k = 0; k < dim; k++) {                      // A <- A G, V <- V G
+                    for (C *m : {a.data(), vv.data()}) {
+                        const C xp = m[k * dim + p], xq = m[k * dim + q];
+                        m[k * dim + p] = c * xp + g_qp * xq;
+                        m[k * dim + q] = s * xp + g_qq * xq;
+                    }
+                }
+                for (std::size_t k = 0; k < dim; k++) { // A <- G^H A
+                    const C xp = a[p * dim + k], xq = a[q * dim + k];
+                    a[p * dim + k] = c * xp + std::conj(g_qp) * xq;
+                    a[q * dim + k] = s * xp + std::conj(g_qq) * xq;
+                }
+                a[p * dim + q] = a[q * dim + p] = C{0.0, 0.0};
+            }
+        }
+    }
+    std::vector<std::size_t> order(dim);
+    std::iota(order.begin(), order.end(), std::size_t{0});
+    std::stable_sort(order.begin(), order.end(),
+                     [&](std::size_t i, std::size_t j) { return a[i * dim + i].real() < a[j * dim + j].real(); });
+    w.resize(dim);
+    v.assign(dim * dim, C{0.0, 0.0});
+    for (std::size_t k = 0; k < dim; k++) {
+        w[k] = a[order[k] * dim + order[k]].real();
+        for (std::size_t i = 0; i < dim; i++) {
+            v[i * dim + k] = vv[i * dim + order[k]];
+        }
+    }
+}
+
+/* kron of eigenvalue lists, first list most significant */
+template <class T> std::vector<T> kron_values(const std::vector<std::vector<T>> &lists) {
+    std::vector<T> out{T{1}};
+    for (const auto &l : lists) {
+        std::vector<T> next;
+        next.reserve(out.size() * l.size());
+        for (const T x : out) {
+            for (const T y : l) {
+                next.push_back(x * y);
+            }
+        }
+        out.swap(next);
+    }
+    return out;
 }
 } // namespace detail
 
@@ -330,6 +424,18 @@ template <class StateVectorT> class Observable {
         buf.resize(std::char_traits<char>::length(buf.c_str()));
         return buf;
     }
+    /* Observable::applyInPlaceShots (Observables.hpp:76): rotates `sv` into
+     * the observable's eigenbasis and returns, per factor, its eigenvalues
+     * and the wires to sample (shot-based expval / var / probs) */
+    virtual void applyInPlaceShots([[maybe_unused]] StateVectorT &sv,
+                                   [[maybe_unused]] std::vector<std::vector<PrecisionT>> &eigenValues,
+                                   [[maybe_unused]] std::vector<std::size_t> &ob_wires) const {
+        throw LightningException("This observable does not support shot measurement.");
+    }
+    /* the terms of a tensor product or a Hamiltonian, and a Hamiltonian's
+     * coefficients (Observables.hpp:94-104) */
+    [[nodiscard]] virtual auto getObs() const -> std::vector<std::shared_ptr<Observable<StateVectorT>>> { return {}; }
+    [[nodiscard]] virtual auto getCoeffs() const -> std::vector<PrecisionT> { return {}; }
 
   protected:
     Observable() = default;
@@ -341,18 +447,41 @@ template <class StateVectorT> class Observable {
 
 template <class StateVectorT> class NamedObs final : public Observable<StateVectorT> {
   public:
-    NamedObs(std::string obs_name, std::vector<std::size_t> wires) {
+    using PrecisionT = typename StateVectorT::PrecisionType;
+    NamedObs(std::string obs_name, std::vector<std::size_t> wires) : name_{std::move(obs_name)}, wires_{wires} {
         const auto w = detail::wires64(wires);
         plgb_obs *h = nullptr;
-        detail::check(plgb_obs_named(obs_name.c_str(), w.data(), static_cast<int>(w.size()), &h));
+        detail::check(plgb_obs_named(name_.c_str(), w.data(), static_cast<int>(w.size()), &h));
         this->adopt(h);
     }
+    /* Observables.hpp:176-202: X by H, Y by Z S H, Hadamard by RY(-pi/4);
+     * eigenvalues (1, -1), Identity (1, 1) */
+    void applyInPlaceShots(StateVectorT &sv, std::vector<std::vector<PrecisionT>> &eigenValues,
+                           std::vector<std::size_t> &ob_wires) const override {
+        ob_wires.assign(1, wires_.at(0));
+        eigenValues.clear();
+        if (name_ == "PauliX") {
+            sv.applyOperation("Hadamard", wires_, false);
+        } else if (name_ == "PauliY") {
+            sv.applyOperations({"PauliZ", "S", "Hadamard"}, {wires_, wires_, wires_}, {false, false, false});
+        } else if (name_ == "Hadamard") {
+            sv.applyOperation("RY", wires_, false, {static_cast<PrecisionT>(-std::acos(-1.0) / 4.0)});
+        } else if (name_ != "PauliZ" && name_ != "Identity") {
+            throw LightningException("Provided NamedObs does not support shot measurement.");
+        }
+        eigenValues.push_back(name_ == "Identity" ? std::vector<PrecisionT>{1, 1} : std::vector<PrecisionT>{1, -1});
+    }
+
+  private:
+    std::string name_;
+    std::vector<std::size_t> wires_;
 };
 
 template <class StateVectorT> class HermitianObs final : public Observable<StateVectorT> {
   public:
+    using PrecisionT = typename StateVectorT::PrecisionType;
     using ComplexT = typename StateVectorT::ComplexT;
-    HermitianObs(std::vector<ComplexT> matrix, std::vector<std::size_t> wires) {
+    HermitianObs(std::vector<ComplexT> matrix, std::vector<std::size_t> wires) : matrix_{matrix}, wires_{wires} {
         if (matrix.size() != (std::size_t{1} << (2 * wires.size()))) {
             throw LightningException("The size of matrix does not match with the given number of wires");
         }
@@ -362,11 +491,40 @@ template <class StateVectorT> class HermitianObs final : public Observable<State
         detail::check(plgb_obs_hermitian(m.data(), w.data(), static_cast<int>(w.size()), &h));
         this->adopt(h);
     }
+    /* Observables.hpp:290-302: the matrix's eigenvectors rotated onto the
+     * computational basis (U = V^H on the observable's wires), eigenvalues
+     * ascending; the decomposition is computed once */
+    void applyInPlaceShots(StateVectorT &sv, std::vector<std::vector<PrecisionT>> &eigenValues,
+                           std::vector<std::size_t> &ob_wires) const override {
+        if (eigen_values_.empty()) {
+            const std::size_t dim = std::size_t{1} << wires_.size();
+            std::vector<std::complex<double>> a(matrix_.begin(), matrix_.end()), vecs;
+            std::vector<double> vals;
+            detail::hermitian_eigh(a, dim, vals, vecs);
+            unitary_.resize(dim * dim);
+            for (std::size_t i = 0; i < dim; i++) {
+                for (std::size_t j = 0; j < dim; j++) {
+                    unitary_[i * dim + j] = static_cast<ComplexT>(std::conj(vecs[j * dim + i]));
+                }
+            }
+            eigen_values_.assign(vals.begin(), vals.end());
+        }
+        ob_wires = wires_;
+        sv.applyMatrix(unitary_, wires_);
+        eigenValues.assign(1, eigen_values_);
+    }
+
+  private:
+    std::vector<ComplexT> matrix_;
+    std::vector<std::size_t> wires_;
+    mutable std::vector<PrecisionT> eigen_values_;
+    mutable std::vector<ComplexT> unitary_;
 };
 
 template <class StateVectorT> class TensorProdObs final : public Observable<StateVectorT> {
   public:
-    explicit TensorProdObs(std::vector<std::shared_ptr<Observable<StateVectorT>>> obs) {
+    using PrecisionT = typename StateVectorT::PrecisionType;
+    explicit TensorProdObs(std::vector<std::shared_ptr<Observable<StateVectorT>>> obs) : obs_{obs} {
         std::vector<plgb_obs *> hs;
         for (const auto &o : obs) {
             hs.push_back(o->handle());
@@ -379,12 +537,40 @@ template <class StateVectorT> class TensorProdObs final : public Observable<Stat
         -> std::shared_ptr<TensorProdObs<StateVectorT>> {
         return std::make_shared<TensorProdObs<StateVectorT>>(std::vector(obs));
     }
+    [[nodiscard]] auto getObs() const -> std::vector<std::shared_ptr<Observable<StateVectorT>>> override {
+        return obs_;
+    }
+    /* Observables.hpp:428-448: every factor rotated in turn; a multi-wire
+     * Hermitian factor contributes all of its wires and its whole eigenvalue
+     * list (the reference keeps its first wire only) */
+    void applyInPlaceShots(StateVectorT &sv, std::vector<std::vector<PrecisionT>> &eigenValues,
+                           std::vector<std::size_t> &ob_wires) const override {
+        eigenValues.clear();
+        ob_wires.clear();
+        for (const auto &ob : obs_) {
+            if (!ob->getCoeffs().empty() || ob->getObsName().find("Hamiltonian") != std::string::npos) {
+                throw LightningException("Hamiltonian observables as a term of an TensorProd observable do not "
+                                         "support shot measurement.");
+            }
+        }
+        for (const auto &ob : obs_) {
+            std::vector<std::vector<PrecisionT>> ev;
+            std::vector<std::size_t> w;
+            ob->applyInPlaceShots(sv, ev, w);
+            ob_wires.insert(ob_wires.end(), w.begin(), w.end());
+            eigenValues.push_back(detail::kron_values(ev));
+        }
+    }
+
+  private:
+    std::vector<std::shared_ptr<Observable<StateVectorT>>> obs_;
 };
 
 template <class StateVectorT> class Hamiltonian final : public Observable<StateVectorT> {
   public:
     using PrecisionT = typename StateVectorT::PrecisionType;
-    Hamiltonian(std::vector<PrecisionT> coeffs, std::vector<std::shared_ptr<Observable<StateVectorT>>> obs) {
+    Hamiltonian(std::vector<PrecisionT> coeffs, std::vector<std::shared_ptr<Observable<StateVectorT>>> obs)
+        : coeffs_{coeffs}, obs_{obs} {
         if (coeffs.size() != obs.size()) {
             throw LightningException("Hamiltonian: the number of coefficients and observables must match");
         }
@@ -402,10 +588,19 @@ template <class StateVectorT> class Hamiltonian final : public Observable<StateV
         -> std::shared_ptr<Hamiltonian<StateVectorT>> {
         return std::make_shared<Hamiltonian<StateVectorT>>(std::vector(coeffs), std::vector(obs));
     }
+    [[nodiscard]] auto getObs() const -> std::vector<std::shared_ptr<Observable<StateVectorT>>> override {
+        return obs_;
+    }
+    [[nodiscard]] auto getCoeffs() const -> std::vector<PrecisionT> override { return coeffs_; }
+
+  private:
+    std::vector<PrecisionT> coeffs_;
+    std::vector<std::shared_ptr<Observable<StateVectorT>>> obs_;
 };
 
 template <class StateVectorT> class SparseHamiltonian final : public Observable<StateVectorT> {
   public:
+    using PrecisionT = typename StateVectorT::PrecisionType;
     using ComplexT = typename StateVectorT::ComplexT;
     /* CSR over the listed wires: data, column indices, row offsets */
     SparseHamiltonian(std::vector<ComplexT> data, std::vector<std::size_t> indices, std::vector<std::size_t> offsets,
@@ -418,6 +613,12 @@ template <class StateVectorT> class SparseHamiltonian final : public Observable<
                                                   static_cast<int>(w.size()), &h));
         this->adopt(h);
     }
+    /* MeasurementsBase.hpp:164-167 */
+    void applyInPlaceShots([[maybe_unused]] StateVectorT &sv,
+                           [[maybe_unused]] std::vector<std::vector<PrecisionT>> &eigenValues,
+                           [[maybe_unused]] std::vector<std::size_t> &ob_wires) const override {
+        throw LightningException("SparseHamiltonian observables do not support shot measurement.");
+    }
 };
 
 /* ---- measurements (MeasurementsLQubit.hpp:73-768) ---- */
@@ -426,7 +627,7 @@ template <class StateVectorT> class MeasurementsGB300 {
     using PrecisionT = typename StateVectorT::PrecisionType;
     using ComplexT = typename StateVectorT::ComplexT;
 
-    explicit MeasurementsGB300(const StateVectorT &statevector) : sv_{statevector.handle()} {}
+    explicit MeasurementsGB300(const StateVectorT &statevector) : svp_{&statevector}, sv_{statevector.handle()} {}
 
     /* MeasurementsBase::setSeed: samples drawn after it use this seed */
     void setSeed(std::optional<std::size_t> seed = std::nullopt) { seed_ = seed; }
@@ -492,6 +693,117 @@ template <class StateVectorT> class MeasurementsGB300 {
     auto generate_samples(std::size_t num_samples) -> std::vector<std::size_t> {
         return samples_(nullptr, -1, num_qubits_(), num_samples);
     }
+    /* Metropolis-Hastings samples, kernel "Local" or "NonZeroRandom"
+     * (MeasurementsLQubit.hpp:551-594): num_samples x num_qubits bits */
+    auto generate_samples_metropolis(const std::string &kernelname, std::size_t num_burnin,
+                                     std::size_t num_samples) -> std::vector<std::size_t> {
+        const uint64_t seed = seed_.has_value() ? static_cast<uint64_t>(*seed_) : std::random_device{}();
+        std::vector<int64_t> out(num_samples * num_qubits_());
+        detail::check(plgb_meas_generate_mcmc_samples(sv_, kernelname.c_str(), static_cast<int64_t>(num_burnin),
+                                                      static_cast<int64_t>(num_samples), seed, out.data()));
+        return {out.begin(), out.end()};
+    }
+    auto sample(const std::size_t &num_shots) -> std::vector<std::size_t> { return generate_samples(num_shots); }
+
+    /* ---- shot-based measurements (MeasurementsBase.hpp:150-420) ---- */
+    /* probabilities of the sampled basis states over `wires` */
+    auto probs(const std::vector<std::size_t> &wires, std::size_t num_shots) -> std::vector<PrecisionT> {
+        const std::size_t n = num_qubits_();
+        const auto smp = generate_samples(num_shots);
+        std::vector<std::size_t> hits(std::size_t{1} << wires.size(), 0);
+        for (std::size_t i = 0; i < num_shots; i++) {
+            std::size_t idx = 0;
+            for (const std::size_t w : wires) {
+                idx = (idx << 1) | smp[i * n + w];
+            }
+            hits[idx]++;
+        }
+        std::vector<PrecisionT> out(hits.size());
+        for (std::size_t k = 0; k < hits.size(); k++) {
+            out[k] = static_cast<PrecisionT>(hits[k]) / static_cast<PrecisionT>(num_shots);
+        }
+        return out;
+    }
+    auto probs(std::size_t num_shots) -> std::vector<PrecisionT> {
+        std::vector<std::size_t> all(num_qubits_());
+        std::iota(all.begin(), all.end(), std::size_t{0});
+        return probs(all, num_shots);
+    }
+    /* eigenvalue of the observable for each sampled shot: the state copied,
+     * rotated into the observable's eigenbasis, the whole register sampled
+     * with this object's seed (MeasurementsBase.hpp:195-225, 477-518) */
+    auto measure_with_samples(const Observable<StateVectorT> &obs, const std::size_t &num_shots,
+                              const std::vector<std::size_t> &shot_range) -> std::vector<PrecisionT> {
+        StateVectorT rotated(*svp_);
+        std::vector<std::vector<PrecisionT>> eigen_values;
+        std::vector<std::size_t> obs_wires;
+        obs.applyInPlaceShots(rotated, eigen_values, obs_wires);
+        MeasurementsGB300<StateVectorT> m(rotated);
+        m.setSeed(seed_);
+        const std::size_t n = num_qubits_();
+        const auto smp = m.generate_samples(num_shots);
+        const auto values = detail::kron_values(eigen_values);
+        std::vector<std::size_t> shots = shot_range;
+        if (shots.empty()) {
+            shots.resize(num_shots);
+            std::iota(shots.begin(), shots.end(), std::size_t{0});
+        }
+        std::vector<PrecisionT> out;
+        out.reserve(shots.size());
+        for (const std::size_t i : shots) {
+            if (i >= num_shots) {
+                throw LightningException("shot_range holds a shot index beyond num_shots");
+            }
+            std::size_t idx = 0;
+            for (const std::size_t w : obs_wires) {
+                idx = (idx << 1) | smp[i * n + w];
+            }
+            out.push_back(values.at(idx));
+        }
+        return out;
+    }
+    /* a Hamiltonian term by term, its terms and other observables by
+     * sampling (MeasurementsBase.hpp:159-183) */
+    auto expval(const Observable<StateVectorT> &obs, const std::size_t &num_shots,
+                const std::vector<std::size_t> &shot_range = {}) -> PrecisionT {
+        if (dynamic_cast<const SparseHamiltonian<StateVectorT> *>(&obs) != nullptr) {
+            throw LightningException("SparseHamiltonian observables do not support shot measurement.");
+        }
+        if (const auto *h = dynamic_cast<const Hamiltonian<StateVectorT> *>(&obs)) {
+            const auto coeffs = h->getCoeffs();
+            const auto terms = h->getObs();
+            PrecisionT result{0};
+            for (std::size_t k = 0; k < coeffs.size(); k++) {
+                result += coeffs[k] * expval(*terms[k], num_shots, shot_range);
+            }
+            return result;
+        }
+        const auto v = measure_with_samples(obs, num_shots, shot_range);
+        return std::accumulate(v.begin(), v.end(), PrecisionT{0}) / static_cast<PrecisionT>(v.size());
+    }
+    /* a Hamiltonian as sum_k c_k^2 var(term_k), as the reference computes it
+     * (MeasurementsBase.hpp:239-268) */
+    auto var(const Observable<StateVectorT> &obs, const std::size_t &num_shots) -> PrecisionT {
+        if (dynamic_cast<const SparseHamiltonian<StateVectorT> *>(&obs) != nullptr) {
+            throw LightningException("SparseHamiltonian observables do not support shot measurement.");
+        }
+        if (const auto *h = dynamic_cast<const Hamiltonian<StateVectorT> *>(&obs)) {
+            const auto coeffs = h->getCoeffs();
+            const auto terms = h->getObs();
+            PrecisionT result{0};
+            for (std::size_t k = 0; k < coeffs.size(); k++) {
+                result += coeffs[k] * coeffs[k] * var(*terms[k], num_shots);
+            }
+            return result;
+        }
+        const auto v = measure_with_samples(obs, num_shots, {});
+        const auto len = static_cast<PrecisionT>(v.size());
+        const PrecisionT mean = std::accumulate(v.begin(), v.end(), PrecisionT{0}) / len;
+        const PrecisionT mean_sq =
+            std::accumulate(v.begin(), v.end(), PrecisionT{0}, [](PrecisionT a, PrecisionT x) { return a + x * x; }) /
+            len;
+        return mean_sq - mean * mean;
+    }
 
   private:
     std::size_t num_qubits_() const {
@@ -512,6 +824,7 @@ template <class StateVectorT> class MeasurementsGB300 {
         detail::check(plgb_meas_generate_samples(sv_, w, nw, static_cast<int64_t>(shots), seed, out.data()));
         return {out.begin(), out.end()};
     }
+    const StateVectorT *svp_;
     plgb_sv *sv_;
     std::optional<std::size_t> seed_;
 };

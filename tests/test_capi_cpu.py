@@ -92,3 +92,15 @@ def test_cpp_api_header_compiles():
 
     proc = subprocess.run(compile_cmd(REPO / "unused", syntax_only=True), capture_output=True, text=True)
     assert proc.returncode == 0, proc.stderr
+
+
+def test_catalyst_device_links_against_the_backend(tmp_path):
+    # the Catalyst device test program links against libplgb300.so (every C
+    # ABI entry point the device calls is exported); it runs under -m gpu
+    import subprocess
+
+    from cpp_build import CPP, compile_cmd
+
+    proc = subprocess.run(compile_cmd(tmp_path / "catalyst_link", sources=(CPP / "test_catalyst_device.cpp",)),
+                          capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr

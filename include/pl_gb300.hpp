@@ -47,6 +47,7 @@
 #include <span>
 #include <string>
 #include <type_traits>
+#include <unordered_map>
 #include <unordered_set>
 #include <utility>
 #include <vector>
@@ -781,6 +782,47 @@ template <class StateVectorT> class MeasurementsGB300 {
         const auto v = measure_with_samples(obs, num_shots, shot_range);
         return std::accumulate(v.begin(), v.end(), PrecisionT{0}) / static_cast<PrecisionT>(v.size());
     }
+    /* eigenvalues of the observable drawn in num_shots shots
+     * (MeasurementsBase.hpp:382-391) */
+    auto sample(const Observable<StateVectorT> &obs, const std::size_t &num_shots) -> std::vector<PrecisionT> {
+        no_hamiltonian_(obs);
+        return measure_with_samples(obs, num_shots, {});
+    }
+    /* eigenvalue -> occurrences, and basis state -> occurrences
+     * (MeasurementsBase.hpp:411-460) */
+    auto counts(const Observable<StateVectorT> &obs, const std::size_t &num_shots)
+        -> std::unordered_map<PrecisionT, std::size_t> {
+        std::unordered_map<PrecisionT, std::size_t> out;
+        for (const PrecisionT v : sample(obs, num_shots)) {
+            out[v]++;
+        }
+        return out;
+    }
+    auto counts(const std::size_t &num_shots) -> std::unordered_map<std::size_t, std::size_t> {
+        const std::size_t n = num_qubits_();
+        const auto smp = generate_samples(num_shots);
+        std::unordered_map<std::size_t, std::size_t> out;
+        for (std::size_t s = 0; s < num_shots; s++) {
+            std::size_t idx = 0;
+            for (std::size_t w = 0; w < n; w++) {
+                idx = (idx << 1) | smp[s * n + w];
+            }
+            out[idx]++;
+        }
+        return out;
+    }
+    /* probabilities of the observable's eigenbasis states over its wires,
+     * analytic or from num_shots samples (MeasurementsBase.hpp:283-318) */
+    auto probs(const Observable<StateVectorT> &obs, std::size_t num_shots = 0) -> std::vector<PrecisionT> {
+        no_hamiltonian_(obs);
+        StateVectorT rotated(*svp_);
+        std::vector<std::vector<PrecisionT>> eigen_values;
+        std::vector<std::size_t> obs_wires;
+        obs.applyInPlaceShots(rotated, eigen_values, obs_wires);
+        MeasurementsGB300<StateVectorT> m(rotated);
+        m.setSeed(seed_);
+        return num_shots > 0 ? m.probs(obs_wires, num_shots) : m.probs(obs_wires);
+    }
     /* a Hamiltonian as sum_k c_k^2 var(term_k), as the reference computes it
      * (MeasurementsBase.hpp:239-268) */
     auto var(const Observable<StateVectorT> &obs, const std::size_t &num_shots) -> PrecisionT {
@@ -806,6 +848,12 @@ template <class StateVectorT> class MeasurementsGB300 {
     }
 
   private:
+    static void no_hamiltonian_(const Observable<StateVectorT> &obs) {
+        if (dynamic_cast<const Hamiltonian<StateVectorT> *>(&obs) != nullptr ||
+            dynamic_cast<const SparseHamiltonian<StateVectorT> *>(&obs) != nullptr) {
+            throw LightningException("Hamiltonian and Sparse Hamiltonian do not support samples().");
+        }
+    }
     std::size_t num_qubits_() const {
         int n = 0;
         detail::check(plgb_sv_num_qubits(sv_, &n));

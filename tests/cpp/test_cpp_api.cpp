@@ -168,6 +168,103 @@ template <class P> int run(double tol) {
     expect(rc == 0, "oracle adjoint ran");
     expect(close_vec(std::vector<double>(jac.begin(), jac.end()), jref, tol), "adjoint Jacobian vs oracle");
 
+    // shot-based <H> (MeasurementsBase.hpp:159-183): each term's state copy is
+    // rotated into the term's eigenbasis and sampled with the seed, so the
+    // complex128 value equals the one formed from the oracle's samples of the
+    // same rotated states; complex64 within five standard errors
+    {
+        const int64_t shots = 4000;
+        m.setSeed(41);
+        const double e_shots = static_cast<double>(m.expval(*H, static_cast<size_t>(shots)));
+        struct Term {
+            double c;
+            std::vector<std::pair<const char *, int64_t>> factors;
+        };
+        const Term terms[3] = {{0.5, {{"PauliZ", 0}, {"PauliZ", 1}}}, {-1.25, {{"PauliY", 2}}}, {0.3, {{"PauliX", 9}}}};
+        double from_samples = 0.0;
+        for (const auto &t : terms) {
+            void *r = orc_sv_new(static_cast<int>(n), is_double);
+            orc_sv_set_state(r, ref.data());
+            for (const auto &[name, w] : t.factors) {
+                const int64_t ww[1] = {w};
+                const std::string s = name;
+                for (const char *g : s == "PauliX"   ? std::vector<const char *>{"Hadamard"}
+                                     : s == "PauliY" ? std::vector<const char *>{"PauliZ", "S", "Hadamard"}
+                                                     : std::vector<const char *>{}) {
+                    orc_sv_apply(r, g, nullptr, nullptr, 0, ww, 1, 0, nullptr, 0);
+                }
+            }
+            std::vector<int64_t> bits(static_cast<size_t>(shots) * n);
+            orc_samples(r, nullptr, -1, shots, 41, bits.data());
+            double acc = 0.0;
+            for (size_t s = 0; s < static_cast<size_t>(shots); s++) {
+                double v = 1.0;
+                for (const auto &[name, w] : t.factors) {
+                    v *= bits[s * n + static_cast<size_t>(w)] != 0 ? -1.0 : 1.0;
+                }
+                acc += v;
+            }
+            from_samples += t.c * acc / static_cast<double>(shots);
+            orc_sv_free(r);
+        }
+        if (is_double != 0) {
+            expect(std::abs(e_shots - from_samples) <= 1e-12, "shot-based expval(H) from the oracle's samples");
+        } else {
+            expect(std::abs(e_shots - h_ref) <= 5.0 * (0.5 + 1.25 + 0.3) / std::sqrt(static_cast<double>(shots)),
+                   "shot-based expval(H) within five standard errors");
+        }
+        const auto pz = m.probs({4, 1}, static_cast<size_t>(shots));
+        double total = 0.0;
+        for (const auto x : pz) {
+            total += static_cast<double>(x);
+        }
+        expect(pz.size() == 4 && std::abs(total - 1.0) < 1e-6 && std::abs(pz[0] - pref[0]) < 0.05,
+               "shot-based probs({4, 1})");
+        const double v_shots = static_cast<double>(m.var(*x9, static_cast<size_t>(shots)));
+        double vx = 0.0;
+        const int64_t w9[1] = {9};
+        orc_var_named(o, "PauliX", w9, 1, &vx);
+        expect(std::abs(v_shots - vx) < 0.1, "shot-based var(X9)");
+
+        // eigenbasis probabilities, eigenvalue counts and basis-state counts
+        double ex = 0.0;
+        orc_expval_named(o, "PauliX", w9, 1, &ex);
+        const auto px = m.probs(*x9);
+        expect(px.size() == 2 && close(px[0], (1.0 + ex) / 2, tol, 1.0) && close(px[1], (1.0 - ex) / 2, tol, 1.0),
+               "probs(X9) in its eigenbasis");
+        const auto cx = m.counts(*x9, static_cast<size_t>(shots));
+        size_t counted = 0;
+        for (const auto &[value, k] : cx) {
+            expect(value == P{1} || value == P{-1}, "X9 samples are eigenvalues");
+            counted += k;
+        }
+        expect(counted == static_cast<size_t>(shots), "counts(X9) adds up to the shots");
+        m.setSeed(43);
+        const auto basis = m.counts(static_cast<size_t>(shots));
+        m.setSeed(43);
+        const auto again = m.generate_samples(static_cast<size_t>(shots));
+        std::vector<size_t> tally(size_t{1} << n, 0);
+        for (size_t s = 0; s < static_cast<size_t>(shots); s++) {
+            size_t idx = 0;
+            for (size_t w = 0; w < n; w++) {
+                idx = (idx << 1) | again[s * n + w];
+            }
+            tally[idx]++;
+        }
+        bool same_counts = true;
+        for (const auto &[idx, k] : basis) {
+            same_counts = same_counts && tally[idx] == k;
+        }
+        expect(same_counts && !basis.empty(), "counts(shots) tallies the seeded samples");
+        bool refused = false;
+        try {
+            (void)m.probs(*H);
+        } catch (const LightningException &e) {
+            refused = std::string(e.what()).find("do not support samples()") != std::string::npos;
+        }
+        expect(refused, "probs(Hamiltonian) is refused");
+    }
+
     bool threw = false;
     try {
         sv.applyOperation("RX", {0}, {true}, {0}, false, {static_cast<P>(0.1)});

@@ -296,9 +296,19 @@ class QubitMap {
 /* Purity Tr(rho_S^2) of the reduced state of the wires in `subset` of a
  * (possibly unnormalised) register held on the host: rho_S = sum over the
  * other wires' basis states e of |psi_e><psi_e| / <psi|psi>, accumulated in
- * one pass over the amplitudes (dim(S)^2 per amplitude). */
+ * one pass over the amplitudes (dim(S) operations per amplitude).  A pure
+ * state's two parts have the same purity, so the smaller part is used. */
 inline double subsystem_purity(const std::vector<std::complex<double>> &psi, std::size_t num_qubits,
-                               const std::vector<std::size_t> &subset) {
+                               std::vector<std::size_t> subset) {
+    if (2 * subset.size() > num_qubits) {
+        std::vector<std::size_t> other;
+        for (std::size_t w = 0; w < num_qubits; w++) {
+            if (std::find(subset.begin(), subset.end(), w) == subset.end()) {
+                other.push_back(w);
+            }
+        }
+        subset.swap(other);
+    }
     const std::size_t k = subset.size(), dim = std::size_t{1} << k;
     std::vector<std::size_t> bit(k);
     std::size_t mask = 0;

@@ -98,6 +98,7 @@ void purity() {
     bell[5] = s;
     expect(std::abs(subsystem_purity(bell, 3, {2}) - 0.5) < 1e-14, "Bell pair: purity 1/2");
     expect(std::abs(subsystem_purity(bell, 3, {1}) - 1.0) < 1e-14, "spectator wire is pure");
+    expect(std::abs(subsystem_purity(bell, 3, {0, 1}) - 0.5) < 1e-14, "the larger part by its complement");
     // unnormalised input is normalised first
     for (auto &x : bell) {
         x *= 3.0;
